@@ -1,0 +1,123 @@
+/*
+ * sdim_gb300 C ABI: the GB300 stabilizer-tableau engine behind sdim's
+ * prime-dimension tableau path.
+ *
+ * The reference (events555/sdim) is pure Python; its tableau path is the
+ * per-shot loop Program._simulate_tableau (sdim/program.py:269-365) driving
+ * ExtendedTableau (sdim/tableau/tableau_prime.py:8-380).  These entry points
+ * replace that loop: a Python Program (sdim_gb300/program.py) encodes its
+ * Circuit objects (sdim/circuit.py:76-126) into the op table below and runs
+ * every shot on the GPU.  ctypes is the binding (sdim_gb300/_lib.py).
+ *
+ * Conventions: plain pointers and sizes only; every call returns 0 or a
+ * negative SDIM_E* status and never aborts; sdim_last_error() gives the
+ * message.  The library owns all device memory it allocates; the caller owns
+ * the buffers it passes in.  A context is not re-entrant (one host thread at
+ * a time), like sdim's Program.
+ *
+ * Records: one byte per measurement (M, M_X or RESET instruction, in program
+ * order) per shot: value | deterministic << 7.  The reference returns the
+ * same data as MeasurementResult(qudit_index, deterministic,
+ * measurement_value) nested [qudit][round][shot] (sdim/program.py:355-365).
+ */
+#ifndef SDIM_GB300_H
+#define SDIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDIM_OK 0
+#define SDIM_EINVAL -1     /* bad argument: gate id, qudit index, dimension, size */
+#define SDIM_ECUDA -2      /* CUDA runtime error (no device, launch failure, ...) */
+#define SDIM_ENOMEM -3     /* device or host allocation failed */
+#define SDIM_EDEVICE -4    /* the kernel reported a bad instruction */
+#define SDIM_EUNSUPPORTED -5 /* composite dimension or d >= 128 */
+
+/* run flags */
+#define SDIM_FLAG_PLAIN 1u       /* one single-warp launch per shot (the plain form) */
+#define SDIM_FLAG_OUT_DEVICE 2u  /* output pointers are device pointers */
+#define SDIM_FLAG_ASYNC 4u       /* do not synchronise; call sdim_sync() later */
+#define SDIM_FLAG_TIME 8u        /* time the kernels with CUDA events (sdim_last_kernel_ms) */
+#define SDIM_FLAG_FORCE_GMEM 16u /* keep tableaux in global memory even when they fit in smem */
+
+/* snapshot modes for sdim_snapshot */
+#define SDIM_SNAP_EVERY_INSTRUCTION 1
+#define SDIM_SNAP_AT_MEASUREMENT 2
+#define SDIM_SNAP_FINAL 3
+
+typedef struct sdim_ctx sdim_ctx;
+typedef struct sdim_circuit sdim_circuit;
+
+/* Context on one CUDA device: stream, device buffers, error string.
+ * Replaces the state Program keeps between calls (sdim/program.py:194-204). */
+int sdim_ctx_create(int device, sdim_ctx** out);
+int sdim_ctx_destroy(sdim_ctx* ctx);
+const char* sdim_last_error(const sdim_ctx* ctx);
+/* info[0] = SM count, [1] = opt-in shared memory per block (bytes),
+ * [2] = L2 bytes, [3] = total global memory (bytes). */
+int sdim_device_info(sdim_ctx* ctx, int64_t info[4]);
+
+/* Encodes one program.  ops is nops rows of 4 int32:
+ *   gate id (sdim/gatedata.py:55-102: I 0, X 1, X_INV 2, Z 3, Z_INV 4, H 5,
+ *   H_INV 6, P 7, P_INV 8, CNOT 9, CNOT_INV 10, CZ 11, CZ_INV 12, SWAP 13,
+ *   M 14, M_X 15, RESET 16, N1 17), qudit, target (-1 for one-qudit gates),
+ *   noise channel for N1 (1 'd', 2 'f', 3 'p'; else 0).
+ * noise_prob: nops doubles (only N1 rows are read) or NULL when there is no N1.
+ * The instruction list replaces Circuit.operations
+ * (sdim/circuit.py:6-41, 76-126) and GATE_FUNCTIONS (sdim/program.py:13-32).
+ * Errors: SDIM_EINVAL for unknown gates / qudits out of range (the reference
+ * raises ValueError / IndexError), SDIM_EUNSUPPORTED for composite d (the
+ * reference switches to WeylTableau, sdim/program.py:196-199). */
+int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* noise_prob,
+                        int n, int d, sdim_circuit** out);
+int sdim_circuit_destroy(sdim_circuit* circ);
+/* info[0] n, [1] d, [2] records per shot, [3] user instructions,
+ * [4] device ops, [5] backend (0 residue bytes, 1 bit planes), [6] tableau slot bytes. */
+int sdim_circuit_info(const sdim_circuit* circ, int64_t info[8]);
+
+/* Runs shots [shot0, shot0 + nshots) of one program; out holds
+ * nshots x records bytes (host memory unless SDIM_FLAG_OUT_DEVICE).
+ * Replaces Program.simulate(shots, force_tableau=True) (sdim/program.py:206-267, 269-365). */
+int sdim_run(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot0, int64_t nshots,
+             uint8_t* out, unsigned flags);
+/* Same, with the work on a caller-provided CUDA stream (cudaStream_t as void*,
+ * NULL for the context's stream) and out on the device. */
+int sdim_run_device(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot0,
+                    int64_t nshots, uint8_t* out_dev, void* stream, unsigned flags);
+/* Many programs (uneven n, d, depth, shots) in persistent launches fed by a
+ * device work queue.  outs[i] holds nshots[i] x records(circs[i]) bytes.
+ * The reference has no batch API; it is Program.simulate called once per program. */
+int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, const uint64_t* seeds,
+                   const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs, void* stream,
+                   unsigned flags);
+/* Measured shared-memory read bandwidth of the device in GB/s (all SMs):
+ * the roofline denominator for tableaux resident in shared memory.  No
+ * counterpart in the reference (which has no device code). */
+int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs);
+/* Waits for the context's work and reports a device-side error, if any. */
+int sdim_sync(sdim_ctx* ctx);
+/* Milliseconds of the kernels of the last call made with SDIM_FLAG_TIME. */
+double sdim_last_kernel_ms(const sdim_ctx* ctx);
+
+/* Tableau export of one shot in the reference's int8 block order
+ * x[n][n], z[n][n], phase[n], destab_x[n][n], destab_z[n][n], destab_phase[n]
+ * (sdim/tableau/dataclasses.py:8-47, sdim/tableau/tableau_prime.py:8-95), reduced.
+ * mode SDIM_SNAP_EVERY_INSTRUCTION: one tableau after each user instruction
+ *   (out: user instructions x (4n^2 + 2n) bytes);
+ * mode SDIM_SNAP_AT_MEASUREMENT: one tableau right after each measurement,
+ *   before a RESET correction, as record_tableau stores it
+ *   (sdim/program.py:322-324) (out: records x (4n^2 + 2n) bytes);
+ * mode SDIM_SNAP_FINAL: the state after the last instruction, which a
+ *   Program holds as stabilizer_tableau after simulate (out: 4n^2 + 2n bytes).
+ * records_out (may be NULL) receives that shot's records. */
+int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot, int mode,
+                  int8_t* out, uint8_t* records_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDIM_GB300_H */

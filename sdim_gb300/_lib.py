@@ -1,0 +1,132 @@
+"""ctypes binding of ``include/sdim_gb300.h``.
+
+The library is the only execution path: when it cannot be built or loaded,
+or no CUDA device is present, every call raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from . import build as _build
+
+SDIM_OK = 0
+SDIM_EINVAL = -1
+SDIM_ECUDA = -2
+SDIM_ENOMEM = -3
+SDIM_EDEVICE = -4
+SDIM_EUNSUPPORTED = -5
+
+FLAG_PLAIN = 1
+FLAG_OUT_DEVICE = 2
+FLAG_ASYNC = 4
+FLAG_TIME = 8
+FLAG_FORCE_GMEM = 16
+
+SNAP_EVERY_INSTRUCTION = 1
+SNAP_AT_MEASUREMENT = 2
+SNAP_FINAL = 3
+
+# exported symbol -> (restype, argtypes)
+_P = C.c_void_p
+SIGNATURES = {
+    "sdim_ctx_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
+    "sdim_ctx_destroy": (C.c_int, [_P]),
+    "sdim_last_error": (C.c_char_p, [_P]),
+    "sdim_device_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sdim_encode_circuit": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int, C.c_int, C.POINTER(_P)]),
+    "sdim_circuit_destroy": (C.c_int, [_P]),
+    "sdim_circuit_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sdim_run": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, C.c_uint]),
+    "sdim_run_device": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, _P, C.c_uint]),
+    "sdim_run_batch": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.c_uint]),
+    "sdim_sync": (C.c_int, [_P]),
+    "sdim_last_kernel_ms": (C.c_double, [_P]),
+    "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P]),
+    "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads (building first when needed) the CUDA library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_missing and not _build.up_to_date():
+            _build.build_library()
+        path = _build.LIB
+        if not path.exists():
+            raise RuntimeError(f"sdim_gb300 CUDA library missing at {path}; run sdim_gb300.build.build_library()")
+        lib = C.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+class SdimError(RuntimeError):
+    pass
+
+
+def check(rc: int, ctx_ptr=None, what: str = ""):
+    if rc == SDIM_OK:
+        return
+    msg = ""
+    if ctx_ptr:
+        raw = load().sdim_last_error(ctx_ptr)
+        msg = raw.decode() if raw else ""
+    text = f"{what}: {msg}" if what else msg
+    if rc == SDIM_EINVAL:
+        if "out of range" in msg:
+            raise IndexError(text)
+        raise ValueError(text)
+    if rc == SDIM_EUNSUPPORTED:
+        raise NotImplementedError(text)
+    raise SdimError(f"{text} (status {rc})")
+
+
+class Context:
+    """One CUDA device: owns the library context (stream, device buffers)."""
+
+    _default = {}
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        ptr = _P()
+        rc = lib.sdim_ctx_create(int(device), C.byref(ptr))
+        if rc != SDIM_OK:
+            raise SdimError(f"no usable CUDA device {device} for sdim_gb300 (status {rc})")
+        self.ptr = ptr
+        self.device = int(device)
+        self.lib = lib
+        info = (C.c_int64 * 4)()
+        check(lib.sdim_device_info(ptr, info), ptr)
+        self.num_sms, self.smem_optin, self.l2_bytes, self.gmem_bytes = (int(v) for v in info)
+
+    @classmethod
+    def default(cls, device: int = 0) -> "Context":
+        if device not in cls._default:
+            cls._default[device] = Context(device)
+        return cls._default[device]
+
+    def close(self):
+        if self.ptr:
+            self.lib.sdim_ctx_destroy(self.ptr)
+            self.ptr = None
+
+    def last_kernel_ms(self) -> float:
+        return float(self.lib.sdim_last_kernel_ms(self.ptr))
+
+    def sync(self):
+        check(self.lib.sdim_sync(self.ptr), self.ptr, "sdim_sync")

@@ -1,0 +1,84 @@
+"""Batched execution of many programs (uneven n, d, depth and shots).
+
+The reference has no batch API: each program is a ``Program.simulate`` call
+(sdim/program.py:206-267).  ``BatchRunner`` encodes every program once and runs
+all (program, shot) items through ``sdim_run_batch``: one persistent launch
+per engine variant, fed by a device work queue, largest programs first.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .encode import DeviceProgram, encode_program
+
+
+@dataclass
+class BatchEntry:
+    program: DeviceProgram
+    shots: int
+    seed: int
+    shot0: int = 0
+
+
+class BatchRunner:
+    def __init__(self, ctx: Optional[_lib.Context] = None):
+        self.ctx = ctx or _lib.Context.default(0)
+        self.entries: List[BatchEntry] = []
+
+    def add_spec(self, spec, shots: int, seed: int, shot0: int = 0, noise: bool = True) -> BatchEntry:
+        circuit = spec.build()
+        enc = encode_program([circuit], spec.num_qudits, spec.dimension, noise=noise)
+        e = BatchEntry(DeviceProgram(self.ctx, enc), int(shots), int(seed), int(shot0))
+        self.entries.append(e)
+        return e
+
+    def add_program(self, program: DeviceProgram, shots: int, seed: int, shot0: int = 0) -> BatchEntry:
+        e = BatchEntry(program, int(shots), int(seed), int(shot0))
+        self.entries.append(e)
+        return e
+
+    def _arrays(self, entries):
+        k = len(entries)
+        circs = (C.c_void_p * k)(*[e.program.ptr.value for e in entries])
+        seeds = (C.c_uint64 * k)(*[e.seed & 0xFFFFFFFFFFFFFFFF for e in entries])
+        shot0 = (C.c_int64 * k)(*[e.shot0 for e in entries])
+        nshots = (C.c_int64 * k)(*[e.shots for e in entries])
+        return circs, seeds, shot0, nshots
+
+    def run(self, plain: bool = False, time_kernels: bool = False,
+            entries: Optional[Sequence[BatchEntry]] = None) -> List[np.ndarray]:
+        """Runs every entry; returns one (shots, records) uint8 array each."""
+        entries = list(self.entries if entries is None else entries)
+        outs = [np.empty((e.shots, e.program.num_records), dtype=np.uint8) for e in entries]
+        ptrs = (C.c_void_p * len(entries))(*[o.ctypes.data for o in outs])
+        circs, seeds, shot0, nshots = self._arrays(entries)
+        flags = (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_TIME if time_kernels else 0)
+        rc = self.ctx.lib.sdim_run_batch(self.ctx.ptr, len(entries), circs, seeds, shot0, nshots, ptrs, None,
+                                         flags)
+        _lib.check(rc, self.ctx.ptr, "batch")
+        return outs
+
+    def run_device(self, outs_dev: Sequence[int], stream: Optional[int] = None, plain: bool = False,
+                   time_kernels: bool = False, asynchronous: bool = False,
+                   entries: Optional[Sequence[BatchEntry]] = None):
+        """Same with device output pointers (e.g. ``tensor.data_ptr()``)."""
+        entries = list(self.entries if entries is None else entries)
+        ptrs = (C.c_void_p * len(entries))(*[int(p) for p in outs_dev])
+        circs, seeds, shot0, nshots = self._arrays(entries)
+        flags = _lib.FLAG_OUT_DEVICE | (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_TIME if time_kernels else 0)
+        if asynchronous:
+            flags |= _lib.FLAG_ASYNC
+        rc = self.ctx.lib.sdim_run_batch(self.ctx.ptr, len(entries), circs, seeds, shot0, nshots, ptrs,
+                                         C.c_void_p(stream) if stream else None, flags)
+        _lib.check(rc, self.ctx.ptr, "batch")
+
+    def total_shots(self) -> int:
+        return sum(e.shots for e in self.entries)
+
+    def total_gate_updates(self) -> int:
+        return sum(e.shots * e.program.num_instructions for e in self.entries)

@@ -1,0 +1,261 @@
+"""Drop-in ``Program`` for sdim's prime-dimension tableau path.
+
+Mirrors sdim/program.py:167-573: ``Program(circuit)``,
+``simulate(shots, show_measurement, record_tableau, force_tableau, verbose,
+show_gate, exact, options)``, ``append_circuit``, ``measurement_results`` and
+the return shapes (flat list for one shot, ``[qudit][round][shot]``
+otherwise, sdim/program.py:355-365).  Every shot of every call runs the full
+tableau algorithm on the GPU through the C ABI; there is no CPU path.
+
+Differences from the reference, by design:
+* outcomes of random measurements come from the Philox stream keyed by
+  (seed, shot, measurement ordinal) instead of Python's ``random``
+  (sdim/tableau/tableau_prime.py:332); ``seed`` is a keyword of ``simulate``;
+* N1 noise acts on the tableau (X^a then Z^b after the instruction); the
+  reference's tableau path treats N1 as the identity (sdim/program.py:31) and
+  samples noise only in its Pauli-frame route.  ``noise=False`` reproduces
+  the identity behaviour;
+* ``shots > 1`` runs every shot on the tableau (the reference switches to its
+  frame sampler unless ``force_tableau``), so shot 0 is an ordinary shot;
+* composite dimensions raise NotImplementedError (the reference switches to
+  WeylTableau, sdim/program.py:196-199).
+"""
+from __future__ import annotations
+
+import copy
+import secrets
+from dataclasses import dataclass
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from .circuit import Circuit
+from .encode import DeviceProgram, EncodedProgram, encode_program
+from .gatedata import RESET_ID
+from .tableau import ExtendedTableau, MeasurementResult
+
+
+@dataclass
+class SimulationOptions:
+    shots: int = 1
+    show_measurement: bool = False
+    record_tableau: bool = False
+    force_tableau: bool = False
+    verbose: bool = False
+    show_gate: bool = False
+    exact: bool = False
+
+
+def _is_prime(d: int) -> bool:
+    return d >= 2 and all(d % k for k in range(2, int(d ** 0.5) + 1))
+
+
+def records_to_nested(records: np.ndarray, enc: EncodedProgram, num_qudits: int) -> list:
+    """(shots, records) bytes -> [qudit][round][shot] MeasurementResult lists."""
+    records = np.asarray(records, dtype=np.uint8).reshape(-1, enc.num_records)
+    vals = (records & 0x7F).astype(np.int64)
+    dets = (records >> 7).astype(bool)
+    out: List[list] = [[] for _ in range(num_qudits)]
+    for j in range(enc.num_records):
+        q = int(enc.meas_qudit[j])
+        col_v = vals[:, j].tolist()
+        col_d = dets[:, j].tolist()
+        out[q].append([MeasurementResult(q, dd, vv) for vv, dd in zip(col_v, col_d)])
+    return out
+
+
+def flatten_single_shot(nested: list) -> list:
+    flat = []
+    for per_qudit in nested:
+        for shots_list in per_qudit:
+            flat.append(shots_list[0])
+    return flat
+
+
+class Program:
+    def __init__(self, circuit: Circuit, tableau=None, *, device: int = 0, seed: Optional[int] = None):
+        if tableau is not None:
+            raise NotImplementedError("a custom initial tableau is not supported on the GPU path")
+        if not _is_prime(circuit.dimension):
+            raise NotImplementedError(
+                f"dimension {circuit.dimension} is composite: only prime dimensions have a GPU tableau path")
+        self.num_qudits = circuit.num_qudits
+        self.dimension = circuit.dimension
+        self.circuits = [circuit]
+        self.measurement_results: list = []
+        self.device = device
+        self.seed = seed
+        self._ctx = None
+        self._cache = {}
+        self._last = None  # (seed, shot, noise) of the last simulated shot
+
+    # ------------------------------------------------------------------
+    @property
+    def context(self) -> _lib.Context:
+        if self._ctx is None:
+            self._ctx = _lib.Context.default(self.device)
+        return self._ctx
+
+    def _program_key(self, noise: bool):
+        return (tuple((id(c), len(c.operations), c.num_qudits) for c in self.circuits), bool(noise))
+
+    def compile(self, noise: bool = True) -> DeviceProgram:
+        """Encoded program on the device (cached until the circuits change)."""
+        key = self._program_key(noise)
+        dp = self._cache.get(key)
+        if dp is None:
+            enc = encode_program(self.circuits, self.num_qudits, self.dimension, noise=noise)
+            dp = DeviceProgram(self.context, enc)
+            self._cache = {key: dp}
+        return dp
+
+    def _seed(self, seed):
+        if seed is not None:
+            return int(seed) & 0xFFFFFFFFFFFFFFFF
+        if self.seed is not None:
+            return int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        return secrets.randbits(63)
+
+    # ------------------------------------------------------------------
+    def sample(self, shots: int, seed: Optional[int] = None, shot0: int = 0, noise: bool = True,
+               plain: bool = False, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Records of shots [shot0, shot0 + shots) as a (shots, records) uint8
+        array, value | deterministic << 7 -- the fast path without Python objects."""
+        dp = self.compile(noise)
+        s = self._seed(seed)
+        if out is None:
+            out = np.empty((int(shots), dp.num_records), dtype=np.uint8)
+        flags = _lib.FLAG_PLAIN if plain else 0
+        if shots > 0 and dp.num_records > 0:
+            rc = self.context.lib.sdim_run(self.context.ptr, dp.ptr, s, int(shot0), int(shots),
+                                           out.ctypes.data, flags)
+            _lib.check(rc, self.context.ptr, "simulate")
+        elif shots > 0:
+            rc = self.context.lib.sdim_run(self.context.ptr, dp.ptr, s, int(shot0), int(shots), None, flags)
+            _lib.check(rc, self.context.ptr, "simulate")
+        self._last = (s, int(shot0) + int(shots) - 1, noise)
+        return out
+
+    def snapshot(self, seed: int, shot: int = 0, mode: int = _lib.SNAP_EVERY_INSTRUCTION, noise: bool = True):
+        """Tableau exports (int8, reference block order) and the shot's records."""
+        dp = self.compile(noise)
+        n = self.num_qudits
+        tb = 4 * n * n + 2 * n
+        count = {_lib.SNAP_EVERY_INSTRUCTION: dp.num_instructions,
+                 _lib.SNAP_AT_MEASUREMENT: dp.num_records, _lib.SNAP_FINAL: 1}[mode]
+        buf = np.empty((max(count, 1), tb), dtype=np.int8)
+        rec = np.empty(max(dp.num_records, 1), dtype=np.uint8)
+        rc = self.context.lib.sdim_snapshot(self.context.ptr, dp.ptr, int(seed) & 0xFFFFFFFFFFFFFFFF, int(shot),
+                                            int(mode), buf.ctypes.data, rec.ctypes.data)
+        _lib.check(rc, self.context.ptr, "snapshot")
+        return buf[:count], rec[:dp.num_records]
+
+    # ------------------------------------------------------------------
+    def simulate(self, shots: int = 1, show_measurement: bool = False, record_tableau: bool = False,
+                 force_tableau: bool = False, verbose: bool = False, show_gate: bool = False,
+                 exact: bool = False, options: Optional[SimulationOptions] = None, *,
+                 seed: Optional[int] = None, noise: bool = True, plain: bool = False):
+        if options is None:
+            options = SimulationOptions(shots, show_measurement, record_tableau, force_tableau, verbose,
+                                        show_gate, exact)
+        shots = int(options.shots)
+        dp = self.compile(noise)
+        enc = dp.enc
+        s = self._seed(seed)
+        records = self.sample(shots, seed=s, noise=noise, plain=plain)
+        nested = records_to_nested(records, enc, self.num_qudits)
+        if options.record_tableau or options.verbose:
+            n, d = self.num_qudits, self.dimension
+            for shot in range(shots):
+                if options.record_tableau:
+                    snaps, _ = self.snapshot(s, shot, _lib.SNAP_AT_MEASUREMENT, noise)
+                    for j in range(enc.num_records):
+                        q, r = int(enc.meas_qudit[j]), int(enc.meas_round[j])
+                        nested[q][r][shot].stabilizer_tableau = ExtendedTableau.from_export(snaps[j], n, d)
+                if options.verbose:
+                    snaps, _ = self.snapshot(s, shot, _lib.SNAP_EVERY_INSTRUCTION, noise)
+                    print("Initial state")
+                    ExtendedTableau(n, d).print_tableau()
+                    print("\n")
+                    for t in range(enc.num_instructions):
+                        self._show_gate(t, enc) if options.show_gate else None
+                        ExtendedTableau.from_export(snaps[t], n, d).print_tableau()
+                        print("\n")
+        elif options.show_gate:
+            for _ in range(shots):
+                for t in range(enc.num_instructions):
+                    self._show_gate(t, enc)
+        self.measurement_results = nested
+        self._last = (s, shots - 1, noise)
+        if options.show_measurement:
+            self.print_measurements()
+        if shots == 1:
+            return flatten_single_shot(nested)
+        return nested
+
+    @staticmethod
+    def _show_gate(t: int, enc: EncodedProgram):
+        from .gatedata import GateData
+        gid, q, tgt, _ = (int(v) for v in enc.ops[t])
+        name = GateData().get_gate_name(gid)
+        info = tgt if tgt >= 0 else ""
+        label = "Time step" if t < enc.num_instructions - 1 else "Final step"
+        print(label, t, "\t", name, q, info)
+
+    # ------------------------------------------------------------------
+    @property
+    def stabilizer_tableau(self) -> ExtendedTableau:
+        """Final tableau of the last simulated shot (initial state before any run)."""
+        if self._last is None:
+            return ExtendedTableau(self.num_qudits, self.dimension)
+        s, shot, noise = self._last
+        snaps, _ = self.snapshot(s, max(shot, 0), _lib.SNAP_FINAL, noise)
+        return ExtendedTableau.from_export(snaps[0], self.num_qudits, self.dimension)
+
+    @property
+    def initial_tableau(self) -> ExtendedTableau:
+        return ExtendedTableau(self.num_qudits, self.dimension)
+
+    def append_circuit(self, circuit: Circuit):
+        """Same bookkeeping as sdim/program.py:528-545; the tableau keeps the
+        qudit count of the first circuit."""
+        if self.circuits[-1].num_qudits < circuit.num_qudits:
+            self.circuits[-1].num_qudits = circuit.num_qudits
+        else:
+            circuit.num_qudits = self.circuits[-1].num_qudits
+        if self.circuits[-1].dimension != circuit.dimension:
+            raise ValueError("Circuits must have the same dimension")
+        self.circuits.append(circuit)
+        self._cache = {}
+
+    def print_measurements(self):
+        shot_count = 0
+        for per_qudit in self.measurement_results:
+            for group in per_qudit:
+                shot_count = max(shot_count, len(group))
+        if shot_count == 0:
+            print("No measurements recorded.")
+            return
+        for shot_index in range(shot_count):
+            if shot_count > 1:
+                print(f"Shot {shot_index + 1}:")
+            for per_qudit in self.measurement_results:
+                for number, shots_list in enumerate(per_qudit):
+                    if shot_count > 1:
+                        print(f"{shots_list[shot_index]} during measurement {number}")
+                    else:
+                        print(shots_list[0])
+            if shot_count > 1:
+                print()
+
+    def __str__(self) -> str:
+        return "\n".join(str(c) for c in self.circuits)
+
+    def __deepcopy__(self, memo):
+        other = Program.__new__(Program)
+        other.__dict__.update({k: copy.deepcopy(v, memo) for k, v in self.__dict__.items()
+                               if k not in ("_ctx", "_cache")})
+        other._ctx = self._ctx
+        other._cache = {}
+        return other

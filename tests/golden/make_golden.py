@@ -1,0 +1,295 @@
+"""Generates the golden fixtures by running the reference sdim itself.
+
+Run in a container that holds the reference source (path in $SDIM_REFERENCE,
+default /root/reference):
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
+
+It imports sdim from the reference tree (with import-time stand-ins for
+numba, cirq and Diophantine from ``_stubs``, none of which the
+prime-dimension path calls), never writes into that tree, and drives the
+reference's own ``Program.simulate(force_tableau=True)`` with two injections:
+
+* outcomes: ``sdim.tableau.tableau_prime.random`` is replaced by an object
+  whose ``choice(seq)`` returns ``seq[(word0 * d) >> 32]`` of the Philox block
+  (seed, shot, measurement ordinal, domain 0) -- the only random draw on the
+  path (sdim/tableau/tableau_prime.py:332);
+* noise: after every N1 instruction the reference's own ``apply_X`` /
+  ``apply_Z`` (sdim/tableau/tableau_gates.py:27, 85) are applied a and b
+  times, with (a, b) drawn from the Philox block (seed, shot, N1 ordinal,
+  domain 1), as its deprecated tableau noise function orders them
+  (sdim/tableau/tableau_gates.py:387-391).
+
+Outputs (beside this script): ``cases.json`` (programs, seeds, expected
+known answers) and ``arrays.npz`` (records, per-instruction tableaux of the
+first shot, final tableaux, record_tableau exports; int8/uint8).
+"""
+from __future__ import annotations
+
+import json
+import multiprocessing as mp
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF = os.environ.get("SDIM_REFERENCE", "/root/reference")
+
+
+def _setup_paths():
+    sys.dont_write_bytecode = True
+    for p in (str(ROOT), REF, str(HERE / "_stubs")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+
+
+_setup_paths()
+
+from oracle import philox  # noqa: E402
+from sdim_gb300 import workloads as W  # noqa: E402
+
+MEAS = (14, 15, 16)
+
+
+def _reduce(tab, n, d):
+    order = 2 * d if d % 2 == 0 else d
+    parts = [tab.x_block % d, tab.z_block % d, tab.phase_vector % order,
+             tab.destab_x_block % d, tab.destab_z_block % d, tab.destab_phase_vector % order]
+    return np.concatenate([np.asarray(p, dtype=np.int64).ravel() for p in parts]).astype(np.int8)
+
+
+def run_reference(specs, seed, shot0, nshots, noise=True, snapshots=False, final=False,
+                  record_tableau=False, want_nested=False):
+    """Runs the reference on the programs in ``specs`` (list of CircuitSpec,
+    appended in order) and returns records and tableaux."""
+    import sdim.tableau.tableau_prime as tp
+    from sdim.circuit import Circuit
+    from sdim.program import Program
+    from sdim.tableau.tableau_gates import apply_X, apply_Z
+
+    n, d = specs[0].num_qudits, specs[0].dimension
+    circuits = [s.build(Circuit) for s in specs]
+    prog = Program(circuits[0])
+    for c in circuits[1:]:
+        prog.append_circuit(c)
+    nops = sum(len(c.operations) for c in circuits)
+
+    class Shim:
+        shot = 0
+        mord = 0
+
+        def choice(self, seq):
+            m = int(philox.measurement_outcome(seed, self.shot, self.mord, len(seq)))
+            return seq[m]
+
+    shim = Shim()
+    tp.random = shim
+    st = {"idx": 0, "mord": 0, "nord": 0, "rec": [], "snaps": [], "objs": []}
+    orig = prog.apply_gate
+
+    def wrapped(ins):
+        if snapshots and st["idx"] > 0:
+            st["snaps"].append(_reduce(prog.stabilizer_tableau, n, d))
+        if ins.gate_id in MEAS:
+            shim.mord = st["mord"]
+            st["mord"] += 1
+        res = orig(ins)
+        if ins.gate_id == 17:
+            if noise:
+                params = ins.params or {}
+                ch = params.get("noise_channel", params.get("channel", "d"))
+                thr = philox.noise_threshold(float(params.get("prob", 0.01)))
+                a, b = philox.noise_pauli(seed, shim.shot, st["nord"], d, ch, thr)
+                for _ in range(int(a)):
+                    apply_X(prog.stabilizer_tableau, ins.qudit_index, None)
+                for _ in range(int(b)):
+                    apply_Z(prog.stabilizer_tableau, ins.qudit_index, None)
+            st["nord"] += 1
+        if res is not None:
+            st["rec"].append(int(res.measurement_value) | (0x80 if res.deterministic else 0))
+            st["objs"].append(res)
+        st["idx"] += 1
+        return res
+
+    prog.apply_gate = wrapped
+    records, finals, snaps, rts, nested = [], [], None, [], None
+    for s in range(nshots):
+        shim.shot = shot0 + s
+        st.update(idx=0, mord=0, nord=0, rec=[], snaps=[], objs=[])
+        out = prog.simulate(shots=1, force_tableau=True, record_tableau=record_tableau)
+        if snapshots and s == 0:
+            st["snaps"].append(_reduce(prog.stabilizer_tableau, n, d))
+            snaps = np.stack(st["snaps"]) if st["snaps"] else np.zeros((0, 4 * n * n + 2 * n), np.int8)
+            assert snaps.shape[0] == nops
+        if final:
+            finals.append(_reduce(prog.stabilizer_tableau, n, d))
+        if record_tableau and s == 0:
+            for r in st["objs"]:  # program order; set by the reference after apply_gate
+                rts.append(_reduce(r.stabilizer_tableau, n, d))
+        if want_nested and s == 0:
+            nested = [[(r.qudit_index, bool(r.deterministic), int(r.measurement_value)) for r in out]]
+        records.append(st["rec"])
+    rec = np.asarray(records, dtype=np.uint8).reshape(nshots, -1)
+    return {"records": rec, "snapshots": snaps, "final": np.stack(finals) if finals else None,
+            "record_tableau": np.stack(rts) if rts else None, "nested": nested}
+
+
+def _worker(args):
+    specs_json, seed, shot0, nshots, noise = args
+    _setup_paths()
+    specs = [W.CircuitSpec.from_json(s) for s in specs_json]
+    return run_reference(specs, seed, shot0, nshots, noise=noise)["records"]
+
+
+def run_parallel(specs, seed, nshots, noise=True, procs=8, chunk=32):
+    jobs = [([s.to_json() for s in specs], seed, a, min(chunk, nshots - a), noise)
+            for a in range(0, nshots, chunk)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        parts = pool.map(_worker, jobs)
+    return np.concatenate(parts, axis=0)
+
+
+# ---------------------------------------------------------------------------
+# cases
+# ---------------------------------------------------------------------------
+def spec(n, d, ops, name):
+    return W.CircuitSpec(n, d, [(o[0], o[1], o[2] if len(o) > 2 else None, o[3] if len(o) > 3 else {})
+                                for o in ops], name)
+
+
+def kat_cases():
+    """Known-answer circuits of the reference's tests (tests/test_circuit.py:9-263,
+    tests/test_program.py:14-47) with their expected outcomes."""
+    out = []
+    out.append((spec(2, 2, [("H", 1), ("P", 1), ("H", 0), ("CNOT", 0, 1), ("H", 1), ("CNOT", 0, 1), ("H", 1),
+                            ("P", 0), ("H", 0), ("M", 0), ("P", 1), ("H", 1), ("M", 1)], "kat_phase_kickback"),
+                [(0, True, 1), (1, True, 1)]))
+    out.append((spec(2, 2, [("H", 0), ("P", 0), ("P", 0), ("H", 0), ("M", 0), ("X", 1), ("M", 1)],
+                     "kat_qubit_flip"), [(0, True, 1), (1, True, 1)]))
+    out.append((spec(2, 3, [("X", 0), ("M", 0)], "kat_qutrit_flip"), [(0, True, 1)]))
+    for d in (2, 3, 5):
+        for x0 in range(d):
+            for x1 in range(d):
+                ops = [("X", 0)] * x0 + [("X", 1)] * x1 + [("SWAP", 0, 1), ("M", 0), ("M", 1)]
+                out.append((spec(2, d, ops, f"kat_swap_d{d}_{x0}{x1}"), [(0, True, x1), (1, True, x0)]))
+                ops = [("X", 0)] * x0 + [("X", 1)] * x1 + [("SWAP", 0, 1), ("SWAP", 0, 1), ("M", 0), ("M", 1)]
+                out.append((spec(2, d, ops, f"kat_double_swap_d{d}_{x0}{x1}"), [(0, True, x0), (1, True, x1)]))
+    for a in range(3):
+        for b in range(3):
+            ops = [("X", 0)] * a + [("DFT", 0)] + [("X", 1)] * b + [("DFT", 1), ("SWAP", 0, 1), ("MX", 0),
+                                                                     ("MX", 1)]
+            out.append((spec(2, 3, ops, f"kat_xswap_{a}{b}"), [(0, True, b), (1, True, a)]))
+    for s0 in (0, 1):
+        for s1 in (0, 1):
+            ops = [("H", 0), ("X", 1), ("H", 1)]
+            if s0:
+                ops += [("CNOT", 0, 1), ("X", 1)]
+            if s1:
+                ops += [("CNOT", 0, 1)]
+            ops += [("H", 0), ("M", 0)]
+            out.append((spec(2, 2, ops, f"kat_qubit_deutsch_{s0}{s1}"), [(0, True, 0 if s0 == s1 else 1)]))
+    ops = [("X", 2), ("X", 3), ("X", 4), ("H", 0), ("CZ", 0, 2), ("CZ", 0, 3), ("CZ_INV", 0, 4), ("H_INV", 0),
+           ("H", 1), ("CZ_INV", 1, 2), ("CZ_INV", 1, 3), ("CZ", 1, 4), ("H_INV", 1), ("M", 0), ("M", 1)]
+    out.append((spec(5, 3, ops, "kat_z_stabilizer_extraction"), [(0, True, 1), (1, True, 2)]))
+    ops = [("H", 2), ("H", 3), ("H", 4), ("Z", 2), ("H", 0), ("CX", 0, 2), ("CX", 0, 3), ("CX_INV", 0, 4),
+           ("H_INV", 0), ("H", 1), ("CX_INV", 1, 2), ("CX_INV", 1, 3), ("CX", 1, 4), ("H_INV", 1), ("M", 0),
+           ("M", 1)]
+    out.append((spec(5, 3, ops, "kat_x_stabilizer_extraction"), [(0, True, 2), (1, True, 1)]))
+    out.append((spec(2, 3, [("H", 0), ("X", 1), ("H", 1), ("CNOT", 0, 1), ("H_INV", 0), ("M", 0)],
+                     "kat_deutsch_d3"), [(0, True, 2)]))
+    out.append((spec(2, 3, [("M", 0), ("M", 1)], "kat_measurement_format_1"), [(0, True, 0), (1, True, 0)]))
+    out.append((spec(2, 3, [("M", 0), ("M", 1), ("M", 0), ("M", 1)], "kat_measurement_format_2"),
+                [(0, True, 0), (0, True, 0), (1, True, 0), (1, True, 0)]))
+    return out
+
+
+def random_cases():
+    out = []
+    k = 0
+    for d in (2, 3, 5, 7, 11, 13):
+        for n in (1, 2, 3, 5, 8):
+            nops = 50 if n <= 2 else 110
+            s = W.all_gates_random(n, d, nops, seed=1000 + k, name=f"rand_d{d}_n{n}")
+            out.append(s)
+            k += 1
+    # long runs of additive gates between reductions (lazy modulo, large intermediates)
+    rng = np.random.Generator(np.random.PCG64(77))
+    for d in (3, 7):
+        ops = []
+        for _ in range(300):
+            g = ["CNOT", "CNOT_INV", "P", "P_INV", "H"][int(rng.integers(5))]
+            if g.startswith("CNOT"):
+                c, t = rng.choice(4, 2, replace=False)
+                ops.append((g, int(c), int(t), {}))
+            else:
+                ops.append((g, int(rng.integers(4)), None, {}))
+        ops += [("M", q, None, {}) for q in range(4)] + [("RESET", q, None, {}) for q in range(4)]
+        out.append(W.CircuitSpec(4, d, ops, f"long_additive_d{d}"))
+    # aliased two-qudit gates (control == target) are accepted by the reference
+    for d in (2, 5):
+        ops = [("H", 0, None, {}), ("CNOT", 1, 0, {}), ("P", 1, None, {}), ("CNOT", 1, 1, {}), ("H", 1, None, {}),
+               ("CZ", 0, 0, {}), ("M", 0, None, {}), ("M", 1, None, {}), ("RESET", 0, None, {}),
+               ("CNOT_INV", 0, 0, {}), ("M", 0, None, {}), ("M", 1, None, {})]
+        out.append(W.CircuitSpec(3, d, ops, f"aliased_pairs_d{d}"))
+    return out
+
+
+def main():
+    cases, arrays = [], {}
+
+    def add(name, specs, seed, nshots, noise=True, snapshots=False, final=False, record_tableau=False,
+            expected=None, parallel=False):
+        if parallel:
+            rec = run_parallel(specs, seed, nshots, noise=noise)
+            res = run_reference(specs, seed, 0, min(4, nshots), noise=noise, final=final)
+            assert np.array_equal(res["records"], rec[:res["records"].shape[0]])
+        else:
+            res = run_reference(specs, seed, 0, nshots, noise=noise, snapshots=snapshots, final=final,
+                                record_tableau=record_tableau, want_nested=expected is not None)
+            rec = res["records"]
+        arrays[f"{name}__records"] = rec
+        if res.get("snapshots") is not None and snapshots:
+            arrays[f"{name}__snapshots"] = res["snapshots"]
+        if res.get("final") is not None:
+            arrays[f"{name}__final"] = res["final"]
+        if res.get("record_tableau") is not None:
+            arrays[f"{name}__record_tableau"] = res["record_tableau"]
+        entry = {"name": name, "seed": seed, "nshots": nshots, "noise": noise,
+                 "circuits": [s.to_json() for s in specs]}
+        if expected is not None:
+            got = res["nested"][0]
+            assert got == [tuple(e) for e in expected], (name, got, expected)
+            entry["expected"] = [list(e) for e in expected]
+        cases.append(entry)
+        print(name, rec.shape, flush=True)
+
+    for s, exp in kat_cases():
+        add(s.name, [s], 7, 1, snapshots=True, final=True, expected=exp)
+    for s in random_cases():
+        add(s.name, [s], 4242, 3, snapshots=True, final=True)
+    for d in (3, 5):
+        s = W.all_gates_random(3, d, 40, seed=555 + d, name=f"record_tableau_d{d}")
+        add(s.name, [s], 99, 1, final=True, record_tableau=True)
+    a = W.all_gates_random(3, 3, 70, seed=31, name="program_part_a")
+    b = W.all_gates_random(3, 3, 70, seed=32, name="program_part_b")
+    add("appended_program_d3", [a, b], 5, 3, snapshots=True, final=True)
+    add("noise_off_d5", [W.all_gates_random(4, 5, 90, seed=71, name="noise_off_d5")], 11, 3, noise=False,
+        snapshots=True, final=True)
+    add("no_measurement_d3", [W.CircuitSpec(3, 3, [("H", 0, None, {}), ("CNOT", 0, 1, {})], "nm")], 1, 2,
+        snapshots=True, final=True)
+    add("pr1_d3_n32", [W.pr1(0)], 0, 1024, final=True, parallel=True)
+    add("surface_L3_r3", [W.surface_memory(3, 3, prob=0.02)], 0, 128, final=True, parallel=True)
+    for d in (5, 7):
+        s = W.random_hpc(24, d, 240, seed=d, weights=(0.25, 0.25, 0.5), mr_every=24, mr_fraction=0.1,
+                         name=f"oddd_small_d{d}")
+        add(s.name, [s], 0, 64, final=True, parallel=True)
+    (HERE / "cases.json").write_text(json.dumps({"cases": cases}, indent=0))
+    np.savez_compressed(HERE / "arrays.npz", **arrays)
+    print("wrote", len(cases), "cases")
+
+
+if __name__ == "__main__":
+    main()

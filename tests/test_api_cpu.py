@@ -1,0 +1,148 @@
+"""CPU: drop-in API behaviour (Circuit, GateData, encoder, result nesting,
+error conventions) and the C ABI library's exports."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from sdim_gb300 import Circuit, GateData, MeasurementResult, Program
+from sdim_gb300.encode import encode_program
+from sdim_gb300.program import flatten_single_shot, records_to_nested
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_gate_ids_and_aliases():
+    g = GateData(3)
+    expected = ["I", "X", "X_INV", "Z", "Z_INV", "H", "H_INV", "P", "P_INV", "CNOT", "CNOT_INV", "CZ",
+                "CZ_INV", "SWAP", "M", "M_X", "RESET", "N1"]
+    assert [g.get_gate_name(i) for i in range(18)] == expected
+    for alias, gid in [("DFT", 5), ("R_DAG", 6), ("S", 7), ("S_INV", 8), ("CX", 9), ("SUM_INV", 10),
+                       ("MEASURE", 14), ("MX", 15), ("MR", 16), ("NOISE1", 17)]:
+        assert g.get_gate_id(alias) == gid
+    assert g.get_gate_id("NOPE") is None
+    with pytest.raises(ValueError):
+        g.get_gate_name(99)
+
+
+def test_add_gate_fan_out_rules():
+    c = Circuit(4, 3)
+    c.add_gate("cnot", 0, [1, 2, 3])
+    assert [(o.qudit_index, o.target_index) for o in c.operations] == [(0, 1), (0, 2), (0, 3)]
+    c = Circuit(4, 3)
+    c.add_gate("CX", [1, 2], 0)
+    assert [(o.qudit_index, o.target_index) for o in c.operations] == [(1, 0), (2, 0)]
+    c = Circuit(4, 3)
+    c.add_gate("CZ", [0, 1], [2, 3])
+    assert [(o.qudit_index, o.target_index, o.name) for o in c.operations] == [(0, 2, "CZ"), (1, 3, "CZ")]
+    with pytest.raises(ValueError):
+        c.add_gate("CNOT", [0, 1], [1, 2, 3])
+    c = Circuit(3, 5)
+    c.add_gate("measure", [0, 1, 2])
+    assert [o.gate_id for o in c.operations] == [14, 14, 14]
+    assert c.operations[0].gate_name == "MEASURE" and c.operations[0].name == "M"
+    c.add_gate("N1", 0)
+    assert c.operations[-1].params == {"channel": "d", "prob": 0.01}
+    with pytest.raises(ValueError):
+        c.add_gate("FOO", 0)
+
+
+def test_circuit_validation_and_arithmetic():
+    with pytest.raises(ValueError):
+        Circuit(0, 2)
+    with pytest.raises(ValueError):
+        Circuit(2, 1)
+    a = Circuit(2, 3)
+    a.add_gate("H", 0)
+    b = Circuit(3, 3)
+    b.add_gate("X", 2)
+    c = a + b
+    assert c.num_qudits == 3 and len(c.operations) == 2
+    with pytest.raises(ValueError):
+        a + Circuit(2, 5)
+    a *= 3
+    assert len(a.operations) == 3
+    d = Circuit.from_operation_list([("H", [0]), ("CNOT", [0, 1])], 2, 3)
+    assert [o.gate_id for o in d.operations] == [5, 9]
+
+
+def test_encoder_rows_and_noise_rule():
+    c = Circuit(3, 3)
+    c.add_gate("H", 0)
+    c.add_gate("CNOT", 0, 1)
+    c.add_gate("N1", 1, prob=0.25, noise_channel="f")
+    c.add_gate("N1", 2, channel="p", prob=0.5)
+    c.add_gate("N1", 2)
+    c.add_gate("MX", 2)
+    c.add_gate("M", 0)
+    c.add_gate("RESET", 2)
+    enc = encode_program([c], 3, 3)
+    assert enc.ops.tolist() == [[5, 0, -1, 0], [9, 0, 1, 0], [17, 1, -1, 2], [17, 2, -1, 3], [17, 2, -1, 1],
+                                [15, 2, -1, 0], [14, 0, -1, 0], [16, 2, -1, 0]]
+    assert enc.probs.tolist()[2:5] == [0.25, 0.5, 0.01]
+    assert enc.meas_qudit.tolist() == [2, 0, 2]
+    assert enc.meas_round.tolist() == [0, 0, 1]
+    off = encode_program([c], 3, 3, noise=False)
+    assert off.ops[2:5, 0].tolist() == [0, 0, 0]
+    bad = Circuit(1, 3)
+    bad.add_gate("N1", 0, noise_channel="q")
+    with pytest.raises(ValueError):
+        encode_program([bad], 1, 3)
+
+
+def test_records_to_nested_shapes():
+    c = Circuit(2, 3)
+    c.add_gate("M", [0, 1])
+    c.add_gate("M", [0, 1])
+    enc = encode_program([c], 2, 3)
+    rec = np.array([[0x80 | 1, 2, 0x80, 1], [0x80 | 2, 0, 0x80, 1]], dtype=np.uint8)
+    nested = records_to_nested(rec, enc, 2)
+    assert nested[0][0] == [MeasurementResult(0, True, 1), MeasurementResult(0, True, 2)]
+    assert nested[0][1] == [MeasurementResult(0, True, 0), MeasurementResult(0, True, 0)]
+    assert nested[1][0] == [MeasurementResult(1, False, 2), MeasurementResult(1, False, 0)]
+    assert nested[1][1] == [MeasurementResult(1, False, 1), MeasurementResult(1, False, 1)]
+    flat = flatten_single_shot(records_to_nested(rec[:1], enc, 2))
+    assert flat == [MeasurementResult(0, True, 1), MeasurementResult(0, True, 0), MeasurementResult(1, False, 2),
+                    MeasurementResult(1, False, 1)]
+
+
+def test_composite_dimension_rejected_without_gpu():
+    with pytest.raises(NotImplementedError):
+        Program(Circuit(2, 4))
+    with pytest.raises(NotImplementedError):
+        Program(Circuit(2, 6))
+
+
+def test_measurement_result_strings():
+    r = MeasurementResult(3, False, 2)
+    assert str(r) == "Measured qudit (3) as (2) and was random"
+    with pytest.raises(ValueError):
+        r.get_tableau()
+
+
+def _header_symbols():
+    text = (ROOT / "include" / "sdim_gb300.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|double|const char\*)\s+(sdim_\w+)\s*\(", text, re.M)))
+
+
+def test_library_builds_and_exports_every_header_symbol():
+    from sdim_gb300 import _lib, build
+    path = build.build_library()
+    lib = ctypes.CDLL(str(path))
+    syms = _header_symbols()
+    assert len(syms) >= 12
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) <= set(_lib.SIGNATURES)
+
+
+def test_library_without_device_reports_error_not_fallback():
+    """With no CUDA device the context cannot be created: the API raises."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    from sdim_gb300 import _lib
+    with pytest.raises(_lib.SdimError):
+        _lib.Context(0)

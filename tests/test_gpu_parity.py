@@ -1,0 +1,168 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's golden
+fixtures and the oracle, bit for bit."""
+import numpy as np
+import pytest
+
+import oracle
+from sdim_gb300 import MeasurementResult, Program, _lib, workloads
+from tests.conftest import oracle_run, program_of, specs_of
+
+pytestmark = pytest.mark.gpu
+
+
+def test_golden_records_every_case(golden):
+    cases, arrays = golden
+    for name, case in cases.items():
+        prog = program_of(case)
+        rec = prog.sample(case["nshots"], seed=case["seed"], noise=case["noise"])
+        assert np.array_equal(rec, arrays[f"{name}__records"]), name
+
+
+def test_golden_records_plain_form(golden):
+    cases, arrays = golden
+    for name, case in cases.items():
+        if case["nshots"] > 64:
+            continue
+        prog = program_of(case)
+        rec = prog.sample(case["nshots"], seed=case["seed"], noise=case["noise"], plain=True)
+        assert np.array_equal(rec, arrays[f"{name}__records"]), name
+
+
+def test_golden_tableau_after_every_instruction(golden):
+    cases, arrays = golden
+    checked = 0
+    for name, case in cases.items():
+        key = f"{name}__snapshots"
+        if key not in arrays.files:
+            continue
+        prog = program_of(case)
+        snaps, rec = prog.snapshot(case["seed"], 0, _lib.SNAP_EVERY_INSTRUCTION, noise=case["noise"])
+        assert np.array_equal(snaps, arrays[key]), name
+        assert np.array_equal(rec, arrays[f"{name}__records"][0]), name
+        checked += 1
+    assert checked > 80
+
+
+def test_golden_final_tableaux(golden):
+    cases, arrays = golden
+    for name, case in cases.items():
+        key = f"{name}__final"
+        if key not in arrays.files:
+            continue
+        ref = arrays[key]
+        prog = program_of(case)
+        for shot in range(ref.shape[0]):
+            snap, _ = prog.snapshot(case["seed"], shot, _lib.SNAP_FINAL, noise=case["noise"])
+            assert np.array_equal(snap[0], ref[shot]), (name, shot)
+
+
+def test_golden_record_tableau(golden):
+    cases, arrays = golden
+    names = [n for n in cases if f"{n}__record_tableau" in arrays.files]
+    assert names
+    for name in names:
+        case = cases[name]
+        prog = program_of(case)
+        res = prog.simulate(seed=case["seed"], record_tableau=True)
+        ref = arrays[f"{name}__record_tableau"]
+        enc = prog.compile().enc
+        for j in range(enc.num_records):
+            q, r = int(enc.meas_qudit[j]), int(enc.meas_round[j])
+            # shots == 1: flat list in (qudit, round) order
+            pos = sum(1 for jj in range(enc.num_records)
+                      if (enc.meas_qudit[jj], enc.meas_round[jj]) < (q, r))
+            t = res[pos].stabilizer_tableau
+            flat = np.concatenate([t.x_block.ravel(), t.z_block.ravel(), t.phase_vector,
+                                   t.destab_x_block.ravel(), t.destab_z_block.ravel(), t.destab_phase_vector])
+            assert np.array_equal(flat.astype(np.int8), ref[j]), (name, j)
+
+
+def test_known_answers_through_simulate(golden):
+    cases, _ = golden
+    for name, case in cases.items():
+        if "expected" not in case:
+            continue
+        prog = program_of(case)
+        res = prog.simulate(seed=case["seed"])
+        assert res == [MeasurementResult(*e) for e in case["expected"]], name
+        # shots > 1: nested [qudit][round][shot]
+        res2 = prog.simulate(shots=3, seed=case["seed"], force_tableau=True)
+        assert [[len(r) for r in q] for q in res2] == [[3] * len(q) for q in res2]
+        assert prog.measurement_results == res2
+
+
+def test_pr1_all_shots_and_per_instruction_tableau():
+    spec = workloads.pr1(0)
+    prog = Program(spec.build())
+    rec = prog.sample(1024, seed=0)
+    ref = oracle_run([spec], 0, 0, 1024)
+    assert np.array_equal(rec, ref["records"])
+    snaps, _ = prog.snapshot(0, 0, _lib.SNAP_EVERY_INSTRUCTION)
+    ref0 = oracle_run([spec], 0, 0, 1, snapshots=True)
+    assert np.array_equal(snaps, ref0["snapshots"])
+
+
+def test_surface_distance7_full_size_sample():
+    spec = workloads.surface_memory(7, 7, prob=1e-3)
+    prog = Program(spec.build())
+    rec = prog.sample(2048, seed=0)
+    ref = oracle_run([spec], 0, 0, 2048)["records"]
+    assert np.array_equal(rec, ref)
+    # shot ranges are position-stable: a sub-range run alone gives the same records
+    part = prog.sample(100, seed=0, shot0=1000)
+    assert np.array_equal(part, rec[1000:1100])
+
+
+@pytest.mark.parametrize("d", [5, 7])
+def test_odd_d_n256_sample(d):
+    spec = workloads.odd_d(d, seed=0)
+    prog = Program(spec.build())
+    rec = prog.sample(32, seed=0)
+    ref = oracle_run([spec], 0, 0, 32)["records"]
+    assert np.array_equal(rec, ref)
+
+
+@pytest.mark.parametrize("d", [2, 3, 11])
+def test_global_memory_slots_match_shared(d):
+    spec = workloads.all_gates_random(9, d, 300, seed=d)
+    prog = Program(spec.build())
+    dp = prog.compile()
+    a = prog.sample(64, seed=4)
+    out = np.empty_like(a)
+    rc = prog.context.lib.sdim_run(prog.context.ptr, dp.ptr, 4, 0, 64, out.ctypes.data, _lib.FLAG_FORCE_GMEM)
+    _lib.check(rc, prog.context.ptr)
+    assert np.array_equal(a, out)
+    assert np.array_equal(a, oracle_run([spec], 4, 0, 64)["records"])
+
+
+def test_large_n_global_memory_path():
+    # n = 700 at d = 3 needs a 1 MB slot: global-memory tableaux
+    spec = workloads.random_hpc(700, 3, 1400, seed=9)
+    prog = Program(spec.build())
+    assert prog.compile().slot_bytes > prog.context.smem_optin
+    rec = prog.sample(4, seed=1)
+    assert np.array_equal(rec, oracle_run([spec], 1, 0, 4)["records"])
+
+
+def test_errors_map_to_python_exceptions():
+    from sdim_gb300 import Circuit
+    c = Circuit(2, 3)
+    c.add_gate("H", 5)
+    with pytest.raises(IndexError):
+        Program(c).simulate(seed=1)
+    c = Circuit(2, 3)
+    c.add_gate("CNOT", 0, 7)
+    with pytest.raises(IndexError):
+        Program(c).simulate(seed=1)
+
+
+def test_stabilizer_tableau_after_simulate(golden):
+    cases, arrays = golden
+    case = cases["kat_deutsch_d3"]
+    prog = program_of(case)
+    prog.simulate(seed=case["seed"])
+    t = prog.stabilizer_tableau
+    ref = arrays["kat_deutsch_d3__final"][0]
+    flat = np.concatenate([t.x_block.ravel(), t.z_block.ravel(), t.phase_vector, t.destab_x_block.ravel(),
+                           t.destab_z_block.ravel(), t.destab_phase_vector]).astype(np.int8)
+    assert np.array_equal(flat, ref)
