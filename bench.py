@@ -85,6 +85,22 @@ def row_bytes(n, d):
     return g, g
 
 
+def group_delta_bytes_per_shot(enc, det_row, resets_fired, n, d):
+    """Per-shot phase-delta bytes of the shot-group engine: a random
+    measurement reads and writes the delta row (2P), a deterministic one reads
+    the stabilizer half (P/2), a RESET whose outcome needs a correction reads
+    and writes it (2P).  N1 coins live in registers; fired N1 (rate p) are not
+    counted."""
+    _, P = row_bytes(n, d)
+    total = 0.0
+    j = 0
+    for gid in enc.ops[:, 0].tolist():
+        if gid in (14, 15, 16):
+            total += P / 2 if det_row[j] else 2 * P
+            j += 1
+    return total + 2 * P * resets_fired
+
+
 def algorithmic_bytes_per_shot(enc, det_row, n, d):
     R, P = row_bytes(n, d)
     h, p, cx, pauli = 4 * R + 2 * P, 3 * R + 2 * P, 6 * R, R + 2 * P
@@ -236,34 +252,48 @@ def run_gb300(args):
     shot0 = rank * shots
     nrec = dp.num_records
     out = torch.empty((shots, nrec), dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library runs on the stream handle it is given
+    # (the legacy default stream has handle 0, which means "context stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
-    def device_step(k):
+    def device_step(extra_flags=0):
         rc = ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 0, shot0, shots, out.data_ptr(), stream.cuda_stream,
-                                     _lib.FLAG_ASYNC | _lib.FLAG_TIME)
+                                     _lib.FLAG_ASYNC | _lib.FLAG_TIME | extra_flags)
         _lib.check(rc, ctx.ptr, "run")
 
-    for _ in range(args.warmup):
-        device_step(0)
+    def timed_steps(steps, extra_flags=0, clocks=None):
+        step_ms, kern_ms = [], []
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            device_step(extra_flags)
+            e1.record(stream)
+            ctx.sync()
+            step_ms.append(e0.elapsed_time(e1))
+            kern_ms.append(ctx.last_kernel_ms())
+        torch.cuda.synchronize()
+        return step_ms, kern_ms, (clocks.stop() if clocks else None)
+
+    # the per-shot engine (one warp per shot) on the same workload, beside
+    for _ in range(2):
+        device_step(_lib.FLAG_PER_SHOT)
     ctx.sync()
-    clocks = Clocks(local)
-    step_ms, kern_ms = [], []
-    if ws > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    for k in range(args.steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        device_step(k)
-        e1.record(stream)
-        ctx.sync()
-        step_ms.append(e0.elapsed_time(e1))
-        kern_ms.append(ctx.last_kernel_ms())
-    torch.cuda.synchronize()
-    clk = clocks.stop()
+    ps_steps = max(2, min(args.steps, 3))
+    ps_step_ms, ps_kern_ms, _ = timed_steps(ps_steps, _lib.FLAG_PER_SHOT)
+    ps_records = out[:64].cpu()
+
+    for _ in range(args.warmup):
+        device_step()
+    ctx.sync()
+    step_ms, kern_ms, clk = timed_steps(args.steps, 0, Clocks(local))
     if ws > 1:
         dist.barrier()
     total_ms = sum(step_ms)
@@ -275,13 +305,24 @@ def run_gb300(args):
     value = units_per_step * ws * args.steps / (total_ms / 1e3)
     shots_per_s = shots * ws * args.steps / (total_ms / 1e3)
 
-    # records are bit-identical across runs; det flags are shot independent
+    # records are bit-identical across engines and runs; det flags are shot independent
     rec = out[:64].cpu().numpy()
+    if not np.array_equal(rec, ps_records.numpy()):
+        raise AssertionError("shot-group and per-shot engines disagree")
     det_row = (rec[0] >> 7).astype(bool)
     assert np.all((rec >> 7) == (rec[0] >> 7)), "deterministic flags differ across shots"
-    bytes_per_shot = algorithmic_bytes_per_shot(enc, det_row, spec.num_qudits, spec.dimension)
+    n, d = spec.num_qudits, spec.dimension
+    bytes_per_shot = algorithmic_bytes_per_shot(enc, det_row, n, d)
+    meas_ids = [g for g in enc.ops[:, 0].tolist() if g in (14, 15, 16)]
+    reset_cols = [j for j, g in enumerate(meas_ids) if g == 16]
+    # RESET records whose outcome needs a correction, per shot (all shots)
+    fired = float((out[:, reset_cols] & 0x7F).ne(0).sum().item()) / shots if reset_cols else 0.0
+    groups = -(-shots // 32)
+    group_bytes = groups * bytes_per_shot + shots * group_delta_bytes_per_shot(enc, det_row, fired, n, d)
     mean_kern = statistics.mean(kern_ms)
-    achieved = bytes_per_shot * shots / (mean_kern / 1e3) / 1e9
+    achieved = group_bytes / (mean_kern / 1e3) / 1e9
+    ps_kern = statistics.mean(ps_kern_ms)
+    ps_achieved = bytes_per_shot * shots / (ps_kern / 1e3) / 1e9
     smem_gbs = C_double_probe(ctx)
     peaks = {}
     try:
@@ -342,11 +383,22 @@ def run_gb300(args):
             "plain_gpu": {"value": plain_rate, "unit": UNIT, "shots": pshots,
                           "form": "one single-warp launch per shot"},
             "batched_vs_plain": value / plain_rate,
+            "per_shot_engine": {
+                "value": units_per_step * ps_steps / (sum(ps_step_ms) / 1e3), "unit": UNIT,
+                "form": "persistent kernel, one warp and one full tableau per shot",
+                "kernel_ms": ps_kern,
+                "roofline": {"bound": "smem", "achieved": ps_achieved, "peak": smem_gbs, "unit": "GB/s",
+                             "frac": ps_achieved / smem_gbs,
+                             "algorithmic_bytes_per_shot": bytes_per_shot}},
             "roofline": {"bound": "smem", "achieved": achieved, "peak": smem_gbs, "unit": "GB/s",
                          "frac": achieved / smem_gbs, "traffic": traffic,
+                         "kernel": "k_group_persistent<GroupBits>",
                          "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth",
-                         "hbm_peak_gbs": hbm, "frac_of_hbm": achieved / hbm,
-                         "algorithmic_bytes_per_shot": bytes_per_shot, "kernel_ms": mean_kern},
+                         "algorithmic_bytes_per_launch": group_bytes,
+                         "bytes_model": "x/z rows + common phase per 32-shot group (per-shot tableau figures), "
+                                        "plus each shot's phase-delta rows at measurements and RESET corrections",
+                         "per_shot_equivalent_GBps": bytes_per_shot * shots / (mean_kern / 1e3) / 1e9,
+                         "hbm_peak_gbs": hbm, "kernel_ms": mean_kern},
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": clk,
@@ -369,7 +421,7 @@ def C_double_probe(ctx):  # noqa: N802
 def read_traffic():
     """DRAM bytes per launch of the persistent kernel from the committed ncu
     summary (a line 'traffic_bytes_per_launch: <int>'), else None."""
-    p = ROOT / "profiles" / "k_persistent_bits_surface_L7.md"
+    p = ROOT / "profiles" / "k_group_persistent_bits_surface_L7.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():

@@ -43,6 +43,7 @@ extern "C" {
 #define SDIM_FLAG_ASYNC 4u       /* do not synchronise; call sdim_sync() later */
 #define SDIM_FLAG_TIME 8u        /* time the kernels with CUDA events (sdim_last_kernel_ms) */
 #define SDIM_FLAG_FORCE_GMEM 16u /* keep tableaux in global memory even when they fit in smem */
+#define SDIM_FLAG_PER_SHOT 32u   /* batched runs use one warp per shot instead of the shot-group engine */
 
 /* snapshot modes for sdim_snapshot */
 #define SDIM_SNAP_EVERY_INSTRUCTION 1
@@ -76,7 +77,8 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
                         int n, int d, sdim_circuit** out);
 int sdim_circuit_destroy(sdim_circuit* circ);
 /* info[0] n, [1] d, [2] records per shot, [3] user instructions,
- * [4] device ops, [5] backend (0 residue bytes, 1 bit planes), [6] tableau slot bytes. */
+ * [4] device ops, [5] backend (0 residue bytes, 1 bit planes), [6] per-shot
+ * tableau slot bytes, [7] shot-group slot bytes (0: no group engine for d). */
 int sdim_circuit_info(const sdim_circuit* circ, int64_t info[8]);
 
 /* Runs shots [shot0, shot0 + nshots) of one program; out holds
@@ -113,9 +115,12 @@ double sdim_last_kernel_ms(const sdim_ctx* ctx);
  *   (sdim/program.py:322-324) (out: records x (4n^2 + 2n) bytes);
  * mode SDIM_SNAP_FINAL: the state after the last instruction, which a
  *   Program holds as stabilizer_tableau after simulate (out: 4n^2 + 2n bytes).
- * records_out (may be NULL) receives that shot's records. */
+ * records_out (may be NULL) receives that shot's records.  With the default
+ * flags the batched engine of the program runs (for d = 2 the shot-group
+ * engine, with the shot simulated inside its group of 32); SDIM_FLAG_PER_SHOT
+ * runs the per-shot engine. */
 int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot, int mode,
-                  int8_t* out, uint8_t* records_out);
+                  int8_t* out, uint8_t* records_out, unsigned flags);
 
 #ifdef __cplusplus
 }

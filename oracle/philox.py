@@ -19,9 +19,12 @@ sdim/tableau/tableau_prime.py:332; the drop-in replaces that draw):
 * domain 0: measurement outcome, ordinal = index of the measurement among the
   M / M_X / RESET instructions of the program, word 0 gives the residue
   ``(w0 * d) >> 32``;
-* domain 1: N1 noise, ordinal = index of the N1 instruction among all N1
-  instructions of the program, word 0 is the coin (identity iff
-  ``w0 < threshold``), word 1 picks the Pauli.
+* domain 1: N1 coins.  For the N1 instruction with ordinal j (its index among
+  all N1 instructions of the program) the block with counter ordinal j >> 2
+  gives the coin in word j & 3: the Pauli is the identity iff
+  ``coin < threshold``;
+* domain 2: N1 Pauli choice, drawn only when the coin fires: word 0 of the
+  block with counter ordinal j picks the Pauli.
 """
 from __future__ import annotations
 
@@ -34,7 +37,8 @@ W1 = np.uint32(0xBB67AE85)
 MASK32 = np.uint64(0xFFFFFFFF)
 
 DOMAIN_MEASURE = 0
-DOMAIN_NOISE = 1
+DOMAIN_COIN = 1
+DOMAIN_CHOICE = 2
 
 # (counter, key, expected output) from the Random123 known-answer tests.
 KAT = [
@@ -114,8 +118,9 @@ def noise_pauli(seed: int, shot, ordinal: int, d: int, channel: str, threshold: 
     'p' draws b in [1, d); the draw is replaced by the identity when the coin
     says so.
     """
-    w0, w1, _, _ = stream_words(seed, shot, ordinal, 1)
-    w0 = np.asarray(w0, dtype=np.uint64)
+    block = stream_words(seed, shot, int(ordinal) >> 2, DOMAIN_COIN)
+    w0 = np.asarray(block[int(ordinal) & 3], dtype=np.uint64)
+    w1 = stream_words(seed, shot, ordinal, DOMAIN_CHOICE)[0]
     fire = w0 >= np.uint64(threshold) if threshold < (1 << 32) else np.zeros_like(w0, dtype=bool)
     if channel == 'd':
         r = 1 + residue(w1, d * d - 1)

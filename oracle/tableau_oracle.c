@@ -431,15 +431,18 @@ int oracle_simulate(int n, int d, int64_t nops, const int64_t *ops, const int64_
             }
             case G_N1: {
               if (noise_on) {
-                uint32_t w[4];
-                stream(seed, shot, nord, 1, w);
+                /* coin: word (j & 3) of block j >> 2, domain 1; choice: word 0 of
+                 * block j, domain 2, drawn only when the coin fires */
+                uint32_t cb[4], w[4];
+                stream(seed, shot, nord >> 2, 1, cb);
                 int64_t thr = noise_thr[g];
                 int64_t chan = ops[g * 5 + 4];
                 int64_t a = 0, b = 0;
-                if ((int64_t)w[0] >= thr) {
-                  if (chan == 1) { int64_t r = 1 + mulshift(w[1], (int64_t)d * d - 1); a = r % d; b = r / d; }
-                  else if (chan == 2) { a = 1 + mulshift(w[1], d - 1); }
-                  else if (chan == 3) { b = 1 + mulshift(w[1], d - 1); }
+                if ((int64_t)cb[nord & 3] >= thr) {
+                  stream(seed, shot, nord, 2, w);
+                  if (chan == 1) { int64_t r = 1 + mulshift(w[0], (int64_t)d * d - 1); a = r % d; b = r / d; }
+                  else if (chan == 2) { a = 1 + mulshift(w[0], d - 1); }
+                  else if (chan == 3) { b = 1 + mulshift(w[0], d - 1); }
                 }
                 for (int64_t k = 0; k < a; ++k) apply_x(&t, q);
                 for (int64_t k = 0; k < b; ++k) apply_z(&t, q);

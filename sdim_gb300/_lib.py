@@ -23,6 +23,7 @@ FLAG_OUT_DEVICE = 2
 FLAG_ASYNC = 4
 FLAG_TIME = 8
 FLAG_FORCE_GMEM = 16
+FLAG_PER_SHOT = 32
 
 SNAP_EVERY_INSTRUCTION = 1
 SNAP_AT_MEASUREMENT = 2
@@ -43,7 +44,7 @@ SIGNATURES = {
     "sdim_run_batch": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.c_uint]),
     "sdim_sync": (C.c_int, [_P]),
     "sdim_last_kernel_ms": (C.c_double, [_P]),
-    "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P]),
+    "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 

@@ -14,7 +14,12 @@ using namespace sdim;
 
 namespace {
 
-enum Variant : int { V_BITS = 0, V_U8_3 = 1, V_U8_5 = 2, V_U8_7 = 3, V_U8_GEN = 4, V_COUNT = 5 };
+// Engine variants.  Per-shot engines (one warp per shot): V_BITS (d = 2),
+// V_U8_* (residue bytes).  Group engines (one warp per 32 shots sharing x/z):
+// V_GBITS (d = 2).
+enum Variant : int { V_BITS = 0, V_U8_3 = 1, V_U8_5 = 2, V_U8_7 = 3, V_U8_GEN = 4, V_GBITS = 5, V_COUNT = 6 };
+
+bool is_group(int v) { return v == V_GBITS; }
 
 struct DevBuf {
   void* p = nullptr;
@@ -36,7 +41,7 @@ struct sdim_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timing_pending = false;
   double last_ms = 0.0;
-  int smem_attr_set[V_COUNT] = {0, 0, 0, 0, 0};
+  int smem_attr_set[V_COUNT] = {0, 0, 0, 0, 0, 0};
 };
 
 struct sdim_circuit {
@@ -44,8 +49,10 @@ struct sdim_circuit {
   int n = 0, d = 0, nmeas = 0;
   int64_t nops_user = 0;
   int nops = 0;
-  int variant = 0;
+  int variant = 0;          // per-shot engine (plain form, per-shot snapshots)
+  int gvariant = -1;        // group engine for batched runs, -1 if none
   size_t slot_bytes = 0;
+  size_t gslot_bytes = 0;
   uint2* h_ops = nullptr;  // pinned host copy
   uint2* d_ops = nullptr;
 };
@@ -103,7 +110,10 @@ int variant_for(int d) {
   }
 }
 
+int group_variant_for(int d) { return d == 2 ? V_GBITS : -1; }
+
 size_t slot_bytes_for(int variant, int n) {
+  if (variant == V_GBITS) return round16(GroupBits::slot_bytes(n));
   return round16(variant == V_BITS ? EngineBits::slot_bytes(n) : SlotU8::bytes(n));
 }
 
@@ -140,6 +150,37 @@ struct KernelSet {
                        int smem_slot, int8_t* snap, int mode, int* status) {
     k_snapshot<E><<<1, 32, smem, s>>>(desc, shot, gslot, smem_slot, snap, mode, status);
   }
+  static void group_snapshot(size_t, cudaStream_t, const CircuitDesc*, long long, uint8_t*, int, int8_t*, int, int,
+                             int*) {}
+};
+
+template <class G>
+struct GroupSet {
+  static cudaError_t set_smem(int bytes) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_group_persistent<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_group_snapshot<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
+  static int occupancy(int block, size_t smem) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_group_persistent<G>, block, smem) != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+    }
+    return std::max(nb, 1);
+  }
+  static void persistent(dim3 g, dim3 b, size_t smem, cudaStream_t s, const CircuitDesc* descs, int nc,
+                         long long total, unsigned long long* counter, uint8_t* gslots, size_t slot,
+                         int smem_slots, int* status) {
+    k_group_persistent<G><<<g, b, smem, s>>>(descs, nc, total, counter, gslots, slot, smem_slots, status);
+  }
+  static void single(size_t, cudaStream_t, const CircuitDesc*, long long, uint8_t*, int, int*) {}
+  static void snapshot(size_t, cudaStream_t, const CircuitDesc*, long long, uint8_t*, int, int8_t*, int, int*) {}
+  static void group_snapshot(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long group, uint8_t* gslot,
+                             int smem_slot, int8_t* snap, int mode, int lane, int* status) {
+    k_group_snapshot<G><<<1, 32, smem, s>>>(desc, group, gslot, smem_slot, snap, mode, lane, status);
+  }
 };
 
 template <class F>
@@ -149,6 +190,7 @@ void with_engine(int variant, F&& f) {
     case V_U8_3: f(KernelSet<EngineU8<3>>()); break;
     case V_U8_5: f(KernelSet<EngineU8<5>>()); break;
     case V_U8_7: f(KernelSet<EngineU8<7>>()); break;
+    case V_GBITS: f(GroupSet<GroupBits>()); break;
     default: f(KernelSet<EngineU8<0>>()); break;
   }
 }
@@ -225,8 +267,16 @@ struct Job {
   uint8_t* out_dev;
 };
 
+// Engine used for a job: the group engine for batched runs when the
+// circuit has one (unless SDIM_FLAG_PER_SHOT), else the per-shot engine.
+int job_variant(const sdim_circuit* c, unsigned flags) {
+  if (!(flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT)) && c->gvariant >= 0) return c->gvariant;
+  return c->variant;
+}
+
 // Launches every job, grouped by engine variant: one persistent launch per
-// group (or one single-warp launch per shot with SDIM_FLAG_PLAIN).
+// variant (or one single-warp launch per shot with SDIM_FLAG_PLAIN).  Work
+// items are shots for per-shot engines and 32-shot groups for group engines.
 int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned flags) {
   const bool plain = flags & SDIM_FLAG_PLAIN;
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
@@ -235,12 +285,14 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
   if ((rc = ensure(ctx, ctx->counters, sizeof(unsigned long long) * V_COUNT)) != SDIM_OK) return rc;
   if ((rc = ensure(ctx, ctx->descs, sizeof(CircuitDesc) * std::max<size_t>(jobs.size(), 1))) != SDIM_OK)
     return rc;
+  std::vector<int> var(jobs.size());
+  for (size_t i = 0; i < jobs.size(); ++i) var[i] = job_variant(jobs[i].c, flags);
   // group by variant; inside a group, most expensive circuits first
   std::vector<int> order(jobs.size());
   for (size_t i = 0; i < jobs.size(); ++i) order[i] = (int)i;
   auto cost = [&](const Job& j) { return (double)j.c->nops * (double)j.c->n; };
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    if (jobs[a].c->variant != jobs[b].c->variant) return jobs[a].c->variant < jobs[b].c->variant;
+    if (var[a] != var[b]) return var[a] < var[b];
     return cost(jobs[a]) > cost(jobs[b]);
   });
   std::vector<CircuitDesc> hd(jobs.size());
@@ -248,8 +300,8 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
   std::vector<Group> groups;
   for (size_t k = 0; k < order.size(); ++k) {
     const Job& j = jobs[order[k]];
-    if (groups.empty() || groups.back().variant != j.c->variant)
-      groups.push_back(Group{j.c->variant, (int)k, (int)k, 0, 0});
+    const int v = var[order[k]];
+    if (groups.empty() || groups.back().variant != v) groups.push_back(Group{v, (int)k, (int)k, 0, 0});
     Group& g = groups.back();
     CircuitDesc& dsc = hd[k];
     dsc.ops = j.c->d_ops;
@@ -263,8 +315,8 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     dsc.nmeas = j.c->nmeas;
     dsc.nshots = (int)j.nshots;
     dsc.slot = 0;
-    g.items += j.nshots;
-    g.slot = std::max(g.slot, j.c->slot_bytes);
+    g.items += is_group(v) ? (j.nshots + 31) / 32 : j.nshots;
+    g.slot = std::max(g.slot, is_group(v) ? j.c->gslot_bytes : j.c->slot_bytes);
     g.end = (int)k + 1;
   }
   CircuitDesc* ddesc = static_cast<CircuitDesc*>(ctx->descs.p);
@@ -478,6 +530,8 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
   c->nops = (int)dev.size();
   c->variant = variant_for(d);
   c->slot_bytes = slot_bytes_for(c->variant, n);
+  c->gvariant = group_variant_for(d);
+  c->gslot_bytes = c->gvariant >= 0 ? slot_bytes_for(c->gvariant, n) : 0;
   const size_t bytes = std::max<size_t>(dev.size(), 1) * sizeof(uint2);
   cudaError_t e = cudaMallocHost(&c->h_ops, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ops, bytes);
@@ -517,7 +571,7 @@ int sdim_circuit_info(const sdim_circuit* c, int64_t info[8]) {
   info[4] = c->nops;
   info[5] = c->variant == V_BITS ? 1 : 0;
   info[6] = (int64_t)c->slot_bytes;
-  info[7] = 0;
+  info[7] = (int64_t)c->gslot_bytes;
   return SDIM_OK;
 }
 
@@ -627,8 +681,8 @@ int sdim_sync(sdim_ctx* ctx) {
 double sdim_last_kernel_ms(const sdim_ctx* ctx) { return ctx ? ctx->last_ms : -1.0; }
 
 int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot, int mode, int8_t* out,
-                  uint8_t* records_out) {
-  if (!ctx || !c || !out ||
+                  uint8_t* records_out, unsigned flags) {
+  if (!ctx || !c || !out || shot < 0 ||
       (mode != SDIM_SNAP_EVERY_INSTRUCTION && mode != SDIM_SNAP_AT_MEASUREMENT && mode != SDIM_SNAP_FINAL))
     return fail(ctx, SDIM_EINVAL, "bad argument to sdim_snapshot");
   CK(cudaSetDevice(ctx->device));
@@ -636,37 +690,49 @@ int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t s
   const size_t count = mode == SDIM_SNAP_EVERY_INSTRUCTION ? (size_t)c->nops_user
                        : mode == SDIM_SNAP_AT_MEASUREMENT ? (size_t)c->nmeas
                                                           : (size_t)1;
+  const int v = job_variant(c, flags);
+  const bool grp = is_group(v);
+  const size_t slot = grp ? c->gslot_bytes : c->slot_bytes;
+  // a group snapshot runs the 32 shots [shot - lane, shot - lane + 32) and exports lane's
+  const int lane = grp ? (int)(shot % 32) : 0;
   int rc;
   if ((rc = ensure(ctx, ctx->snap, std::max<size_t>(count * tb, 1))) != SDIM_OK) return rc;
-  if ((rc = ensure(ctx, ctx->out, std::max<size_t>(c->nmeas, 1))) != SDIM_OK) return rc;
+  if ((rc = ensure(ctx, ctx->out, std::max<size_t>((size_t)c->nmeas * 32, 1))) != SDIM_OK) return rc;
   if ((rc = ensure(ctx, ctx->status, sizeof(int))) != SDIM_OK) return rc;
   if ((rc = ensure(ctx, ctx->descs, sizeof(CircuitDesc))) != SDIM_OK) return rc;
-  if ((rc = set_smem_attr(ctx, c->variant)) != SDIM_OK) return rc;
+  if ((rc = set_smem_attr(ctx, v)) != SDIM_OK) return rc;
   CircuitDesc dsc;
   std::memset(&dsc, 0, sizeof(dsc));
   dsc.ops = c->d_ops;
   dsc.out = static_cast<uint8_t*>(ctx->out.p);
   dsc.seed = seed;
-  dsc.shot0 = shot;
+  dsc.shot0 = shot - lane;
   dsc.nops = c->nops;
   dsc.n = c->n;
   dsc.d = c->d;
   dsc.nmeas = c->nmeas;
-  dsc.nshots = 1;
-  const bool sm = c->slot_bytes <= (size_t)ctx->smem_optin;
-  if (!sm && (rc = ensure(ctx, ctx->gslots, c->slot_bytes)) != SDIM_OK) return rc;
+  dsc.nshots = grp ? 32 : 1;
+  const bool sm = !(flags & SDIM_FLAG_FORCE_GMEM) && slot <= (size_t)ctx->smem_optin;
+  if (!sm && (rc = ensure(ctx, ctx->gslots, slot)) != SDIM_OK) return rc;
   cudaStream_t s = ctx->stream;
   CK(cudaMemcpyAsync(ctx->descs.p, &dsc, sizeof(dsc), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(ctx->status.p, 0, sizeof(int), s));
-  with_engine(c->variant, [&](auto ks) {
-    decltype(ks)::snapshot(sm ? c->slot_bytes : 0, s, static_cast<const CircuitDesc*>(ctx->descs.p), 0,
-                           static_cast<uint8_t*>(ctx->gslots.p), sm ? 1 : 0, static_cast<int8_t*>(ctx->snap.p),
-                           mode, static_cast<int*>(ctx->status.p));
+  const CircuitDesc* dd = static_cast<const CircuitDesc*>(ctx->descs.p);
+  uint8_t* gs = static_cast<uint8_t*>(ctx->gslots.p);
+  int8_t* sp = static_cast<int8_t*>(ctx->snap.p);
+  int* st = static_cast<int*>(ctx->status.p);
+  with_engine(v, [&](auto ks) {
+    if (grp)
+      decltype(ks)::group_snapshot(sm ? slot : 0, s, dd, 0, gs, sm ? 1 : 0, sp, mode, lane, st);
+    else
+      decltype(ks)::snapshot(sm ? slot : 0, s, dd, 0, gs, sm ? 1 : 0, sp, mode, st);
   });
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return cuda_fail(ctx, le, "snapshot launch");
   if (count * tb) CK(cudaMemcpyAsync(out, ctx->snap.p, count * tb, cudaMemcpyDeviceToHost, s));
-  if (records_out && c->nmeas) CK(cudaMemcpyAsync(records_out, ctx->out.p, c->nmeas, cudaMemcpyDeviceToHost, s));
+  if (records_out && c->nmeas)
+    CK(cudaMemcpyAsync(records_out, static_cast<uint8_t*>(ctx->out.p) + (size_t)lane * c->nmeas, c->nmeas,
+                       cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   return read_status(ctx);
 }

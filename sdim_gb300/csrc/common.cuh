@@ -77,19 +77,36 @@ __device__ __forceinline__ uint4 stream_block(unsigned long long seed, long long
 // Multiply-shift map of a 32-bit word onto [0, m).
 __device__ __forceinline__ int mulshift(uint32_t w, uint32_t m) { return (int)__umulhi(w, m); }
 
-// Noise exponents (a, b) of X^a Z^b for one N1 instruction; (0, 0) when the
-// coin keeps the identity.
-__device__ __forceinline__ int2 noise_draw(uint32_t op, uint32_t threshold, int d,
-                                           unsigned long long seed, long long shot,
-                                           uint32_t ordinal) {
-  const uint4 w = stream_block(seed, shot, ordinal, 1u);
-  if (w.x < threshold) return make_int2(0, 0);
+// N1 coins: the coin of N1 ordinal j is word (j & 3) of the domain-1 block
+// with counter ordinal j >> 2, so one Philox block serves four consecutive
+// N1 instructions.  The cache holds the last block.
+struct CoinCache {
+  uint4 blk;
+  uint32_t id;
+  __device__ CoinCache() : blk(make_uint4(0u, 0u, 0u, 0u)), id(0xffffffffu) {}
+  __device__ __forceinline__ uint32_t coin(unsigned long long seed, long long shot, uint32_t ordinal) {
+    if ((ordinal >> 2) != id) {
+      id = ordinal >> 2;
+      blk = stream_block(seed, shot, id, 1u);
+    }
+    const uint32_t j = ordinal & 3u;
+    return j == 0 ? blk.x : j == 1 ? blk.y : j == 2 ? blk.z : blk.w;
+  }
+};
+
+// Exponents (a, b) of X^a Z^b for an N1 whose coin fired: word 0 of the
+// domain-2 block (seed, shot, ordinal).  Channel draws follow the reference's
+// frame-sampler draws (sdim/program.py:486-497): 'd' r in [1, d^2) with
+// a = r % d, b = r / d; 'f' a in [1, d); 'p' b in [1, d).
+__device__ __forceinline__ int2 noise_choice(uint32_t op, int d, unsigned long long seed, long long shot,
+                                             uint32_t ordinal) {
+  const uint4 w = stream_block(seed, shot, ordinal, 2u);
   if (op == OP_N1D) {
-    const int r = 1 + mulshift(w.y, (uint32_t)(d * d - 1));
+    const int r = 1 + mulshift(w.x, (uint32_t)(d * d - 1));
     return make_int2(r % d, r / d);
   }
-  if (op == OP_N1F) return make_int2(1 + mulshift(w.y, (uint32_t)(d - 1)), 0);
-  return make_int2(0, 1 + mulshift(w.y, (uint32_t)(d - 1)));
+  if (op == OP_N1F) return make_int2(1 + mulshift(w.x, (uint32_t)(d - 1)), 0);
+  return make_int2(0, 1 + mulshift(w.x, (uint32_t)(d - 1)));
 }
 
 // Error codes written to the device status word.

@@ -105,105 +105,116 @@ struct EngineBits {
     for (int w = lane; w < W2; w += 32) P1[w] ^= (zr[w] & mz) ^ (xr[w] & mx);
   }
 
-  __device__ int measure(int lane, int q, unsigned long long seed, long long shot,
-                         uint32_t ordinal, int* det) {
-    __syncwarp();
+  // ---------------- Z measurement, in reusable pieces ----------------
+  // Lowest stabilizer with a set x bit in row q, or >= n (tableau_prime.py:273-283).
+  __device__ __forceinline__ int pivot(int lane, int q) const {
     const uint32_t* xq = X + (size_t)q * RS;
-    // pivot: lowest stabilizer bit of row q
     int mine = 0x7fffffff;
     for (int w = lane; w < Wn; w += 32) {
       const uint32_t v = xq[w];
       if (v) { mine = (w << 5) + __ffs(v) - 1; break; }
     }
-    const int p = __reduce_min_sync(0xffffffffu, mine);
-    if (p < n) {
-      const int wp = p >> 5, bp = p & 31;
-      const uint32_t pbit = 1u << bp;
-      const int wd = Wn + wp;
-      const int php = (int)((P0[wp] >> bp) & 1u) | (int)(((P1[wp] >> bp) & 1u) << 1);
-      const uint32_t lo_m = (php & 1) ? 0xffffffffu : 0u;
-      const uint32_t hi_m = (php & 2) ? 0xffffffffu : 0u;
+    return __reduce_min_sync(0xffffffffu, mine);
+  }
+  __device__ __forceinline__ int phase_of(int g) const {
+    const int w = g >> 5, b = g & 31;
+    return (int)((P0[w] >> b) & 1u) | (int)(((P1[w] >> b) & 1u) << 1);
+  }
+
+  // Rowsum of a random measurement (tableau_prime.py:308-322): every
+  // generator g != stabilizer p with x_q[g] = 1 absorbs the pivot column:
+  // x_g ^= x_p, z_g ^= z_p, ph_g += php + 2 (z_g . x_p).  Word w of the
+  // factor row F (the x_q row without bit p) is left in fw[w] when fw != 0.
+  __device__ void rowsum(int lane, int q, int p, int php, uint32_t* fw) {
+    const uint32_t* xq = X + (size_t)q * RS;
+    const int wp = p >> 5, bp = p & 31;
+    const uint32_t pbit = 1u << bp;
+    const uint32_t lo_m = (php & 1) ? 0xffffffffu : 0u;
+    const uint32_t hi_m = (php & 2) ? 0xffffffffu : 0u;
+    if (W2 <= 32) {
+      // rows split over R = 32 / W2p lane groups, W2p = pow2 >= W2
+      int W2p = 1;
+      while (W2p < W2) W2p <<= 1;
+      const int R = 32 / W2p;
+      const int w = lane & (W2p - 1), r = lane / W2p;
+      const bool act = w < W2;
+      uint32_t F = act ? xq[w] : 0u;
+      if (w == wp) F &= ~pbit;
+      if (fw && act && r == 0) fw[w] = F;
+      uint32_t C = 0u;
       __syncwarp();
-      if (W2 <= 32) {
-        // rows split over R = 32 / W2p lane groups, W2p = pow2 >= W2
-        int W2p = 1;
-        while (W2p < W2) W2p <<= 1;
-        const int R = 32 / W2p;
-        const int w = lane & (W2p - 1), r = lane / W2p;
-        const bool act = w < W2;
-        uint32_t F = act ? xq[w] : 0u;
+      if (act) {
+        for (int k = r; k < n; k += R) {
+          uint32_t* xr = X + (size_t)k * RS;
+          uint32_t* zr = Z + (size_t)k * RS;
+          const uint32_t xpk = (xr[wp] >> bp) & 1u, zpk = (zr[wp] >> bp) & 1u;
+          const uint32_t zk = zr[w];
+          C ^= zk & (0u - xpk);
+          xr[w] ^= F & (0u - xpk);
+          zr[w] = zk ^ (F & (0u - zpk));
+        }
+      }
+      for (int off = W2p; off < 32; off <<= 1) C ^= __shfl_xor_sync(0xffffffffu, C, off);
+      if (act && r == 0) {
+        const uint32_t lo = P0[w];
+        const uint32_t a_lo = F & lo_m;
+        const uint32_t carry = lo & a_lo;
+        P0[w] = lo ^ a_lo;
+        P1[w] ^= (F & (hi_m ^ C)) ^ carry;
+      }
+    } else {
+      for (int w = lane; w < W2; w += 32) {
+        uint32_t F = xq[w];
         if (w == wp) F &= ~pbit;
+        if (fw) fw[w] = F;
         uint32_t C = 0u;
-        __syncwarp();
-        if (act) {
-          for (int k = r; k < n; k += R) {
-            uint32_t* xr = X + (size_t)k * RS;
-            uint32_t* zr = Z + (size_t)k * RS;
-            const uint32_t xpk = (xr[wp] >> bp) & 1u, zpk = (zr[wp] >> bp) & 1u;
-            const uint32_t zk = zr[w];
-            C ^= zk & (0u - xpk);
-            xr[w] ^= F & (0u - xpk);
-            zr[w] = zk ^ (F & (0u - zpk));
-          }
+        for (int k = 0; k < n; ++k) {
+          uint32_t* xr = X + (size_t)k * RS;
+          uint32_t* zr = Z + (size_t)k * RS;
+          const uint32_t xpk = (xr[wp] >> bp) & 1u, zpk = (zr[wp] >> bp) & 1u;
+          const uint32_t zk = zr[w];
+          C ^= zk & (0u - xpk);
+          xr[w] ^= F & (0u - xpk);
+          zr[w] = zk ^ (F & (0u - zpk));
         }
-        for (int off = W2p; off < 32; off <<= 1) C ^= __shfl_xor_sync(0xffffffffu, C, off);
-        if (act && r == 0) {
-          // ph_g += php + 2 C_g for g in F (mod 4)
-          const uint32_t lo = P0[w];
-          const uint32_t a_lo = F & lo_m;
-          const uint32_t carry = lo & a_lo;
-          P0[w] = lo ^ a_lo;
-          P1[w] ^= (F & (hi_m ^ C)) ^ carry;
-        }
-      } else {
-        for (int w = lane; w < W2; w += 32) {
-          uint32_t F = xq[w];
-          if (w == wp) F &= ~pbit;
-          uint32_t C = 0u;
-          for (int k = 0; k < n; ++k) {
-            uint32_t* xr = X + (size_t)k * RS;
-            uint32_t* zr = Z + (size_t)k * RS;
-            const uint32_t xpk = (xr[wp] >> bp) & 1u, zpk = (zr[wp] >> bp) & 1u;
-            const uint32_t zk = zr[w];
-            C ^= zk & (0u - xpk);
-            xr[w] ^= F & (0u - xpk);
-            zr[w] = zk ^ (F & (0u - zpk));
-          }
-          const uint32_t lo = P0[w];
-          const uint32_t a_lo = F & lo_m;
-          const uint32_t carry = lo & a_lo;
-          P0[w] = lo ^ a_lo;
-          P1[w] ^= (F & (hi_m ^ C)) ^ carry;
-        }
+        const uint32_t lo = P0[w];
+        const uint32_t a_lo = F & lo_m;
+        const uint32_t carry = lo & a_lo;
+        P0[w] = lo ^ a_lo;
+        P1[w] ^= (F & (hi_m ^ C)) ^ carry;
       }
-      __syncwarp();
-      // destabilizer p <- stabilizer p; stabilizer p <- Z_q
-      for (int k = lane; k < n; k += 32) {
-        uint32_t* xr = X + (size_t)k * RS;
-        uint32_t* zr = Z + (size_t)k * RS;
-        const uint32_t xs = xr[wp], zs = zr[wp];
-        const uint32_t xpk = (xs >> bp) & 1u, zpk = (zs >> bp) & 1u;
-        xr[wd] = (xr[wd] & ~pbit) | (xpk << bp);
-        zr[wd] = (zr[wd] & ~pbit) | (zpk << bp);
-        xr[wp] = xs & ~pbit;
-        zr[wp] = (zs & ~pbit) | ((k == q) ? pbit : 0u);
-      }
-      const uint4 rw = stream_block(seed, shot, ordinal, 0u);
-      const int m = mulshift(rw.x, 2u);
-      if (lane == 0) {
-        P0[wd] = (P0[wd] & ~pbit) | ((uint32_t)(php & 1) << bp);
-        P1[wd] = (P1[wd] & ~pbit) | ((uint32_t)(php >> 1) << bp);
-        P0[wp] &= ~pbit;                                  // ph_p = -2m mod 4 = 2m
-        P1[wp] = (P1[wp] & ~pbit) | ((uint32_t)m << bp);
-      }
-      __syncwarp();
-      *det = 0;
-      return m;
     }
-    // deterministic: f = destab_x row q (words Wn..2Wn), phase
-    //   aph = sum_{i in f} ph_i + 2 sum_k parity(a_k & exclusive_prefix_xor(b_k))
-    // with a_k = x_k & f, b_k = z_k & f over the stabilizer words.
-    const uint32_t* fq = xq + Wn;
+  }
+
+  // destabilizer p <- stabilizer p (phase php); stabilizer p <- Z_q with
+  // phase -2m (tableau_prime.py:324-333)
+  __device__ void pivot_columns(int lane, int q, int p, int php, int m) {
+    const int wp = p >> 5, bp = p & 31;
+    const uint32_t pbit = 1u << bp;
+    const int wd = Wn + wp;
+    for (int k = lane; k < n; k += 32) {
+      uint32_t* xr = X + (size_t)k * RS;
+      uint32_t* zr = Z + (size_t)k * RS;
+      const uint32_t xs = xr[wp], zs = zr[wp];
+      const uint32_t xpk = (xs >> bp) & 1u, zpk = (zs >> bp) & 1u;
+      xr[wd] = (xr[wd] & ~pbit) | (xpk << bp);
+      zr[wd] = (zr[wd] & ~pbit) | (zpk << bp);
+      xr[wp] = xs & ~pbit;
+      zr[wp] = (zs & ~pbit) | ((k == q) ? pbit : 0u);
+    }
+    if (lane == 0) {
+      P0[wd] = (P0[wd] & ~pbit) | ((uint32_t)(php & 1) << bp);
+      P1[wd] = (P1[wd] & ~pbit) | ((uint32_t)(php >> 1) << bp);
+      P0[wp] &= ~pbit;                                  // ph_p = -2m mod 4 = 2m
+      P1[wp] = (P1[wp] & ~pbit) | ((uint32_t)(m & 1) << bp);
+    }
+  }
+
+  // Deterministic outcome phase (tableau_prime.py:348-361), f = destab_x row q:
+  //   aph = sum_{i in f} ph_i + 2 sum_k parity(a_k & exclusive_prefix_xor(b_k))
+  // with a_k = x_k & f, b_k = z_k & f over the stabilizer words; mod 4.
+  __device__ int det_phase(int lane, int q) const {
+    const uint32_t* fq = X + (size_t)q * RS + Wn;
     int pl = 0;
     for (int w = lane; w < Wn; w += 32) {
       const uint32_t f = fq[w];
@@ -216,6 +227,7 @@ struct EngineBits {
       uint32_t carry = 0u;  // parity of b bits below the current word
       for (int w = 0; w < Wn; ++w) {
         const uint32_t f = fq[w];
+        if (!f) continue;
         const uint32_t a = xr[w] & f, b = zr[w] & f;
         uint32_t v = b;
         v ^= v << 1;
@@ -230,10 +242,28 @@ struct EngineBits {
     }
     const int P = __reduce_add_sync(0xffffffffu, pl) & 3;
     const uint32_t T = __reduce_xor_sync(0xffffffffu, tpar) & 1u;
-    const int aph = (P + 2 * (int)T) & 3;
+    return (P + 2 * (int)T) & 3;
+  }
+
+  __device__ int measure(int lane, int q, unsigned long long seed, long long shot,
+                         uint32_t ordinal, int* det) {
+    __syncwarp();
+    const int p = pivot(lane, q);
+    if (p < n) {
+      const int php = phase_of(p);
+      __syncwarp();
+      rowsum(lane, q, p, php, nullptr);
+      __syncwarp();
+      const int m = mulshift(stream_block(seed, shot, ordinal, 0u).x, 2u);
+      pivot_columns(lane, q, p, php, m);
+      __syncwarp();
+      *det = 0;
+      return m;
+    }
+    const int aph = det_phase(lane, q);
     __syncwarp();
     *det = 1;
-    return ((aph + 1) >> 1) & 1;
+    return ((aph + 1) >> 1) & 1;  // floor(-aph / 2) mod 2
   }
 
   __device__ __forceinline__ void reset_fix(int lane, int q, int m) {

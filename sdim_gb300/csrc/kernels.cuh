@@ -7,6 +7,7 @@
 #pragma once
 #include "common.cuh"
 #include "engine_bits.cuh"
+#include "engine_group.cuh"
 #include "engine_u8.cuh"
 
 namespace sdim {
@@ -26,6 +27,7 @@ __device__ __forceinline__ void run_shot(const CircuitDesc& c, long long shot_lo
   const int n = c.n, d = c.d;
   const size_t tb = 4 * (size_t)n * n + 2 * (size_t)n;
   uint32_t mord = 0, nord = 0;
+  CoinCache coins;
   long long user_ins = 0;
   uint2 w = (c.nops > 0) ? __ldg(c.ops) : make_uint2(0u, 0u);
   for (int i = 0; i < c.nops; ++i) {
@@ -70,9 +72,11 @@ __device__ __forceinline__ void run_shot(const CircuitDesc& c, long long shot_lo
       case OP_N1D:
       case OP_N1F:
       case OP_N1P: {
-        const int2 ab = noise_draw(op, cur.y, d, c.seed, shot, nord);
+        if (coins.coin(c.seed, shot, nord) >= cur.y) {
+          const int2 ab = noise_choice(op, d, c.seed, shot, nord);
+          eng.pauli(lane, q, ab.x ? d - ab.x : 0, ab.y);
+        }
         ++nord;
-        if (ab.x | ab.y) eng.pauli(lane, q, ab.x ? d - ab.x : 0, ab.y);
         break;
       }
       case OP_N1OFF: ++nord; break;
@@ -87,6 +91,127 @@ __device__ __forceinline__ void run_shot(const CircuitDesc& c, long long shot_lo
   }
   if (SNAP && snap_mode == SNAP_FINAL) eng.export_tableau(lane, snap);
   __syncwarp();
+}
+
+// One group of up to 32 shots of one program on one warp (lane = shot for
+// the per-shot work); see engine_group.cuh.  snap_lane >= 0 exports that
+// shot's tableau according to snap_mode.
+template <class G, bool SNAP>
+__device__ __forceinline__ void run_group(const CircuitDesc& c, long long group, uint8_t* slot, int lane,
+                                          int8_t* snap, int snap_mode, int snap_lane, int* status) {
+  G eng(slot, c.n, c.d);
+  eng.init(lane);
+  const long long s_local = group * 32 + lane;
+  const bool active = s_local < (long long)c.nshots;
+  const long long shot = c.shot0 + s_local;
+  uint8_t* out = c.out + (active ? s_local : 0) * (long long)c.nmeas;
+  const int n = c.n, d = c.d;
+  const size_t tb = 4 * (size_t)n * n + 2 * (size_t)n;
+  uint32_t mord = 0, nord = 0;
+  CoinCache coins;
+  long long user_ins = 0;
+  uint2 w = (c.nops > 0) ? __ldg(c.ops) : make_uint2(0u, 0u);
+  for (int i = 0; i < c.nops; ++i) {
+    const uint2 cur = w;
+    if (i + 1 < c.nops) w = __ldg(c.ops + i + 1);
+    const uint32_t op = cur.x & kOpMask;
+    const int q = (int)(cur.x >> 8);
+    if (q >= n) {
+      if (lane == 0) atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+      return;
+    }
+    switch (op) {
+      case OP_NOP: break;
+      case OP_X: eng.pauli(lane, q, d - 1, 0); break;
+      case OP_X_INV: eng.pauli(lane, q, 1, 0); break;
+      case OP_Z: eng.pauli(lane, q, 0, 1); break;
+      case OP_Z_INV: eng.pauli(lane, q, 0, d - 1); break;
+      case OP_H: eng.h(lane, q); break;
+      case OP_H_INV: eng.h_inv(lane, q); break;
+      case OP_P: eng.p(lane, q, false); break;
+      case OP_P_INV: eng.p(lane, q, true); break;
+      case OP_CNOT:
+      case OP_CNOT_INV: {
+        const int t = (int)cur.y;
+        if (t >= n) {
+          if (lane == 0) atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+          return;
+        }
+        eng.cnot(lane, q, t, op == OP_CNOT_INV);
+        break;
+      }
+      case OP_M:
+      case OP_RESET: {
+        int det = 0;
+        const int m = eng.measure(lane, active, q, c.seed, shot, mord, &det);
+        if (SNAP && snap_mode == SNAP_AT_MEASUREMENT) eng.export_shot(lane, snap_lane, snap + (size_t)mord * tb);
+        if (op == OP_RESET) eng.reset_fix(lane, active, q, m);
+        if (active && (int)mord < c.nmeas) out[mord] = (uint8_t)(m | (det << 7));
+        ++mord;
+        break;
+      }
+      case OP_N1D:
+      case OP_N1F:
+      case OP_N1P: {
+        const bool fire = active && coins.coin(c.seed, shot, nord) >= cur.y;
+        if (__any_sync(0xffffffffu, fire)) {
+          int2 ab = make_int2(0, 0);
+          if (fire) ab = noise_choice(op, d, c.seed, shot, nord);
+          eng.shot_pauli(lane, fire, q, ab.x ? d - ab.x : 0, ab.y);
+        }
+        ++nord;
+        break;
+      }
+      case OP_N1OFF: ++nord; break;
+      default:
+        if (lane == 0) atomicCAS(status, DEV_OK, DEV_BAD_OPCODE);
+        return;
+    }
+    if (SNAP && snap_mode == SNAP_EVERY_INSTRUCTION && (cur.x & kOpEnd)) {
+      eng.export_shot(lane, snap_lane, snap + (size_t)user_ins * tb);
+      ++user_ins;
+    }
+  }
+  if (SNAP && snap_mode == SNAP_FINAL) eng.export_shot(lane, snap_lane, snap);
+  __syncwarp();
+}
+
+// Persistent shot-group kernel: items are (program, group of 32 shots).
+template <class G>
+__global__ void __launch_bounds__(1024) k_group_persistent(const CircuitDesc* __restrict__ descs, int ncirc,
+                                                           long long total_items,
+                                                           unsigned long long* __restrict__ counter,
+                                                           uint8_t* gslots, size_t slot_bytes, int smem_slots,
+                                                           int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  uint8_t* slot = smem_slots ? smem + (size_t)warp * slot_bytes
+                             : gslots + ((size_t)blockIdx.x * wpb + warp) * slot_bytes;
+  for (;;) {
+    unsigned long long it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1ull);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if ((long long)it >= total_items) break;
+    int lo = 0, hi = ncirc - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (descs[mid].item_begin <= (long long)it) lo = mid; else hi = mid - 1;
+    }
+    const CircuitDesc c = descs[lo];
+    run_group<G, false>(c, (long long)it - c.item_begin, slot, lane, nullptr, SNAP_NONE, 0, status);
+    if (*(volatile int*)status != DEV_OK) break;
+  }
+}
+
+// One group with the tableau of shot (group * 32 + snap_lane) exported.
+template <class G>
+__global__ void __launch_bounds__(32) k_group_snapshot(const CircuitDesc* __restrict__ desc, long long group,
+                                                       uint8_t* gslot, int smem_slot, int8_t* snap, int snap_mode,
+                                                       int snap_lane, int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const CircuitDesc c = *desc;
+  run_group<G, true>(c, group, smem_slot ? smem : gslot, threadIdx.x & 31, snap, snap_mode, snap_lane, status);
 }
 
 // Persistent batched kernel: every warp owns one tableau slot (shared memory

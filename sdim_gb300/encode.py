@@ -108,7 +108,7 @@ class DeviceProgram:
         info = (C.c_int64 * 8)()
         _lib.check(lib.sdim_circuit_info(ptr, info), ctx.ptr)
         (self.n, self.d, self.num_records, self.num_instructions, self.num_device_ops,
-         self.backend, self.slot_bytes, _) = (int(v) for v in info)
+         self.backend, self.slot_bytes, self.group_slot_bytes) = (int(v) for v in info)
 
     def close(self):
         if getattr(self, "ptr", None):

@@ -119,14 +119,14 @@ class Program:
 
     # ------------------------------------------------------------------
     def sample(self, shots: int, seed: Optional[int] = None, shot0: int = 0, noise: bool = True,
-               plain: bool = False, out: Optional[np.ndarray] = None) -> np.ndarray:
+               plain: bool = False, out: Optional[np.ndarray] = None, per_shot: bool = False) -> np.ndarray:
         """Records of shots [shot0, shot0 + shots) as a (shots, records) uint8
         array, value | deterministic << 7 -- the fast path without Python objects."""
         dp = self.compile(noise)
         s = self._seed(seed)
         if out is None:
             out = np.empty((int(shots), dp.num_records), dtype=np.uint8)
-        flags = _lib.FLAG_PLAIN if plain else 0
+        flags = (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_PER_SHOT if per_shot else 0)
         if shots > 0 and dp.num_records > 0:
             rc = self.context.lib.sdim_run(self.context.ptr, dp.ptr, s, int(shot0), int(shots),
                                            out.ctypes.data, flags)
@@ -137,8 +137,12 @@ class Program:
         self._last = (s, int(shot0) + int(shots) - 1, noise)
         return out
 
-    def snapshot(self, seed: int, shot: int = 0, mode: int = _lib.SNAP_EVERY_INSTRUCTION, noise: bool = True):
-        """Tableau exports (int8, reference block order) and the shot's records."""
+    def snapshot(self, seed: int, shot: int = 0, mode: int = _lib.SNAP_EVERY_INSTRUCTION, noise: bool = True,
+                 per_shot: bool = False):
+        """Tableau exports (int8, reference block order) and the shot's records.
+
+        ``per_shot`` selects the one-warp-per-shot engine; by default the
+        batched engine of the program (the shot-group engine for d = 2) runs."""
         dp = self.compile(noise)
         n = self.num_qudits
         tb = 4 * n * n + 2 * n
@@ -147,7 +151,8 @@ class Program:
         buf = np.empty((max(count, 1), tb), dtype=np.int8)
         rec = np.empty(max(dp.num_records, 1), dtype=np.uint8)
         rc = self.context.lib.sdim_snapshot(self.context.ptr, dp.ptr, int(seed) & 0xFFFFFFFFFFFFFFFF, int(shot),
-                                            int(mode), buf.ctypes.data, rec.ctypes.data)
+                                            int(mode), buf.ctypes.data, rec.ctypes.data,
+                                            _lib.FLAG_PER_SHOT if per_shot else 0)
         _lib.check(rc, self.context.ptr, "snapshot")
         return buf[:count], rec[:dp.num_records]
 

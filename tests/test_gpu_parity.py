@@ -166,3 +166,66 @@ def test_stabilizer_tableau_after_simulate(golden):
     flat = np.concatenate([t.x_block.ravel(), t.z_block.ravel(), t.phase_vector, t.destab_x_block.ravel(),
                            t.destab_z_block.ravel(), t.destab_phase_vector]).astype(np.int8)
     assert np.array_equal(flat, ref)
+
+
+# ---------------------------------------------------------------------------
+# shot-group engine (d = 2): 32 shots per warp share x/z; phases = c + delta_s
+# ---------------------------------------------------------------------------
+def test_group_engine_every_lane_tableau_after_every_instruction():
+    """Noisy small surface code: the full tableau of several shots inside one
+    group (and across groups) equals the oracle's after every instruction."""
+    spec = workloads.surface_memory(3, 2, prob=0.08)
+    prog = Program(spec.build())
+    for shot in (0, 5, 31, 33, 70):
+        snaps, rec = prog.snapshot(17, shot, _lib.SNAP_EVERY_INSTRUCTION)
+        ref = oracle_run([spec], 17, shot, 1, snapshots=True)
+        assert np.array_equal(rec, ref["records"][0]), shot
+        assert np.array_equal(snaps, ref["snapshots"]), shot
+
+
+def test_group_engine_random_circuits_every_lane():
+    for d, seed in ((2, 1), (2, 2)):
+        spec = workloads.all_gates_random(6, d, 160, seed=seed, noise_probs=(0.0, 0.4, 1.0))
+        prog = Program(spec.build())
+        for shot in (0, 7, 30):
+            snaps, rec = prog.snapshot(3, shot, _lib.SNAP_EVERY_INSTRUCTION)
+            ref = oracle_run([spec], 3, shot, 1, snapshots=True)
+            assert np.array_equal(snaps, ref["snapshots"]), (d, seed, shot)
+        snaps, _ = prog.snapshot(3, 9, _lib.SNAP_AT_MEASUREMENT)
+        per_shot, _ = prog.snapshot(3, 9, _lib.SNAP_AT_MEASUREMENT, per_shot=True)
+        assert np.array_equal(snaps, per_shot)
+
+
+@pytest.mark.parametrize("nshots", [1, 31, 45, 97])
+def test_group_engine_partial_groups(nshots):
+    spec = workloads.surface_memory(3, 3, prob=0.05)
+    prog = Program(spec.build())
+    rec = prog.sample(nshots, seed=8, shot0=13)
+    assert np.array_equal(rec, oracle_run([spec], 8, 13, nshots)["records"])
+
+
+def test_group_engine_equals_per_shot_engine_full_size():
+    spec = workloads.surface_memory(7, 7, prob=1e-3)
+    prog = Program(spec.build())
+    a = prog.sample(4096, seed=3)
+    b = prog.sample(4096, seed=3, per_shot=True)
+    assert np.array_equal(a, b)
+
+
+def test_noiseless_surface_code_properties_100k_shots():
+    """Size-independent properties at full size: without noise, round-1
+    Z-check outcomes are 0 and every later round repeats round 1; the
+    deterministic flags are identical in every shot."""
+    spec = workloads.surface_memory(7, 7, noise=False)
+    prog = Program(spec.build())
+    rec = prog.sample(100_000, seed=0)
+    det = rec >> 7
+    assert np.all(det == det[0])
+    vals = (rec & 0x7F).astype(np.int64)
+    n_anc = 48
+    rounds = vals[:, :7 * n_anc].reshape(-1, 7, n_anc)
+    assert np.all(rounds[:, 1:, :] == rounds[:, :1, :])
+    assert np.all(rounds[:, 0, 24:] == 0)          # Z checks start at +1
+    assert np.all(det[0, n_anc:7 * n_anc] == 1)     # later rounds are deterministic
+    frac_one = rounds[:, 0, :24].mean()
+    assert 0.48 < frac_one < 0.52                    # X checks start random
