@@ -122,6 +122,26 @@ double sdim_last_kernel_ms(const sdim_ctx* ctx);
 int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot, int mode,
                   int8_t* out, uint8_t* records_out, unsigned flags);
 
+/* Allocation-free run, for callers that cannot call cudaMalloc (code living
+ * under another framework's allocator, a process whose device memory is
+ * already reserved, or a hot path that must not allocate).  No counterpart
+ * in the reference.  Takes the same op table as sdim_encode_circuit, runs
+ * shots [shot0, shot0 + nshots) with the per-shot engine on the current
+ * device and `stream` (NULL: the legacy default stream), writes
+ * nshots x records bytes to the device buffer out_dev, and waits for it.
+ * It allocates nothing: its scratch (work-queue counter, status word and the
+ * device instruction stream) lives in one fixed file-scope device array of
+ * 1 MiB + 256 B per device, kept until the process exits.  Limits: at most
+ * 131,072 device instructions (CZ and CZ_INV count 3, SWAP 9, M_X 2) and a
+ * tableau that fits in shared memory; larger programs return SDIM_EINVAL.
+ * The first call on a device looks up the array's address and sets kernel
+ * attributes, so make it before any stream capture.  Calls share the array:
+ * each clears its counter and status first, and calls that overlap on the
+ * GPU race.  Errors are written to err (err_len bytes) when err is not NULL. */
+int sdim_run_noalloc(const int32_t* ops, int64_t nops, const double* noise_prob, int n, int d,
+                     uint64_t seed, int64_t shot0, int64_t nshots, uint8_t* out_dev, void* stream,
+                     char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

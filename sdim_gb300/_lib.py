@@ -46,6 +46,8 @@ SIGNATURES = {
     "sdim_last_kernel_ms": (C.c_double, [_P]),
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "sdim_run_noalloc": (C.c_int, [_P, C.c_int64, _P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_int64, _P,
+                                   _P, C.c_char_p, C.c_size_t]),
 }
 
 _lock = threading.Lock()
