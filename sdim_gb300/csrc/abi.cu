@@ -1,5 +1,6 @@
 // C ABI of the GB300 tableau engine: context, program encoder, launch
-// planner and the plain / persistent / snapshot launches.
+// planner and the plain / persistent / snapshot launches.  The kernels live
+// in k_pershot.cu and k_group.cu behind the launch table of variants.cuh.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -9,17 +10,11 @@
 
 #include "../../include/sdim_gb300.h"
 #include "kernels.cuh"
+#include "variants.cuh"
 
 using namespace sdim;
 
 namespace {
-
-// Engine variants.  Per-shot engines (one warp per shot): V_BITS (d = 2),
-// V_U8_* (residue bytes).  Group engines (one warp per 32 shots sharing x/z):
-// V_GBITS (d = 2).
-enum Variant : int { V_BITS = 0, V_U8_3 = 1, V_U8_5 = 2, V_U8_7 = 3, V_U8_GEN = 4, V_GBITS = 5, V_COUNT = 6 };
-
-bool is_group(int v) { return v == V_GBITS; }
 
 struct DevBuf {
   void* p = nullptr;
@@ -41,7 +36,7 @@ struct sdim_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timing_pending = false;
   double last_ms = 0.0;
-  int smem_attr_set[V_COUNT] = {0, 0, 0, 0, 0, 0};
+  int smem_attr_set[V_COUNT] = {};
 };
 
 struct sdim_circuit {
@@ -49,8 +44,9 @@ struct sdim_circuit {
   int n = 0, d = 0, nmeas = 0;
   int64_t nops_user = 0;
   int nops = 0;
-  int variant = 0;          // per-shot engine (plain form, per-shot snapshots)
-  int gvariant = -1;        // group engine for batched runs, -1 if none
+  int variant = 0;     // per-shot engine (plain form, per-shot snapshots)
+  int gvariant = 0;    // shot-group engine for batched runs
+  int gblock = 32;     // threads of one group team
   size_t slot_bytes = 0;
   size_t gslot_bytes = 0;
   uint2* h_ops = nullptr;  // pinned host copy
@@ -98,8 +94,6 @@ bool is_prime(int d) {
   return true;
 }
 
-size_t round16(size_t b) { return (b + 15) & ~(size_t)15; }
-
 int variant_for(int d) {
   switch (d) {
     case 2: return V_BITS;
@@ -110,95 +104,31 @@ int variant_for(int d) {
   }
 }
 
-int group_variant_for(int d) { return d == 2 ? V_GBITS : -1; }
+// Programs with at least this many qudits run one group per CTA: their
+// measurements touch n x 2n residues, which one warp would walk alone.
+constexpr int kCtaTeamQudits = 160;
 
-size_t slot_bytes_for(int variant, int n) {
-  if (variant == V_GBITS) return round16(GroupBits::slot_bytes(n));
-  return round16(variant == V_BITS ? EngineBits::slot_bytes(n) : SlotU8::bytes(n));
+int group_variant_for(int d, int n) {
+  const bool cta = n >= kCtaTeamQudits;
+  switch (d) {
+    case 2: return cta ? V_GBITS_C : V_GBITS_W;
+    case 3: return cta ? V_GU8_3_C : V_GU8_3_W;
+    case 5: return cta ? V_GU8_5_C : V_GU8_5_W;
+    case 7: return cta ? V_GU8_7_C : V_GU8_7_W;
+    default: return cta ? V_GU8_GEN_C : V_GU8_GEN_W;
+  }
 }
 
-// ---------------------------------------------------------------------------
-// per-engine kernel table
-// ---------------------------------------------------------------------------
-template <class E>
-struct KernelSet {
-  static cudaError_t set_smem(int bytes) {
-    cudaError_t e = cudaFuncSetAttribute(k_persistent<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_single<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_snapshot<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  }
-  static int occupancy(int block, size_t smem) {
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_persistent<E>, block, smem) != cudaSuccess) {
-      cudaGetLastError();
-      return 1;
-    }
-    return std::max(nb, 1);
-  }
-  static void persistent(dim3 g, dim3 b, size_t smem, cudaStream_t s, const CircuitDesc* descs, int nc,
-                         long long total, unsigned long long* counter, uint8_t* gslots, size_t slot,
-                         int smem_slots, int* status) {
-    k_persistent<E><<<g, b, smem, s>>>(descs, nc, total, counter, gslots, slot, smem_slots, status);
-  }
-  static void single(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gslot,
-                     int smem_slot, int* status) {
-    k_single<E><<<1, 32, smem, s>>>(desc, shot, gslot, smem_slot, status);
-  }
-  static void snapshot(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gslot,
-                       int smem_slot, int8_t* snap, int mode, int* status) {
-    k_snapshot<E><<<1, 32, smem, s>>>(desc, shot, gslot, smem_slot, snap, mode, status);
-  }
-  static void group_snapshot(size_t, cudaStream_t, const CircuitDesc*, long long, uint8_t*, int, int8_t*, int, int,
-                             int*) {}
-};
-
-template <class G>
-struct GroupSet {
-  static cudaError_t set_smem(int bytes) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_group_persistent<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_group_snapshot<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  }
-  static int occupancy(int block, size_t smem) {
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_group_persistent<G>, block, smem) != cudaSuccess) {
-      cudaGetLastError();
-      return 1;
-    }
-    return std::max(nb, 1);
-  }
-  static void persistent(dim3 g, dim3 b, size_t smem, cudaStream_t s, const CircuitDesc* descs, int nc,
-                         long long total, unsigned long long* counter, uint8_t* gslots, size_t slot,
-                         int smem_slots, int* status) {
-    k_group_persistent<G><<<g, b, smem, s>>>(descs, nc, total, counter, gslots, slot, smem_slots, status);
-  }
-  static void single(size_t, cudaStream_t, const CircuitDesc*, long long, uint8_t*, int, int*) {}
-  static void snapshot(size_t, cudaStream_t, const CircuitDesc*, long long, uint8_t*, int, int8_t*, int, int*) {}
-  static void group_snapshot(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long group, uint8_t* gslot,
-                             int smem_slot, int8_t* snap, int mode, int lane, int* status) {
-    k_group_snapshot<G><<<1, 32, smem, s>>>(desc, group, gslot, smem_slot, snap, mode, lane, status);
-  }
-};
-
-template <class F>
-void with_engine(int variant, F&& f) {
-  switch (variant) {
-    case V_BITS: f(KernelSet<EngineBits>()); break;
-    case V_U8_3: f(KernelSet<EngineU8<3>>()); break;
-    case V_U8_5: f(KernelSet<EngineU8<5>>()); break;
-    case V_U8_7: f(KernelSet<EngineU8<7>>()); break;
-    case V_GBITS: f(GroupSet<GroupBits>()); break;
-    default: f(KernelSet<EngineU8<0>>()); break;
-  }
+// threads of a CTA team: a power of two near n, 64 to 512
+int cta_block_for(int n) {
+  int b = 64;
+  while (b < n && b < 512) b <<= 1;
+  return b;
 }
 
 int set_smem_attr(sdim_ctx* ctx, int variant) {
   if (ctx->smem_attr_set[variant]) return SDIM_OK;
-  cudaError_t e = cudaSuccess;
-  with_engine(variant, [&](auto ks) { e = decltype(ks)::set_smem(ctx->smem_optin); });
+  const cudaError_t e = variant_ops(variant).set_smem(ctx->smem_optin);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFuncSetAttribute");
   ctx->smem_attr_set[variant] = 1;
   return SDIM_OK;
@@ -206,30 +136,40 @@ int set_smem_attr(sdim_ctx* ctx, int variant) {
 
 struct Plan {
   bool smem_slots;
-  int warps;    // warps (tableau slots) per block
-  int blocks;   // grid size
-  size_t slot;  // bytes per slot
+  int team_threads;  // 32 for warp teams
+  int slots_per_block;
+  int blocks;
+  size_t slot;
 };
 
-Plan plan_group(const sdim_ctx* ctx, int variant, size_t slot, long long items, bool force_gmem) {
+Plan plan_launch(const sdim_ctx* ctx, int variant, size_t slot, long long items, int cta_block,
+                 bool force_gmem) {
+  const VariantOps& ops = variant_ops(variant);
   Plan p;
   p.slot = slot;
   p.smem_slots = !force_gmem && slot <= (size_t)ctx->smem_optin;
-  if (p.smem_slots) {
-    p.warps = (int)std::min<size_t>(32, (size_t)ctx->smem_optin / slot);
-    int occ = 1;
-    with_engine(variant, [&](auto ks) { occ = decltype(ks)::occupancy(p.warps * 32, p.warps * slot); });
-    long long need = (items + p.warps - 1) / p.warps;
-    p.blocks = (int)std::max<long long>(1, std::min<long long>((long long)ctx->num_sms * occ, need));
+  p.team_threads = ops.cta ? cta_block : 32;
+  if (ops.cta) {
+    p.slots_per_block = 1;
+  } else if (p.smem_slots) {
+    p.slots_per_block = (int)std::min<size_t>(32, (size_t)ctx->smem_optin / slot);
+    // spread the items over every SM before stacking more warps on one
+    const long long per_sm = (items + ctx->num_sms - 1) / ctx->num_sms;
+    if (per_sm < p.slots_per_block) p.slots_per_block = (int)std::max<long long>(1, per_sm);
   } else {
-    p.warps = 4;
-    int occ = 1;
-    with_engine(variant, [&](auto ks) { occ = decltype(ks)::occupancy(p.warps * 32, 0); });
-    long long by_budget = (long long)(ctx->gmem_slot_budget / (slot * p.warps));
-    long long need = (items + p.warps - 1) / p.warps;
-    p.blocks = (int)std::max<long long>(
-        1, std::min<long long>(std::min<long long>((long long)ctx->num_sms * occ, need), by_budget));
+    p.slots_per_block = 4;
   }
+  const int block = p.team_threads * p.slots_per_block;
+  const size_t smem = p.smem_slots ? slot * p.slots_per_block : 0;
+  const int occ = ops.occupancy(block, smem);
+  long long blocks = (long long)ctx->num_sms * occ;
+  const long long need = (items + p.slots_per_block - 1) / p.slots_per_block;
+  blocks = std::min(blocks, need);
+  if (!p.smem_slots) {
+    const long long by_budget = (long long)(ctx->gmem_slot_budget / (slot * p.slots_per_block));
+    blocks = std::min(blocks, std::max<long long>(1, by_budget));
+  }
+  p.blocks = (int)std::max<long long>(1, blocks);
   return p;
 }
 
@@ -267,16 +207,17 @@ struct Job {
   uint8_t* out_dev;
 };
 
-// Engine used for a job: the group engine for batched runs when the
-// circuit has one (unless SDIM_FLAG_PER_SHOT), else the per-shot engine.
+// Engine used for a job: the shot-group engine for batched runs (unless
+// SDIM_FLAG_PER_SHOT), the per-shot engine for the plain form.
 int job_variant(const sdim_circuit* c, unsigned flags) {
-  if (!(flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT)) && c->gvariant >= 0) return c->gvariant;
+  if (!(flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT))) return c->gvariant;
   return c->variant;
 }
 
 // Launches every job, grouped by engine variant: one persistent launch per
 // variant (or one single-warp launch per shot with SDIM_FLAG_PLAIN).  Work
-// items are shots for per-shot engines and 32-shot groups for group engines.
+// items are shots for per-shot engines and 32-shot groups for group engines;
+// inside a variant the most expensive programs are queued first.
 int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned flags) {
   const bool plain = flags & SDIM_FLAG_PLAIN;
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
@@ -287,23 +228,24 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     return rc;
   std::vector<int> var(jobs.size());
   for (size_t i = 0; i < jobs.size(); ++i) var[i] = job_variant(jobs[i].c, flags);
-  // group by variant; inside a group, most expensive circuits first
   std::vector<int> order(jobs.size());
   for (size_t i = 0; i < jobs.size(); ++i) order[i] = (int)i;
-  auto cost = [&](const Job& j) { return (double)j.c->nops * (double)j.c->n; };
+  auto cost = [&](const Job& j) { return (double)j.c->nops * (double)j.c->n * (double)j.c->n; };
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     if (var[a] != var[b]) return var[a] < var[b];
     return cost(jobs[a]) > cost(jobs[b]);
   });
   std::vector<CircuitDesc> hd(jobs.size());
-  struct Group { int variant, begin, end; long long items; size_t slot; };
+  struct Group { int variant, begin, end; long long items; size_t slot; int block; };
   std::vector<Group> groups;
   for (size_t k = 0; k < order.size(); ++k) {
     const Job& j = jobs[order[k]];
     const int v = var[order[k]];
-    if (groups.empty() || groups.back().variant != v) groups.push_back(Group{v, (int)k, (int)k, 0, 0});
+    const bool grp = variant_ops(v).group;
+    if (groups.empty() || groups.back().variant != v) groups.push_back(Group{v, (int)k, (int)k, 0, 0, 32});
     Group& g = groups.back();
     CircuitDesc& dsc = hd[k];
+    std::memset(&dsc, 0, sizeof(dsc));
     dsc.ops = j.c->d_ops;
     dsc.out = j.out_dev;
     dsc.seed = j.seed;
@@ -314,9 +256,9 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     dsc.d = j.c->d;
     dsc.nmeas = j.c->nmeas;
     dsc.nshots = (int)j.nshots;
-    dsc.slot = 0;
-    g.items += is_group(v) ? (j.nshots + 31) / 32 : j.nshots;
-    g.slot = std::max(g.slot, is_group(v) ? j.c->gslot_bytes : j.c->slot_bytes);
+    g.items += grp ? (j.nshots + 31) / 32 : j.nshots;
+    g.slot = std::max(g.slot, grp ? j.c->gslot_bytes : j.c->slot_bytes);
+    g.block = std::max(g.block, grp ? j.c->gblock : 32);
     g.end = (int)k + 1;
   }
   CircuitDesc* ddesc = static_cast<CircuitDesc*>(ctx->descs.p);
@@ -330,27 +272,22 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     const Group& g = groups[gi];
     if (g.items == 0) continue;
     if ((rc = set_smem_attr(ctx, g.variant)) != SDIM_OK) return rc;
+    const VariantOps& ops = variant_ops(g.variant);
     if (plain) {
       const bool sm = !force_gmem && g.slot <= (size_t)ctx->smem_optin;
       if (!sm && (rc = ensure(ctx, ctx->gslots, g.slot)) != SDIM_OK) return rc;
-      for (int k = g.begin; k < g.end; ++k) {
-        for (long long sh = 0; sh < hd[k].nshots; ++sh) {
-          with_engine(g.variant, [&](auto ks) {
-            decltype(ks)::single(sm ? g.slot : 0, s, ddesc + k, sh, static_cast<uint8_t*>(ctx->gslots.p),
-                                 sm ? 1 : 0, status);
-          });
-        }
-      }
+      for (int k = g.begin; k < g.end; ++k)
+        for (long long sh = 0; sh < hd[k].nshots; ++sh)
+          ops.single(sm ? g.slot : 0, s, ddesc + k, sh, static_cast<uint8_t*>(ctx->gslots.p), sm ? 1 : 0, status);
     } else {
-      Plan p = plan_group(ctx, g.variant, g.slot, g.items, force_gmem);
-      if (!p.smem_slots && (rc = ensure(ctx, ctx->gslots, p.slot * p.warps * (size_t)p.blocks)) != SDIM_OK)
+      const Plan p = plan_launch(ctx, g.variant, g.slot, g.items, g.block, force_gmem);
+      if (!p.smem_slots &&
+          (rc = ensure(ctx, ctx->gslots, p.slot * p.slots_per_block * (size_t)p.blocks)) != SDIM_OK)
         return rc;
-      unsigned long long* counter = static_cast<unsigned long long*>(ctx->counters.p) + gi % V_COUNT;
-      with_engine(g.variant, [&](auto ks) {
-        decltype(ks)::persistent(dim3(p.blocks), dim3(p.warps * 32), p.smem_slots ? p.slot * p.warps : 0, s,
-                                 ddesc + g.begin, g.end - g.begin, g.items, counter,
-                                 static_cast<uint8_t*>(ctx->gslots.p), p.slot, p.smem_slots ? 1 : 0, status);
-      });
+      unsigned long long* counter = static_cast<unsigned long long*>(ctx->counters.p) + g.variant;
+      ops.persistent(dim3(p.blocks), dim3(p.team_threads * p.slots_per_block),
+                     p.smem_slots ? p.slot * p.slots_per_block : 0, s, ddesc + g.begin, g.end - g.begin, g.items,
+                     counter, static_cast<uint8_t*>(ctx->gslots.p), p.slot, p.smem_slots ? 1 : 0, status);
     }
     cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch");
@@ -529,9 +466,10 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
   c->nops_user = nops;
   c->nops = (int)dev.size();
   c->variant = variant_for(d);
-  c->slot_bytes = slot_bytes_for(c->variant, n);
-  c->gvariant = group_variant_for(d);
-  c->gslot_bytes = c->gvariant >= 0 ? slot_bytes_for(c->gvariant, n) : 0;
+  c->slot_bytes = variant_ops(c->variant).slot_bytes(n);
+  c->gvariant = group_variant_for(d, n);
+  c->gslot_bytes = variant_ops(c->gvariant).slot_bytes(n);
+  c->gblock = variant_ops(c->gvariant).cta ? cta_block_for(n) : 32;
   const size_t bytes = std::max<size_t>(dev.size(), 1) * sizeof(uint2);
   cudaError_t e = cudaMallocHost(&c->h_ops, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ops, bytes);
@@ -569,7 +507,7 @@ int sdim_circuit_info(const sdim_circuit* c, int64_t info[8]) {
   info[2] = c->nmeas;
   info[3] = c->nops_user;
   info[4] = c->nops;
-  info[5] = c->variant == V_BITS ? 1 : 0;
+  info[5] = c->d == 2 ? 1 : 0;
   info[6] = (int64_t)c->slot_bytes;
   info[7] = (int64_t)c->gslot_bytes;
   return SDIM_OK;
@@ -691,7 +629,8 @@ int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t s
                        : mode == SDIM_SNAP_AT_MEASUREMENT ? (size_t)c->nmeas
                                                           : (size_t)1;
   const int v = job_variant(c, flags);
-  const bool grp = is_group(v);
+  const VariantOps& ops = variant_ops(v);
+  const bool grp = ops.group;
   const size_t slot = grp ? c->gslot_bytes : c->slot_bytes;
   // a group snapshot runs the 32 shots [shot - lane, shot - lane + 32) and exports lane's
   const int lane = grp ? (int)(shot % 32) : 0;
@@ -717,16 +656,9 @@ int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t s
   cudaStream_t s = ctx->stream;
   CK(cudaMemcpyAsync(ctx->descs.p, &dsc, sizeof(dsc), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(ctx->status.p, 0, sizeof(int), s));
-  const CircuitDesc* dd = static_cast<const CircuitDesc*>(ctx->descs.p);
-  uint8_t* gs = static_cast<uint8_t*>(ctx->gslots.p);
-  int8_t* sp = static_cast<int8_t*>(ctx->snap.p);
-  int* st = static_cast<int*>(ctx->status.p);
-  with_engine(v, [&](auto ks) {
-    if (grp)
-      decltype(ks)::group_snapshot(sm ? slot : 0, s, dd, 0, gs, sm ? 1 : 0, sp, mode, lane, st);
-    else
-      decltype(ks)::snapshot(sm ? slot : 0, s, dd, 0, gs, sm ? 1 : 0, sp, mode, st);
-  });
+  ops.snapshot(dim3(ops.cta ? c->gblock : 32), sm ? slot : 0, s, static_cast<const CircuitDesc*>(ctx->descs.p),
+               0, static_cast<uint8_t*>(ctx->gslots.p), sm ? 1 : 0, static_cast<int8_t*>(ctx->snap.p), mode, lane,
+               static_cast<int*>(ctx->status.p));
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return cuda_fail(ctx, le, "snapshot launch");
   if (count * tb) CK(cudaMemcpyAsync(out, ctx->snap.p, count * tb, cudaMemcpyDeviceToHost, s));

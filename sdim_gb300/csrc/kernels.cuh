@@ -7,7 +7,8 @@
 #pragma once
 #include "common.cuh"
 #include "engine_bits.cuh"
-#include "engine_group.cuh"
+#include "group_bits.cuh"
+#include "group_u8.cuh"
 #include "engine_u8.cuh"
 
 namespace sdim {
@@ -93,18 +94,22 @@ __device__ __forceinline__ void run_shot(const CircuitDesc& c, long long shot_lo
   __syncwarp();
 }
 
-// One group of up to 32 shots of one program on one warp (lane = shot for
-// the per-shot work); see engine_group.cuh.  snap_lane >= 0 exports that
+// One group of up to 32 shots of one program on one team.  Thread t < 32
+// owns shot t's scalar work (coins, outcomes, records); the engine spreads
+// per-shot vector work over (shot, chunk) pairs.  snap_lane >= 0 exports that
 // shot's tableau according to snap_mode.
 template <class G, bool SNAP>
-__device__ __forceinline__ void run_group(const CircuitDesc& c, long long group, uint8_t* slot, int lane,
-                                          int8_t* snap, int snap_mode, int snap_lane, int* status) {
-  G eng(slot, c.n, c.d);
-  eng.init(lane);
-  const long long s_local = group * 32 + lane;
-  const bool active = s_local < (long long)c.nshots;
-  const long long shot = c.shot0 + s_local;
-  uint8_t* out = c.out + (active ? s_local : 0) * (long long)c.nmeas;
+__device__ __forceinline__ void run_tgroup(const CircuitDesc& c, long long group, G& eng, int8_t* snap,
+                                           int snap_mode, int snap_lane, int* status) {
+  const int t = eng.tm.t;
+  const int s = t & 31;
+  const long long base = group * 32;
+  const long long left = (long long)c.nshots - base;
+  const int nact = left >= 32 ? 32 : (int)left;
+  eng.init(nact);
+  const bool active = t < 32 && s < nact;
+  const long long shot = c.shot0 + base + s;
+  uint8_t* out = c.out + (active ? base + s : 0) * (long long)c.nmeas;
   const int n = c.n, d = c.d;
   const size_t tb = 4 * (size_t)n * n + 2 * (size_t)n;
   uint32_t mord = 0, nord = 0;
@@ -117,35 +122,35 @@ __device__ __forceinline__ void run_group(const CircuitDesc& c, long long group,
     const uint32_t op = cur.x & kOpMask;
     const int q = (int)(cur.x >> 8);
     if (q >= n) {
-      if (lane == 0) atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+      if (t == 0) atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
       return;
     }
     switch (op) {
       case OP_NOP: break;
-      case OP_X: eng.pauli(lane, q, d - 1, 0); break;
-      case OP_X_INV: eng.pauli(lane, q, 1, 0); break;
-      case OP_Z: eng.pauli(lane, q, 0, 1); break;
-      case OP_Z_INV: eng.pauli(lane, q, 0, d - 1); break;
-      case OP_H: eng.h(lane, q); break;
-      case OP_H_INV: eng.h_inv(lane, q); break;
-      case OP_P: eng.p(lane, q, false); break;
-      case OP_P_INV: eng.p(lane, q, true); break;
+      case OP_X: eng.pauli(q, d - 1, 0); break;
+      case OP_X_INV: eng.pauli(q, 1, 0); break;
+      case OP_Z: eng.pauli(q, 0, 1); break;
+      case OP_Z_INV: eng.pauli(q, 0, d - 1); break;
+      case OP_H: eng.h(q); break;
+      case OP_H_INV: eng.h_inv(q); break;
+      case OP_P: eng.p(q, false); break;
+      case OP_P_INV: eng.p(q, true); break;
       case OP_CNOT:
       case OP_CNOT_INV: {
-        const int t = (int)cur.y;
-        if (t >= n) {
-          if (lane == 0) atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+        const int tq = (int)cur.y;
+        if (tq >= n) {
+          if (t == 0) atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
           return;
         }
-        eng.cnot(lane, q, t, op == OP_CNOT_INV);
+        eng.cnot(q, tq, op == OP_CNOT_INV);
         break;
       }
       case OP_M:
       case OP_RESET: {
-        int det = 0;
-        const int m = eng.measure(lane, active, q, c.seed, shot, mord, &det);
-        if (SNAP && snap_mode == SNAP_AT_MEASUREMENT) eng.export_shot(lane, snap_lane, snap + (size_t)mord * tb);
-        if (op == OP_RESET) eng.reset_fix(lane, active, q, m);
+        const int det = eng.measure(q, c.seed, c.shot0 + base, mord);
+        if (SNAP && snap_mode == SNAP_AT_MEASUREMENT) eng.export_shot(snap_lane, snap + (size_t)mord * tb);
+        const int m = (t < 32) ? eng.shot_m[s] : 0;
+        if (op == OP_RESET) eng.reset_fix(q);
         if (active && (int)mord < c.nmeas) out[mord] = (uint8_t)(m | (det << 7));
         ++mord;
         break;
@@ -154,35 +159,49 @@ __device__ __forceinline__ void run_group(const CircuitDesc& c, long long group,
       case OP_N1F:
       case OP_N1P: {
         const bool fire = active && coins.coin(c.seed, shot, nord) >= cur.y;
-        if (__any_sync(0xffffffffu, fire)) {
-          int2 ab = make_int2(0, 0);
-          if (fire) ab = noise_choice(op, d, c.seed, shot, nord);
-          eng.shot_pauli(lane, fire, q, ab.x ? d - ab.x : 0, ab.y);
+        if (eng.tm.any(fire)) {
+          if (t < 32) {
+            int2 ab = make_int2(0, 0);
+            if (fire) ab = noise_choice(op, d, c.seed, shot, nord);
+            eng.set_shot_ab(s, ab.x ? d - ab.x : 0, ab.y);
+          }
+          eng.shot_pauli(q);
         }
         ++nord;
         break;
       }
       case OP_N1OFF: ++nord; break;
       default:
-        if (lane == 0) atomicCAS(status, DEV_OK, DEV_BAD_OPCODE);
+        if (t == 0) atomicCAS(status, DEV_OK, DEV_BAD_OPCODE);
         return;
     }
     if (SNAP && snap_mode == SNAP_EVERY_INSTRUCTION && (cur.x & kOpEnd)) {
-      eng.export_shot(lane, snap_lane, snap + (size_t)user_ins * tb);
+      eng.export_shot(snap_lane, snap + (size_t)user_ins * tb);
       ++user_ins;
     }
   }
-  if (SNAP && snap_mode == SNAP_FINAL) eng.export_shot(lane, snap_lane, snap);
-  __syncwarp();
+  if (SNAP && snap_mode == SNAP_FINAL) eng.export_shot(snap_lane, snap);
+  eng.tm.sync();
 }
 
-// Persistent shot-group kernel: items are (program, group of 32 shots).
 template <class G>
-__global__ void __launch_bounds__(1024) k_group_persistent(const CircuitDesc* __restrict__ descs, int ncirc,
-                                                           long long total_items,
-                                                           unsigned long long* __restrict__ counter,
-                                                           uint8_t* gslots, size_t slot_bytes, int smem_slots,
-                                                           int* status) {
+__device__ __forceinline__ int find_desc(const CircuitDesc* descs, int ncirc, long long it) {
+  int lo = 0, hi = ncirc - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (descs[mid].item_begin <= it) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Persistent shot-group kernel, one warp per group: items are
+// (program, group of 32 shots); each warp owns one slot (shared memory when
+// smem_slots != 0, else global memory).
+template <class G>
+__global__ void __launch_bounds__(1024) k_group_warp(const CircuitDesc* __restrict__ descs, int ncirc,
+                                                     long long total_items, unsigned long long* __restrict__ counter,
+                                                     uint8_t* gslots, size_t slot_bytes, int smem_slots,
+                                                     int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
@@ -193,25 +212,56 @@ __global__ void __launch_bounds__(1024) k_group_persistent(const CircuitDesc* __
     if (lane == 0) it = atomicAdd(counter, 1ull);
     it = __shfl_sync(0xffffffffu, it, 0);
     if ((long long)it >= total_items) break;
-    int lo = 0, hi = ncirc - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (descs[mid].item_begin <= (long long)it) lo = mid; else hi = mid - 1;
-    }
-    const CircuitDesc c = descs[lo];
-    run_group<G, false>(c, (long long)it - c.item_begin, slot, lane, nullptr, SNAP_NONE, 0, status);
+    const int ci = find_desc<G>(descs, ncirc, (long long)it);
+    const CircuitDesc c = descs[ci];
+    G eng(slot, c.n, c.d, WarpTeam());
+    run_tgroup<G, false>(c, (long long)it - c.item_begin, eng, nullptr, SNAP_NONE, 0, status);
     if (*(volatile int*)status != DEV_OK) break;
   }
 }
 
-// One group with the tableau of shot (group * 32 + snap_lane) exported.
+// Persistent shot-group kernel, one CTA per group (programs with many
+// qudits): the whole CTA shares one slot.
 template <class G>
-__global__ void __launch_bounds__(32) k_group_snapshot(const CircuitDesc* __restrict__ desc, long long group,
-                                                       uint8_t* gslot, int smem_slot, int8_t* snap, int snap_mode,
-                                                       int snap_lane, int* status) {
+__global__ void __launch_bounds__(512) k_group_cta(const CircuitDesc* __restrict__ descs, int ncirc,
+                                                   long long total_items, unsigned long long* __restrict__ counter,
+                                                   uint8_t* gslots, size_t slot_bytes, int smem_slots, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int red[40];
+  __shared__ long long item;
+  uint8_t* slot = smem_slots ? smem : gslots + (size_t)blockIdx.x * slot_bytes;
+  for (;;) {
+    if (threadIdx.x == 0) item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long it = item;
+    __syncthreads();
+    if (it >= total_items) break;
+    const int ci = find_desc<G>(descs, ncirc, it);
+    const CircuitDesc c = descs[ci];
+    G eng(slot, c.n, c.d, CtaTeam(red));
+    run_tgroup<G, false>(c, it - c.item_begin, eng, nullptr, SNAP_NONE, 0, status);
+    __syncthreads();
+    if (*(volatile int*)status != DEV_OK) break;
+  }
+}
+
+// One group with the tableau of shot (group * 32 + snap_lane) exported;
+// CTA-team engines run with blockDim threads, warp-team engines with 32.
+template <class G, bool CTA>
+__global__ void __launch_bounds__(512) k_group_snapshot(const CircuitDesc* __restrict__ desc, long long group,
+                                                        uint8_t* gslot, int smem_slot, int8_t* snap, int snap_mode,
+                                                        int snap_lane, int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int red[40];
   const CircuitDesc c = *desc;
-  run_group<G, true>(c, group, smem_slot ? smem : gslot, threadIdx.x & 31, snap, snap_mode, snap_lane, status);
+  uint8_t* slot = smem_slot ? smem : gslot;
+  if constexpr (CTA) {
+    G eng(slot, c.n, c.d, CtaTeam(red));
+    run_tgroup<G, true>(c, group, eng, snap, snap_mode, snap_lane, status);
+  } else {
+    G eng(slot, c.n, c.d, WarpTeam());
+    run_tgroup<G, true>(c, group, eng, snap, snap_mode, snap_lane, status);
+  }
 }
 
 // Persistent batched kernel: every warp owns one tableau slot (shared memory

@@ -1,0 +1,59 @@
+// Thread teams: the threads that share one tableau slot.  WarpTeam is one
+// warp (up to 32 slots per CTA); CtaTeam is a whole CTA (one slot per CTA,
+// for programs with many qudits).  Both expose the same strided-loop index,
+// barrier and reductions, so one engine source serves both.
+#pragma once
+#include <climits>
+#include "common.cuh"
+
+namespace sdim {
+
+struct WarpTeam {
+  int t;
+  __device__ WarpTeam() : t(threadIdx.x & 31) {}
+  __device__ __forceinline__ int size() const { return 32; }
+  __device__ __forceinline__ void sync() const { __syncwarp(); }
+  __device__ __forceinline__ int min(int v) const { return __reduce_min_sync(0xffffffffu, v); }
+  __device__ __forceinline__ int add(int v) const { return __reduce_add_sync(0xffffffffu, v); }
+  __device__ __forceinline__ unsigned bxor(unsigned v) const { return __reduce_xor_sync(0xffffffffu, v); }
+  __device__ __forceinline__ bool any(bool b) const { return __any_sync(0xffffffffu, b); }
+  __device__ __forceinline__ bool leader() const { return t == 0; }
+};
+
+// red: at least 33 ints of shared memory owned by the team.
+struct CtaTeam {
+  int t, nt;
+  int* red;
+  __device__ CtaTeam(int* red_) : t(threadIdx.x), nt(blockDim.x), red(red_) {}
+  __device__ __forceinline__ int size() const { return nt; }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ bool leader() const { return t == 0; }
+  __device__ __forceinline__ bool any(bool b) const { return __syncthreads_or(b) != 0; }
+  template <class Op>
+  __device__ __forceinline__ int reduce(int v, int ident, Op op) const {
+    const int lane = t & 31, w = t >> 5, nw = (nt + 31) >> 5;
+    for (int off = 16; off > 0; off >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      int x = lane < nw ? red[lane] : ident;
+      for (int off = 16; off > 0; off >>= 1) x = op(x, __shfl_xor_sync(0xffffffffu, x, off));
+      if (lane == 0) red[32] = x;
+    }
+    __syncthreads();
+    const int r = red[32];
+    __syncthreads();
+    return r;
+  }
+  __device__ __forceinline__ int min(int v) const {
+    return reduce(v, INT_MAX, [](int a, int b) { return a < b ? a : b; });
+  }
+  __device__ __forceinline__ int add(int v) const {
+    return reduce(v, 0, [](int a, int b) { return a + b; });
+  }
+  __device__ __forceinline__ unsigned bxor(unsigned v) const {
+    return (unsigned)reduce((int)v, 0, [](int a, int b) { return a ^ b; });
+  }
+};
+
+}  // namespace sdim

@@ -1,0 +1,56 @@
+// Launch table of the engine variants.  Each variant's kernels are
+// instantiated in their own translation unit (k_pershot.cu, k_group.cu) so
+// the library compiles in parallel; abi.cu only sees these function pointers.
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sdim {
+
+enum Variant : int {
+  // per-shot engines: one warp and one full tableau per shot
+  V_BITS = 0,
+  V_U8_3,
+  V_U8_5,
+  V_U8_7,
+  V_U8_GEN,
+  // shot-group engines: 32 shots share x / z; W = one warp per group, C = one CTA per group
+  V_GBITS_W,
+  V_GBITS_C,
+  V_GU8_3_W,
+  V_GU8_5_W,
+  V_GU8_7_W,
+  V_GU8_GEN_W,
+  V_GU8_3_C,
+  V_GU8_5_C,
+  V_GU8_7_C,
+  V_GU8_GEN_C,
+  V_COUNT
+};
+
+struct VariantOps {
+  int group;  // 1: items are 32-shot groups
+  int cta;    // 1: one CTA per slot (block threads given by the planner)
+  size_t (*slot_bytes)(int n);
+  cudaError_t (*set_smem)(int bytes);
+  int (*occupancy)(int block, size_t smem);
+  void (*persistent)(dim3 grid, dim3 block, size_t smem, cudaStream_t s, const CircuitDesc* descs, int nc,
+                     long long total, unsigned long long* counter, uint8_t* gslots, size_t slot, int smem_slots,
+                     int* status);
+  // per-shot engines: one shot, one warp
+  void (*single)(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gslot, int smem_slot,
+                 int* status);
+  // tableau export of one shot (per-shot engines: shot index; group engines:
+  // group 0 of desc, exported lane)
+  void (*snapshot)(dim3 block, size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot_or_group,
+                   uint8_t* gslot, int smem_slot, int8_t* snap, int mode, int lane, int* status);
+};
+
+const VariantOps& pershot_ops(int variant);
+const VariantOps& group_ops(int variant);
+
+inline const VariantOps& variant_ops(int v) { return v < V_GBITS_W ? pershot_ops(v) : group_ops(v); }
+
+}  // namespace sdim
