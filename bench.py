@@ -1,25 +1,33 @@
 #!/usr/bin/env python
-"""Benchmark: tableau gate-updates/s on the d=2 surface-code memory workload.
+"""Benchmark: tableau gate-updates/s of the GB300 tableau engine.
 
-Workload (one "step"): rotated distance-7 surface-code memory circuit,
-49 data + 48 ancilla qubits, 7 rounds (H on X ancillas, 4-step CNOT schedule,
-H, MEASURE+RESET of all ancillas), depolarizing N1 (p = 1e-3) after every gate
-on every qudit it touches, final MEASURE of the data; 100,000 shots in one
-persistent launch per GPU (bit-plane tableaux in shared memory).  A
-gate-update is one circuit instruction (N1, M and RESET included) applied to
-one shot's tableau.
+A gate-update is one circuit instruction (N1, M and RESET included) applied
+to one shot's tableau; a "step" is one batched run of the whole workload.
 
-Arms:
-  default            the GB300 engine (persistent batched kernel); value from
-                     CUDA events on the launching stream, e2e through the
-                     C ABI with pinned host buffers and copies inside the
-                     timed region; plain per-shot form and the CPU oracle on
-                     a bounded sample reported beside it.
-  --impl reference   the CPU restatement of the reference's algorithm
-                     (C oracle, every host core) on a bounded sample per step.
+Workloads (--workload):
+  surface (default)  rotated distance-7 surface-code memory, 97 qubits, 7 rounds
+                     (H on X ancillas, 4-step CNOT schedule, H, MEASURE+RESET of
+                     the 48 ancillas), depolarizing N1 p=1e-3 after every gate on
+                     every qudit it touches, final MEASURE of the 49 data qubits;
+                     100,000 shots per step in one persistent launch, d=2.
+  pr1                d=3, n=32, 640 gates i.i.d. {H,P,CNOT}, MEASURE all; 1,024 shots.
+  oddd5, oddd7       d in {5,7}, n=256, 2,560 gates (H 25%, P 25%, CNOT 50%),
+                     MEASURE+RESET on 10% every 256 gates, MEASURE all; 4,096 shots.
+  uneven             8,192 programs, n log-uniform in [8,1024], d uniform over
+                     {2,3,5,7}, 4n gates {H,P,CNOT} + MEASURE all, shots uniform in
+                     [1,64]; one persistent launch per engine variant.
 
-Multi-GPU: replicas -- rank r simulates its own shot range
-[r * shots, (r + 1) * shots); no data-path collective (weak scaling).
+Arms: the default is the GB300 engine (shot-group persistent kernels):
+`value` from CUDA events on the launching stream with records in device
+memory, `e2e` through the C ABI with pinned host records and the copies
+inside the timed region; the per-shot engine and the plain form (one
+single-warp launch per shot) on the same inputs, and the CPU oracle on a
+bounded sample, are reported beside it.  `--impl reference` times the CPU
+restatement of the reference's algorithm (the C oracle over every host core)
+on a bounded sample per step.
+
+Multi-GPU: replicas -- rank r runs the same programs on its own shot range
+(shot0 = r * shots), no collective on the data path (weak scaling).
 """
 from __future__ import annotations
 
@@ -49,32 +57,42 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--shots", type=int, default=100_000)
-    ap.add_argument("--distance", type=int, default=7)
-    ap.add_argument("--rounds", type=int, default=7)
-    ap.add_argument("--prob", type=float, default=1e-3)
+    ap.add_argument("--workload", default="surface", choices=["surface", "pr1", "oddd5", "oddd7", "uneven"])
+    ap.add_argument("--shots", type=int, default=None, help="shots per GPU (single-program workloads)")
+    ap.add_argument("--circuits", type=int, default=8192, help="programs of the uneven batch")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-shots", type=int, default=256)
     return ap.parse_args()
 
 
-def workload(args):
-    from sdim_gb300 import workloads
-    return workloads.surface_memory(args.distance, args.rounds, prob=args.prob)
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def single_workload(args):
+    from sdim_gb300 import workloads as W
+    if args.workload == "surface":
+        spec, shots = W.surface_memory(7, 7, prob=1e-3), 100_000
+        desc = ("surface-code memory, rotated distance 7, 7 rounds, depolarizing p=0.001 after every gate, "
+                "d=2, 97 qubits")
+    elif args.workload == "pr1":
+        spec, shots = W.pr1(0), 1024
+        desc = "PR1: d=3, n=32, 640 i.i.d. {H,P,CNOT} gates, MEASURE all 32"
+    else:
+        d = 5 if args.workload == "oddd5" else 7
+        spec, shots = W.odd_d(d, seed=0), 4096
+        desc = (f"odd d={d}, n=256, 2,560 gates (H 25%, P 25%, CNOT 50%), MEASURE+RESET on 10% every 256 gates, "
+                "MEASURE all")
+    return spec, (args.shots or shots), desc
 
 
-def config(args, spec, scaling_note):
-    return {"workload": f"surface-code memory, rotated distance {args.distance}, {args.rounds} rounds, "
-                        f"depolarizing p={args.prob:g} after every gate, d=2",
-            "qudits": spec.num_qudits, "dimension": spec.dimension, "instructions": len(spec.ops),
-            "shots_per_gpu": args.shots, "records_per_shot": spec.num_measurements(),
-            "seed": 0, "l2": "flushed (256 MB write) between timed steps; the flush is outside the events",
-            "parallelism": scaling_note}
+def uneven_items(args):
+    from sdim_gb300 import workloads as W
+    return W.uneven_batch(args.circuits, seed=0)
 
 
 # ---------------------------------------------------------------------------
-# algorithmic bytes per gate-update (residue rows R, phase vector P over 2n)
+# algorithmic bytes (rows R and phase vector P over the 2n generators)
 # ---------------------------------------------------------------------------
 def row_bytes(n, d):
     g = 2 * n
@@ -85,23 +103,8 @@ def row_bytes(n, d):
     return g, g
 
 
-def group_delta_bytes_per_shot(enc, det_row, resets_fired, n, d):
-    """Per-shot phase-delta bytes of the shot-group engine: a random
-    measurement reads and writes the delta row (2P), a deterministic one reads
-    the stabilizer half (P/2), a RESET whose outcome needs a correction reads
-    and writes it (2P).  N1 coins live in registers; fired N1 (rate p) are not
-    counted."""
-    _, P = row_bytes(n, d)
-    total = 0.0
-    j = 0
-    for gid in enc.ops[:, 0].tolist():
-        if gid in (14, 15, 16):
-            total += P / 2 if det_row[j] else 2 * P
-            j += 1
-    return total + 2 * P * resets_fired
-
-
 def algorithmic_bytes_per_shot(enc, det_row, n, d):
+    """Bytes one shot's tableau update touches, per instruction type."""
     R, P = row_bytes(n, d)
     h, p, cx, pauli = 4 * R + 2 * P, 3 * R + 2 * P, 6 * R, R + 2 * P
     m_det, m_rand = n * R + P / 2 + R, 2 * (2 * n * R + P)
@@ -131,6 +134,28 @@ def algorithmic_bytes_per_shot(enc, det_row, n, d):
     return total
 
 
+def group_delta_bytes_per_shot(enc, det_row, resets_fired, n, d):
+    """Per-shot phase-delta bytes of the shot-group engine: a random
+    measurement reads and writes the delta row (2P), a deterministic one reads
+    the stabilizer half (P/2), a RESET whose outcome needs a correction reads
+    and writes it (2P).  N1 coins live in registers; fired N1 (rate p) are not
+    counted."""
+    _, P = row_bytes(n, d)
+    total = 0.0
+    j = 0
+    for gid in enc.ops[:, 0].tolist():
+        if gid in (14, 15, 16):
+            total += P / 2 if det_row[j] else 2 * P
+            j += 1
+    return total + 2 * P * resets_fired
+
+
+def group_bytes(enc, det_row, resets_fired_per_shot, n, d, shots):
+    groups = -(-shots // 32)
+    return (groups * algorithmic_bytes_per_shot(enc, det_row, n, d)
+            + shots * group_delta_bytes_per_shot(enc, det_row, resets_fired_per_shot, n, d))
+
+
 # ---------------------------------------------------------------------------
 class Clocks:
     """nvidia-smi sampling during the timed region."""
@@ -153,6 +178,7 @@ class Clocks:
                  "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        time.sleep(0.25)
 
     def stop(self):
         if self.proc is None:
@@ -188,13 +214,16 @@ def dist_setup():
     return ws, rank, local
 
 
-def cpu_oracle_rate(spec, seconds_budget, seed=0, shot0=0):
-    """C oracle on a bounded sample, every host core: (gate-updates/s, shots, s, threads)."""
+# ---------------------------------------------------------------------------
+# CPU: the C oracle over every host core
+# ---------------------------------------------------------------------------
+def cpu_rate_single(spec, seconds_budget, seed=0, shot0=0):
+    """(gate-updates/s, shots, seconds, threads) on a bounded shot sample."""
     import oracle
     threads = os.cpu_count() or 1
     prog = oracle.OracleProgram([spec], spec.num_qudits, spec.dimension)
-    t0 = time.perf_counter()
     cal = max(threads, 16)
+    t0 = time.perf_counter()
     oracle.simulate(prog, seed, shot0, cal, threads=threads)
     per_shot = (time.perf_counter() - t0) / cal
     shots = int(max(threads, min(200_000, seconds_budget / max(per_shot, 1e-9))))
@@ -204,32 +233,365 @@ def cpu_oracle_rate(spec, seconds_budget, seed=0, shot0=0):
     return len(spec.ops) * shots / dt, shots, dt, threads
 
 
+def cpu_rate_uneven(items, seconds_budget):
+    """C oracle on a systematic sample of the batch, min(shots, 4) shots per program."""
+    import oracle
+    threads = os.cpu_count() or 1
+    units, t_all, used = 0, 0.0, 0
+    order = list(range(0, len(items), 97)) + [i for i in range(len(items)) if i % 97]
+    for i in order:
+        it = items[i]
+        prog = oracle.OracleProgram([it.spec], it.spec.num_qudits, it.spec.dimension)
+        k = min(it.shots, 4)
+        t0 = time.perf_counter()
+        oracle.simulate(prog, it.seed, 0, k, threads=threads)
+        t_all += time.perf_counter() - t0
+        units += len(it.spec.ops) * k
+        used += 1
+        if t_all > seconds_budget:
+            break
+    return units / t_all, used, t_all, threads
+
+
 def run_reference_arm(args):
     ws, rank, _ = dist_setup()
-    spec = workload(args)
     if rank != 0:
         return
     per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
-    for _ in range(args.warmup):
-        cpu_oracle_rate(spec, min(1.0, per_step))
-    rates, samples = [], []
-    t_all = 0.0
+    if args.workload == "uneven":
+        items = uneven_items(args)
+        fn = lambda budget, k: cpu_rate_uneven(items, budget)  # noqa: E731
+        desc = f"uneven batch of {len(items)} programs"
+        cfg = {"workload": desc}
+        unit_desc = "programs (systematic sample, min(shots,4) shots each)"
+    else:
+        spec, shots, desc = single_workload(args)
+        fn = lambda budget, k: cpu_rate_single(spec, budget, shot0=k * 1_000_000)  # noqa: E731
+        cfg = {"workload": desc, "qudits": spec.num_qudits, "dimension": spec.dimension,
+               "instructions": len(spec.ops), "shots_per_gpu": shots}
+        unit_desc = "shots of the workload"
+    for k in range(args.warmup):
+        fn(min(1.0, per_step), k)
+    rates, samples, t_all, threads = [], [], 0.0, 1
     for k in range(args.steps):
-        r, shots, dt, threads = cpu_oracle_rate(spec, per_step, shot0=k * 1_000_000)
+        r, used, dt, threads = fn(per_step, k)
         rates.append(r)
-        samples.append(shots)
+        samples.append(used)
         t_all += dt
     value = statistics.median(rates)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * t_all / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u32 bit-planes / int64 oracle", "data": "synthetic (seeded)",
-            "config": config(args, spec, "host cores, one process"),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_all / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64 (CPU oracle)",
+            "data": "synthetic (seeded)", "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{statistics.median(samples):.0f} shots per step of the workload "
-                                       f"(C restatement of sdim's ExtendedTableau, OpenMP over shots)"},
+                             "sample": f"{statistics.median(samples):.0f} {unit_desc} per step (C restatement "
+                                       f"of sdim's ExtendedTableau + shot loop, OpenMP over shots)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def smem_peak(ctx):
+    import ctypes
+    from sdim_gb300 import _lib
+    v = ctypes.c_double()
+    _lib.check(ctx.lib.sdim_probe_smem_bandwidth(ctx.ptr, ctypes.byref(v)), ctx.ptr, "smem probe")
+    return v.value
+
+
+def read_traffic(name):
+    """DRAM bytes per launch of the timed kernel from the committed ncu
+    summary (a line 'traffic_bytes_per_launch: <int>'), else None."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(float(line.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
+def hbm_peak():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0)
+    except (OSError, ValueError):
+        return 6800.0
+
+
+class Timer:
+    """Per-step CUDA events on a dedicated stream; L2 flushed between steps."""
+
+    def __init__(self, torch, stream, ctx, ws, dist):
+        self.torch, self.stream, self.ctx, self.ws, self.dist = torch, stream, ctx, ws, dist
+        self.flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def run(self, steps, step_fn, clocks=None):
+        torch = self.torch
+        step_ms, kern_ms = [], []
+        if self.ws > 1:
+            self.dist.barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        for _ in range(steps):
+            self.flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            step_fn()
+            e1.record(self.stream)
+            self.ctx.sync()
+            step_ms.append(e0.elapsed_time(e1))
+            kern_ms.append(self.ctx.last_kernel_ms())
+        torch.cuda.synchronize()
+        return step_ms, kern_ms, (clocks.stop() if clocks else None)
+
+    def max_over_ranks(self, value):
+        if self.ws == 1:
+            return value
+        t = self.torch.tensor([value], device="cuda", dtype=self.torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+def run_single(args, torch, dist, ws, rank, local):
+    from sdim_gb300 import Program, _lib
+
+    spec, shots, desc = single_workload(args)
+    prog = Program(spec.build(), device=local)
+    ctx = prog.context
+    dp = prog.compile()
+    enc = dp.enc
+    n, d = spec.num_qudits, spec.dimension
+    shot0 = rank * shots
+    nrec = dp.num_records
+    out = torch.empty((shots, max(nrec, 1)), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()  # the library runs on the handle it is given
+    torch.cuda.set_stream(stream)
+    timer = Timer(torch, stream, ctx, ws, dist)
+
+    def step(extra=0):
+        rc = ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 0, shot0, shots, out.data_ptr(), stream.cuda_stream,
+                                     _lib.FLAG_ASYNC | _lib.FLAG_TIME | extra)
+        _lib.check(rc, ctx.ptr, "run")
+
+    # per-shot engine (one warp, one full tableau per shot) on the same inputs
+    step(_lib.FLAG_PER_SHOT)
+    ctx.sync()
+    ps_steps = 2
+    ps_step_ms, ps_kern_ms, _ = timer.run(ps_steps, lambda: step(_lib.FLAG_PER_SHOT))
+    ps_records = out[:64, :nrec].cpu().numpy()
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    step_ms, kern_ms, clk = timer.run(args.steps, step, Clocks(local))
+    total_ms = timer.max_over_ranks(sum(step_ms))
+    units_per_step = len(spec.ops) * shots
+    value = units_per_step * ws * args.steps / (total_ms / 1e3)
+
+    rec = out[:64, :nrec].cpu().numpy()
+    if not np.array_equal(rec, ps_records):
+        raise AssertionError("shot-group and per-shot engines disagree")
+    det_row = (rec[0] >> 7).astype(bool) if nrec else np.zeros(0, bool)
+    assert np.all((rec >> 7) == (rec[0] >> 7)), "deterministic flags differ across shots"
+    meas_ids = [g for g in enc.ops[:, 0].tolist() if g in (14, 15, 16)]
+    reset_cols = [j for j, g in enumerate(meas_ids) if g == 16]
+    if reset_cols:
+        fired = float((out[:, reset_cols] & 0x7F).ne(0).sum().item()) / shots
+    else:
+        fired = 0.0
+    gbytes = group_bytes(enc, det_row, fired, n, d, shots)
+    per_shot_bytes = algorithmic_bytes_per_shot(enc, det_row, n, d)
+    mean_kern = statistics.mean(kern_ms)
+    achieved = gbytes / (mean_kern / 1e3) / 1e9
+    ps_kern = statistics.mean(ps_kern_ms)
+    ps_achieved = per_shot_bytes * shots / (ps_kern / 1e3) / 1e9
+    peak = smem_peak(ctx)
+
+    # end to end through the C ABI: pinned host records, instruction stream
+    # uploaded and records downloaded inside the timed region
+    host = torch.empty((shots, max(nrec, 1)), dtype=torch.uint8, pin_memory=True)
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 0, shot0, shots, host.data_ptr(), 0)
+        _lib.check(rc, ctx.ptr, "run")
+        if k >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    if not np.array_equal(host[:64, :nrec].numpy(), rec):
+        raise AssertionError("end-to-end records differ from the device-timed run")
+    e2e_total = timer.max_over_ranks(sum(e2e_ms))
+    e2e_value = units_per_step * ws * args.steps / (e2e_total / 1e3)
+
+    if rank != 0:
+        return None
+    pshots = min(args.plain_shots, shots)
+    pout = np.empty((pshots, max(nrec, 1)), dtype=np.uint8)
+    t0 = time.perf_counter()
+    rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 0, shot0, pshots, pout.ctypes.data, _lib.FLAG_PLAIN)
+    _lib.check(rc, ctx.ptr, "plain")
+    plain_s = time.perf_counter() - t0
+    if not np.array_equal(pout[:64, :nrec], rec[:min(64, pshots)]):
+        raise AssertionError("plain form differs from the batched form")
+    plain_rate = len(spec.ops) * pshots / plain_s
+    cpu = None
+    if not args.no_cpu:
+        r, cshots, cdt, threads = cpu_rate_single(spec, args.cpu_seconds)
+        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{cshots} shots of the same workload in {cdt:.1f} s (C restatement of sdim's "
+                         f"ExtendedTableau + shot loop, OpenMP over shots)"}
+    kernel = {2: "k_group_warp<TGroupBits<WarpTeam>>"}.get(d, f"k_group_{'cta' if n >= 160 else 'warp'}"
+                                                              f"<TGroupU8<{d}>>")
+    if d == 2 and n >= 160:
+        kernel = "k_group_cta<TGroupBits<CtaTeam>>"
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 bit planes (d=2) / u8 residues (odd d): exact integer mod d",
+        "data": "synthetic (seeded circuit generator, Philox outcome and noise stream)",
+        "config": {"workload": desc, "qudits": n, "dimension": d, "instructions": len(spec.ops),
+                   "shots_per_gpu": shots, "records_per_shot": nrec, "seed": 0,
+                   "l2": "flushed (256 MB write) between timed steps, outside the events",
+                   "parallelism": f"replicas x{ws}: per-GPU shot ranges, no collective"},
+        "shots_per_s": shots * ws * args.steps / (total_ms / 1e3),
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(dp.num_device_ops * 8),
+                "d2h_bytes_per_step": int(shots * nrec), "ms_per_step": e2e_total / args.steps},
+        "plain_gpu": {"value": plain_rate, "unit": UNIT, "shots": pshots, "form": "one single-warp launch per shot"},
+        "batched_vs_plain": value / plain_rate,
+        "per_shot_engine": {
+            "value": units_per_step * ps_steps / (sum(ps_step_ms) / 1e3), "unit": UNIT,
+            "form": "persistent kernel, one warp and one full tableau per shot", "kernel_ms": ps_kern,
+            "roofline": {"bound": "smem", "achieved": ps_achieved, "peak": peak, "unit": "GB/s",
+                         "frac": ps_achieved / peak, "algorithmic_bytes_per_shot": per_shot_bytes}},
+        "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": read_traffic("k_group_persistent_bits_surface_L7.md") if args.workload == "surface"
+                     else None,
+                     "kernel": kernel,
+                     "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth",
+                     "algorithmic_bytes_per_launch": gbytes,
+                     "bytes_model": "x/z rows + common phase once per 32-shot group (per-shot tableau figures), "
+                                    "plus each shot's phase-delta rows at measurements and RESET corrections",
+                     "per_shot_equivalent_GBps": per_shot_bytes * shots / (mean_kern / 1e3) / 1e9,
+                     "hbm_peak_gbs": hbm_peak(), "kernel_ms": mean_kern},
+        "cpu_baseline": cpu,
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+
+
+def run_uneven(args, torch, dist, ws, rank, local):
+    from sdim_gb300 import _lib
+    from sdim_gb300.batch import BatchRunner
+
+    items = uneven_items(args)
+    br = BatchRunner(_lib.Context.default(local))
+    ctx = br.ctx
+    for it in items:
+        br.add_spec(it.spec, it.shots, it.seed, shot0=rank * 64)
+    entries = br.entries
+    sizes = [e.shots * e.program.num_records for e in entries]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    out = torch.empty(int(offs[-1]) + 1, dtype=torch.uint8, device="cuda")
+    ptrs = [out.data_ptr() + int(o) for o in offs[:-1]]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    timer = Timer(torch, stream, ctx, ws, dist)
+
+    def step(extra=0):
+        br.run_device(ptrs, stream=stream.cuda_stream, time_kernels=True, asynchronous=True,
+                      per_shot=bool(extra & _lib.FLAG_PER_SHOT))
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    step_ms, kern_ms, clk = timer.run(args.steps, step, Clocks(local))
+    total_ms = timer.max_over_ranks(sum(step_ms))
+    units_per_step = br.total_gate_updates()
+    value = units_per_step * ws * args.steps / (total_ms / 1e3)
+    ref_out = out.cpu().numpy()
+
+    # the per-shot engine on the same batch
+    step(_lib.FLAG_PER_SHOT)
+    ctx.sync()
+    ps_step_ms, ps_kern_ms, _ = timer.run(1, lambda: step(_lib.FLAG_PER_SHOT))
+    if not np.array_equal(out.cpu().numpy(), ref_out):
+        raise AssertionError("shot-group and per-shot engines disagree on the uneven batch")
+
+    # algorithmic bytes: det flags per program from its first shot
+    gb = 0.0
+    for e, o in zip(entries, offs[:-1]):
+        enc = e.program.enc
+        nr = e.program.num_records
+        rec0 = ref_out[int(o):int(o) + nr]
+        gb += group_bytes(enc, (rec0 >> 7).astype(bool), 0.0, enc.n, enc.d, e.shots)
+    mean_kern = statistics.mean(kern_ms)
+    peak = smem_peak(ctx)
+
+    # end to end: host records (pinned), descriptors up and records down inside
+    host = torch.empty(int(offs[-1]) + 1, dtype=torch.uint8, pin_memory=True)
+    host_np = host.numpy()
+    houts = [host_np[int(a):int(b)].reshape(e.shots, e.program.num_records)
+             for a, b, e in zip(offs[:-1], offs[1:], entries)]
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        br.run(outs=houts)
+        if k >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    if not np.array_equal(host_np[:-1], ref_out[:-1]):
+        raise AssertionError("end-to-end records differ")
+    e2e_total = timer.max_over_ranks(sum(e2e_ms))
+    e2e_value = units_per_step * ws * args.steps / (e2e_total / 1e3)
+    if rank != 0:
+        return None
+    # plain form (one single-warp launch per shot) on a systematic sample of programs
+    sample = entries[::128]
+    t0 = time.perf_counter()
+    br.run(plain=True, entries=sample)
+    plain_s = time.perf_counter() - t0
+    plain_units = sum(e.shots * e.program.num_instructions for e in sample)
+    plain_rate = plain_units / plain_s
+    cpu = None
+    if not args.no_cpu:
+        r, used, cdt, threads = cpu_rate_uneven(items, args.cpu_seconds)
+        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{used} programs, min(shots,4) shots each, in {cdt:.1f} s (C oracle, OpenMP)"}
+    ns = np.array([it.spec.num_qudits for it in items])
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 bit planes (d=2) / u8 residues (odd d): exact integer mod d",
+        "data": "synthetic (seeded generator, Philox outcome stream)",
+        "config": {"workload": f"uneven batch: {len(items)} programs, n log-uniform [8,1024] (median "
+                               f"{int(np.median(ns))}), d in {{2,3,5,7}}, 4n gates + MEASURE all, shots 1-64",
+                   "programs": len(items), "shots_per_gpu": br.total_shots(),
+                   "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
+        "shots_per_s": br.total_shots() * ws * args.steps / (total_ms / 1e3),
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 80 * len(items),
+                "d2h_bytes_per_step": int(offs[-1]), "ms_per_step": e2e_total / args.steps},
+        "plain_gpu": {"value": plain_rate, "unit": UNIT, "programs": len(sample),
+                      "form": "one single-warp launch per shot, systematic sample of programs"},
+        "batched_vs_plain": value / plain_rate,
+        "per_shot_engine": {"value": units_per_step / (sum(ps_step_ms) / 1e3), "unit": UNIT,
+                            "kernel_ms": statistics.mean(ps_kern_ms)},
+        "roofline": {"bound": "smem", "achieved": gb / (mean_kern / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": gb / (mean_kern / 1e3) / 1e9 / peak, "traffic": None,
+                     "kernel": "k_group_warp / k_group_cta over all variants",
+                     "algorithmic_bytes_per_launch": gb, "kernel_ms": mean_kern,
+                     "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth"},
+        "cpu_baseline": cpu,
+        # one persistent launch per (dimension, team kind) present in the batch
+        "gpu_launches": args.steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),
+        "clocks": clk,
+    }
 
 
 def run_gb300(args):
@@ -240,197 +602,15 @@ def run_gb300(args):
     if ws > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-    from sdim_gb300 import Program, _lib
-    from sdim_gb300.encode import DeviceProgram
-
-    spec = workload(args)
-    prog = Program(spec.build(), device=local)
-    ctx = prog.context
-    dp = prog.compile()
-    enc = dp.enc
-    shots = args.shots
-    shot0 = rank * shots
-    nrec = dp.num_records
-    out = torch.empty((shots, nrec), dtype=torch.uint8, device="cuda")
-    # a dedicated stream: the library runs on the stream handle it is given
-    # (the legacy default stream has handle 0, which means "context stream")
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-
-    def device_step(extra_flags=0):
-        rc = ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 0, shot0, shots, out.data_ptr(), stream.cuda_stream,
-                                     _lib.FLAG_ASYNC | _lib.FLAG_TIME | extra_flags)
-        _lib.check(rc, ctx.ptr, "run")
-
-    def timed_steps(steps, extra_flags=0, clocks=None):
-        step_ms, kern_ms = [], []
-        if ws > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        if clocks:
-            clocks.start()
-        for _ in range(steps):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            device_step(extra_flags)
-            e1.record(stream)
-            ctx.sync()
-            step_ms.append(e0.elapsed_time(e1))
-            kern_ms.append(ctx.last_kernel_ms())
-        torch.cuda.synchronize()
-        return step_ms, kern_ms, (clocks.stop() if clocks else None)
-
-    # the per-shot engine (one warp per shot) on the same workload, beside
-    for _ in range(2):
-        device_step(_lib.FLAG_PER_SHOT)
-    ctx.sync()
-    ps_steps = max(2, min(args.steps, 3))
-    ps_step_ms, ps_kern_ms, _ = timed_steps(ps_steps, _lib.FLAG_PER_SHOT)
-    ps_records = out[:64].cpu()
-
-    for _ in range(args.warmup):
-        device_step()
-    ctx.sync()
-    step_ms, kern_ms, clk = timed_steps(args.steps, 0, Clocks(local))
-    if ws > 1:
-        dist.barrier()
-    total_ms = sum(step_ms)
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    units_per_step = len(spec.ops) * shots
-    value = units_per_step * ws * args.steps / (total_ms / 1e3)
-    shots_per_s = shots * ws * args.steps / (total_ms / 1e3)
-
-    # records are bit-identical across engines and runs; det flags are shot independent
-    rec = out[:64].cpu().numpy()
-    if not np.array_equal(rec, ps_records.numpy()):
-        raise AssertionError("shot-group and per-shot engines disagree")
-    det_row = (rec[0] >> 7).astype(bool)
-    assert np.all((rec >> 7) == (rec[0] >> 7)), "deterministic flags differ across shots"
-    n, d = spec.num_qudits, spec.dimension
-    bytes_per_shot = algorithmic_bytes_per_shot(enc, det_row, n, d)
-    meas_ids = [g for g in enc.ops[:, 0].tolist() if g in (14, 15, 16)]
-    reset_cols = [j for j, g in enumerate(meas_ids) if g == 16]
-    # RESET records whose outcome needs a correction, per shot (all shots)
-    fired = float((out[:, reset_cols] & 0x7F).ne(0).sum().item()) / shots if reset_cols else 0.0
-    groups = -(-shots // 32)
-    group_bytes = groups * bytes_per_shot + shots * group_delta_bytes_per_shot(enc, det_row, fired, n, d)
-    mean_kern = statistics.mean(kern_ms)
-    achieved = group_bytes / (mean_kern / 1e3) / 1e9
-    ps_kern = statistics.mean(ps_kern_ms)
-    ps_achieved = bytes_per_shot * shots / (ps_kern / 1e3) / 1e9
-    smem_gbs = C_double_probe(ctx)
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-    except (OSError, ValueError):
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    traffic = read_traffic()
-
-    # end to end through the C ABI: pinned host output, instruction stream
-    # uploaded and records downloaded inside the timed region
-    host = torch.empty((shots, nrec), dtype=torch.uint8, pin_memory=True)
-    e2e_ms = []
-    for k in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 0, shot0, shots, host.data_ptr(), 0)
-        _lib.check(rc, ctx.ptr, "run")
-        if k >= args.warmup:
-            e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    if not torch.equal(host[:64].cuda(), out[:64]):
-        raise AssertionError("end-to-end records differ from the device-timed run")
-    e2e_total = sum(e2e_ms)
-    if ws > 1:
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = units_per_step * ws * args.steps / (e2e_total / 1e3)
-
-    line = None
-    if rank == 0:
-        # plain per-shot form (one single-warp launch per shot) on a sample
-        pshots = min(args.plain_shots, shots)
-        pout = np.empty((pshots, nrec), dtype=np.uint8)
-        t0 = time.perf_counter()
-        rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 0, shot0, pshots, pout.ctypes.data, _lib.FLAG_PLAIN | _lib.FLAG_TIME)
-        _lib.check(rc, ctx.ptr, "plain")
-        plain_s = time.perf_counter() - t0
-        if not np.array_equal(pout[:64], rec[:min(64, pshots)]):
-            raise AssertionError("plain form differs from the batched form")
-        plain_rate = len(spec.ops) * pshots / plain_s
-        cpu = None
-        if not args.no_cpu:
-            r, cshots, cdt, threads = cpu_oracle_rate(spec, args.cpu_seconds)
-            cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"{cshots} shots of the same workload in {cdt:.1f} s (C restatement of sdim's "
-                             f"ExtendedTableau + shot loop, OpenMP over shots)"}
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32 bit-planes (exact mod-2 / mod-4 integer)",
-            "data": "synthetic (seeded circuit generator, Philox outcome/noise stream)",
-            "config": config(args, spec, f"replicas x{ws}: per-GPU shot ranges, no collective"),
-            "shots_per_s": shots_per_s,
-            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(dp.num_device_ops * 8),
-                    "d2h_bytes_per_step": int(shots * nrec),
-                    "ms_per_step": e2e_total / args.steps},
-            "plain_gpu": {"value": plain_rate, "unit": UNIT, "shots": pshots,
-                          "form": "one single-warp launch per shot"},
-            "batched_vs_plain": value / plain_rate,
-            "per_shot_engine": {
-                "value": units_per_step * ps_steps / (sum(ps_step_ms) / 1e3), "unit": UNIT,
-                "form": "persistent kernel, one warp and one full tableau per shot",
-                "kernel_ms": ps_kern,
-                "roofline": {"bound": "smem", "achieved": ps_achieved, "peak": smem_gbs, "unit": "GB/s",
-                             "frac": ps_achieved / smem_gbs,
-                             "algorithmic_bytes_per_shot": bytes_per_shot}},
-            "roofline": {"bound": "smem", "achieved": achieved, "peak": smem_gbs, "unit": "GB/s",
-                         "frac": achieved / smem_gbs, "traffic": traffic,
-                         "kernel": "k_group_persistent<GroupBits>",
-                         "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth",
-                         "algorithmic_bytes_per_launch": group_bytes,
-                         "bytes_model": "x/z rows + common phase per 32-shot group (per-shot tableau figures), "
-                                        "plus each shot's phase-delta rows at measurements and RESET corrections",
-                         "per_shot_equivalent_GBps": bytes_per_shot * shots / (mean_kern / 1e3) / 1e9,
-                         "hbm_peak_gbs": hbm, "kernel_ms": mean_kern},
-            "cpu_baseline": cpu,
-            "gpu_launches": args.steps,
-            "clocks": clk,
-        }
+    if args.workload == "uneven":
+        line = run_uneven(args, torch, dist, ws, rank, local)
+    else:
+        line = run_single(args, torch, dist, ws, rank, local)
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
     if line is not None:
         print(json.dumps(line), flush=True)
-
-
-def C_double_probe(ctx):  # noqa: N802
-    import ctypes
-    from sdim_gb300 import _lib
-    v = ctypes.c_double()
-    _lib.check(ctx.lib.sdim_probe_smem_bandwidth(ctx.ptr, ctypes.byref(v)), ctx.ptr, "smem probe")
-    return v.value
-
-
-def read_traffic():
-    """DRAM bytes per launch of the persistent kernel from the committed ncu
-    summary (a line 'traffic_bytes_per_launch: <int>'), else None."""
-    p = ROOT / "profiles" / "k_group_persistent_bits_surface_L7.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return int(float(line.split(":", 1)[1].strip()))
-            except ValueError:
-                return None
-    return None
 
 
 def main():

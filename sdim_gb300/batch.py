@@ -42,7 +42,8 @@ class BatchRunner:
         self.entries.append(e)
         return e
 
-    def _arrays(self, entries):
+    @staticmethod
+    def _arrays(entries):
         k = len(entries)
         circs = (C.c_void_p * k)(*[e.program.ptr.value for e in entries])
         seeds = (C.c_uint64 * k)(*[e.seed & 0xFFFFFFFFFFFFFFFF for e in entries])
@@ -50,31 +51,37 @@ class BatchRunner:
         nshots = (C.c_int64 * k)(*[e.shots for e in entries])
         return circs, seeds, shot0, nshots
 
-    def run(self, plain: bool = False, time_kernels: bool = False,
-            entries: Optional[Sequence[BatchEntry]] = None) -> List[np.ndarray]:
-        """Runs every entry; returns one (shots, records) uint8 array each."""
+    @staticmethod
+    def _flags(plain=False, per_shot=False, time_kernels=False, asynchronous=False, device=False):
+        return ((_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_PER_SHOT if per_shot else 0)
+                | (_lib.FLAG_TIME if time_kernels else 0) | (_lib.FLAG_ASYNC if asynchronous else 0)
+                | (_lib.FLAG_OUT_DEVICE if device else 0))
+
+    def run(self, plain: bool = False, per_shot: bool = False, time_kernels: bool = False,
+            entries: Optional[Sequence[BatchEntry]] = None,
+            outs: Optional[Sequence[np.ndarray]] = None) -> List[np.ndarray]:
+        """Runs every entry; returns one (shots, records) uint8 array each
+        (into ``outs`` when given, e.g. views of a pinned buffer)."""
         entries = list(self.entries if entries is None else entries)
-        outs = [np.empty((e.shots, e.program.num_records), dtype=np.uint8) for e in entries]
+        if outs is None:
+            outs = [np.empty((e.shots, e.program.num_records), dtype=np.uint8) for e in entries]
         ptrs = (C.c_void_p * len(entries))(*[o.ctypes.data for o in outs])
         circs, seeds, shot0, nshots = self._arrays(entries)
-        flags = (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_TIME if time_kernels else 0)
         rc = self.ctx.lib.sdim_run_batch(self.ctx.ptr, len(entries), circs, seeds, shot0, nshots, ptrs, None,
-                                         flags)
+                                         self._flags(plain, per_shot, time_kernels))
         _lib.check(rc, self.ctx.ptr, "batch")
-        return outs
+        return list(outs)
 
     def run_device(self, outs_dev: Sequence[int], stream: Optional[int] = None, plain: bool = False,
-                   time_kernels: bool = False, asynchronous: bool = False,
+                   per_shot: bool = False, time_kernels: bool = False, asynchronous: bool = False,
                    entries: Optional[Sequence[BatchEntry]] = None):
         """Same with device output pointers (e.g. ``tensor.data_ptr()``)."""
         entries = list(self.entries if entries is None else entries)
         ptrs = (C.c_void_p * len(entries))(*[int(p) for p in outs_dev])
         circs, seeds, shot0, nshots = self._arrays(entries)
-        flags = _lib.FLAG_OUT_DEVICE | (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_TIME if time_kernels else 0)
-        if asynchronous:
-            flags |= _lib.FLAG_ASYNC
         rc = self.ctx.lib.sdim_run_batch(self.ctx.ptr, len(entries), circs, seeds, shot0, nshots, ptrs,
-                                         C.c_void_p(stream) if stream else None, flags)
+                                         C.c_void_p(stream) if stream else None,
+                                         self._flags(plain, per_shot, time_kernels, asynchronous, True))
         _lib.check(rc, self.ctx.ptr, "batch")
 
     def total_shots(self) -> int:
