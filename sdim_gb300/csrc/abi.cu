@@ -126,6 +126,9 @@ int cta_block_for(int n) {
   return b;
 }
 
+// shared memory a block may use for tableau slots
+size_t smem_usable(const sdim_ctx* ctx) { return (size_t)(ctx->smem_optin - kStaticSmemReserve); }
+
 int set_smem_attr(sdim_ctx* ctx, int variant) {
   if (ctx->smem_attr_set[variant]) return SDIM_OK;
   const cudaError_t e = variant_ops(variant).set_smem(ctx->smem_optin);
@@ -147,12 +150,12 @@ Plan plan_launch(const sdim_ctx* ctx, int variant, size_t slot, long long items,
   const VariantOps& ops = variant_ops(variant);
   Plan p;
   p.slot = slot;
-  p.smem_slots = !force_gmem && slot <= (size_t)ctx->smem_optin;
+  p.smem_slots = !force_gmem && slot <= smem_usable(ctx);
   p.team_threads = ops.cta ? cta_block : 32;
   if (ops.cta) {
     p.slots_per_block = 1;
   } else if (p.smem_slots) {
-    p.slots_per_block = (int)std::min<size_t>(32, (size_t)ctx->smem_optin / slot);
+    p.slots_per_block = (int)std::min<size_t>(32, smem_usable(ctx) / slot);
     // spread the items over every SM before stacking more warps on one
     const long long per_sm = (items + ctx->num_sms - 1) / ctx->num_sms;
     if (per_sm < p.slots_per_block) p.slots_per_block = (int)std::max<long long>(1, per_sm);
@@ -274,7 +277,7 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     if ((rc = set_smem_attr(ctx, g.variant)) != SDIM_OK) return rc;
     const VariantOps& ops = variant_ops(g.variant);
     if (plain) {
-      const bool sm = !force_gmem && g.slot <= (size_t)ctx->smem_optin;
+      const bool sm = !force_gmem && g.slot <= smem_usable(ctx);
       if (!sm && (rc = ensure(ctx, ctx->gslots, g.slot)) != SDIM_OK) return rc;
       for (int k = g.begin; k < g.end; ++k)
         for (long long sh = 0; sh < hd[k].nshots; ++sh)
@@ -651,7 +654,7 @@ int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t s
   dsc.d = c->d;
   dsc.nmeas = c->nmeas;
   dsc.nshots = grp ? 32 : 1;
-  const bool sm = !(flags & SDIM_FLAG_FORCE_GMEM) && slot <= (size_t)ctx->smem_optin;
+  const bool sm = !(flags & SDIM_FLAG_FORCE_GMEM) && slot <= smem_usable(ctx);
   if (!sm && (rc = ensure(ctx, ctx->gslots, slot)) != SDIM_OK) return rc;
   cudaStream_t s = ctx->stream;
   CK(cudaMemcpyAsync(ctx->descs.p, &dsc, sizeof(dsc), cudaMemcpyHostToDevice, s));

@@ -13,11 +13,11 @@ struct Group {
   static cudaError_t set_smem(int bytes) {
     cudaError_t e;
     if constexpr (CTA)
-      e = cudaFuncSetAttribute(k_group_cta<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      e = set_dynamic_smem(k_group_cta<G>, bytes);
     else
-      e = cudaFuncSetAttribute(k_group_warp<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      e = set_dynamic_smem(k_group_warp<G>, bytes);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_group_snapshot<G, CTA>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return set_dynamic_smem(k_group_snapshot<G, CTA>, bytes);
   }
   static int occupancy(int block, size_t smem) {
     int nb = 0;

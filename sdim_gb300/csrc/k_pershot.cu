@@ -10,11 +10,11 @@ template <class E>
 struct PerShot {
   static size_t slot_bytes(int n) { return (E::slot_bytes(n) + 15) & ~(size_t)15; }
   static cudaError_t set_smem(int bytes) {
-    cudaError_t e = cudaFuncSetAttribute(k_persistent<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = set_dynamic_smem(k_persistent<E>, bytes);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_single<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    e = set_dynamic_smem(k_single<E>, bytes);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_snapshot<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return set_dynamic_smem(k_snapshot<E>, bytes);
   }
   static int occupancy(int block, size_t smem) {
     int nb = 0;

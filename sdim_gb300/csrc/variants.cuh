@@ -48,6 +48,20 @@ struct VariantOps {
                    uint8_t* gslot, int smem_slot, int8_t* snap, int mode, int lane, int* status);
 };
 
+// Shared memory the planner leaves for the kernels' static arrays.
+constexpr int kStaticSmemReserve = 1024;
+
+// Raises a kernel's dynamic shared-memory cap to the per-block opt-in limit
+// minus the kernel's own static shared memory.
+template <class K>
+inline cudaError_t set_dynamic_smem(K kernel, int optin_bytes) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin_bytes - (int)a.sharedSizeBytes);
+}
+
 const VariantOps& pershot_ops(int variant);
 const VariantOps& group_ops(int variant);
 
