@@ -44,6 +44,8 @@ extern "C" {
 #define SDIM_FLAG_TIME 8u        /* time the kernels with CUDA events (sdim_last_kernel_ms) */
 #define SDIM_FLAG_FORCE_GMEM 16u /* keep tableaux in global memory even when they fit in smem */
 #define SDIM_FLAG_PER_SHOT 32u   /* batched runs use one warp per shot instead of the shot-group engine */
+#define SDIM_FLAG_TEAM_WARP 64u  /* shot groups on one warp each, whatever n */
+#define SDIM_FLAG_TEAM_CTA 128u  /* shot groups on one CTA each, whatever n */
 
 /* snapshot modes for sdim_snapshot */
 #define SDIM_SNAP_EVERY_INSTRUCTION 1

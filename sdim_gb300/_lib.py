@@ -24,6 +24,8 @@ FLAG_ASYNC = 4
 FLAG_TIME = 8
 FLAG_FORCE_GMEM = 16
 FLAG_PER_SHOT = 32
+FLAG_TEAM_WARP = 64
+FLAG_TEAM_CTA = 128
 
 SNAP_EVERY_INSTRUCTION = 1
 SNAP_AT_MEASUREMENT = 2

@@ -44,11 +44,9 @@ struct sdim_circuit {
   int n = 0, d = 0, nmeas = 0;
   int64_t nops_user = 0;
   int nops = 0;
-  int variant = 0;     // per-shot engine (plain form, per-shot snapshots)
-  int gvariant = 0;    // shot-group engine for batched runs
-  int gblock = 32;     // threads of one group team
-  size_t slot_bytes = 0;
-  size_t gslot_bytes = 0;
+  int variant = 0;    // per-shot engine (plain form, per-shot snapshots)
+  int gvariant = 0;   // shot-group engine for batched runs
+  int gblock = 32;    // threads of one group team
   uint2* h_ops = nullptr;  // pinned host copy
   uint2* d_ops = nullptr;
 };
@@ -108,8 +106,10 @@ int variant_for(int d) {
 // measurements touch n x 2n residues, which one warp would walk alone.
 constexpr int kCtaTeamQudits = 160;
 
-int group_variant_for(int d, int n) {
-  const bool cta = n >= kCtaTeamQudits;
+int group_variant_for(int d, int n, unsigned flags) {
+  bool cta = n >= kCtaTeamQudits;
+  if (flags & SDIM_FLAG_TEAM_WARP) cta = false;
+  if (flags & SDIM_FLAG_TEAM_CTA) cta = true;
   switch (d) {
     case 2: return cta ? V_GBITS_C : V_GBITS_W;
     case 3: return cta ? V_GU8_3_C : V_GU8_3_W;
@@ -126,7 +126,7 @@ int cta_block_for(int n) {
   return b;
 }
 
-// shared memory a block may use for tableau slots
+// shared memory a block may use for slots
 size_t smem_usable(const sdim_ctx* ctx) { return (size_t)(ctx->smem_optin - kStaticSmemReserve); }
 
 int set_smem_attr(sdim_ctx* ctx, int variant) {
@@ -137,39 +137,45 @@ int set_smem_attr(sdim_ctx* ctx, int variant) {
   return SDIM_OK;
 }
 
+// Where the slots of one launch live and how many there are.
 struct Plan {
-  bool smem_slots;
-  int team_threads;  // 32 for warp teams
+  bool in_smem;         // big part of each slot in shared memory
+  int team_threads;     // 32 for warp teams
   int slots_per_block;
   int blocks;
-  size_t slot;
+  size_t hot, big;      // bytes of the two parts of a slot
+  size_t smem_per_block;
 };
 
-Plan plan_launch(const sdim_ctx* ctx, int variant, size_t slot, long long items, int cta_block,
+Plan plan_launch(const sdim_ctx* ctx, int variant, size_t hot, size_t big, long long items, int cta_block,
                  bool force_gmem) {
   const VariantOps& ops = variant_ops(variant);
+  const size_t usable = smem_usable(ctx);
   Plan p;
-  p.slot = slot;
-  p.smem_slots = !force_gmem && slot <= smem_usable(ctx);
+  p.hot = hot;
+  p.big = big;
+  p.in_smem = !force_gmem && hot + big <= usable;
   p.team_threads = ops.cta ? cta_block : 32;
+  const size_t per_slot_smem = hot + (p.in_smem ? big : 0);
   if (ops.cta) {
     p.slots_per_block = 1;
-  } else if (p.smem_slots) {
-    p.slots_per_block = (int)std::min<size_t>(32, smem_usable(ctx) / slot);
+  } else {
+    const int max_slots = ops.max_block / 32;
+    p.slots_per_block = per_slot_smem ? (int)std::min<size_t>(max_slots, usable / per_slot_smem) : 8;
+    if (p.slots_per_block < 1) p.slots_per_block = 1;
+    if (!p.in_smem && !ops.group) p.slots_per_block = 4;  // per-shot tableaux in global memory
     // spread the items over every SM before stacking more warps on one
     const long long per_sm = (items + ctx->num_sms - 1) / ctx->num_sms;
     if (per_sm < p.slots_per_block) p.slots_per_block = (int)std::max<long long>(1, per_sm);
-  } else {
-    p.slots_per_block = 4;
   }
   const int block = p.team_threads * p.slots_per_block;
-  const size_t smem = p.smem_slots ? slot * p.slots_per_block : 0;
-  const int occ = ops.occupancy(block, smem);
+  p.smem_per_block = per_slot_smem * p.slots_per_block;
+  const int occ = ops.occupancy(block, p.smem_per_block);
   long long blocks = (long long)ctx->num_sms * occ;
   const long long need = (items + p.slots_per_block - 1) / p.slots_per_block;
   blocks = std::min(blocks, need);
-  if (!p.smem_slots) {
-    const long long by_budget = (long long)(ctx->gmem_slot_budget / (slot * p.slots_per_block));
+  if (!p.in_smem) {
+    const long long by_budget = (long long)(ctx->gmem_slot_budget / (big * p.slots_per_block));
     blocks = std::min(blocks, std::max<long long>(1, by_budget));
   }
   p.blocks = (int)std::max<long long>(1, blocks);
@@ -211,10 +217,12 @@ struct Job {
 };
 
 // Engine used for a job: the shot-group engine for batched runs (unless
-// SDIM_FLAG_PER_SHOT), the per-shot engine for the plain form.
+// SDIM_FLAG_PER_SHOT; SDIM_FLAG_TEAM_* override the team kind), the
+// per-shot engine for the plain form.
 int job_variant(const sdim_circuit* c, unsigned flags) {
-  if (!(flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT))) return c->gvariant;
-  return c->variant;
+  if (flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT)) return c->variant;
+  if (flags & (SDIM_FLAG_TEAM_WARP | SDIM_FLAG_TEAM_CTA)) return group_variant_for(c->d, c->n, flags);
+  return c->gvariant;
 }
 
 // Launches every job, grouped by engine variant: one persistent launch per
@@ -239,13 +247,13 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     return cost(jobs[a]) > cost(jobs[b]);
   });
   std::vector<CircuitDesc> hd(jobs.size());
-  struct Group { int variant, begin, end; long long items; size_t slot; int block; };
+  struct Group { int variant, begin, end; long long items; size_t hot, big; int block; };
   std::vector<Group> groups;
   for (size_t k = 0; k < order.size(); ++k) {
     const Job& j = jobs[order[k]];
     const int v = var[order[k]];
-    const bool grp = variant_ops(v).group;
-    if (groups.empty() || groups.back().variant != v) groups.push_back(Group{v, (int)k, (int)k, 0, 0, 32});
+    const VariantOps& ops = variant_ops(v);
+    if (groups.empty() || groups.back().variant != v) groups.push_back(Group{v, (int)k, (int)k, 0, 0, 0, 32});
     Group& g = groups.back();
     CircuitDesc& dsc = hd[k];
     std::memset(&dsc, 0, sizeof(dsc));
@@ -259,9 +267,10 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     dsc.d = j.c->d;
     dsc.nmeas = j.c->nmeas;
     dsc.nshots = (int)j.nshots;
-    g.items += grp ? (j.nshots + 31) / 32 : j.nshots;
-    g.slot = std::max(g.slot, grp ? j.c->gslot_bytes : j.c->slot_bytes);
-    g.block = std::max(g.block, grp ? j.c->gblock : 32);
+    g.items += ops.group ? (j.nshots + 31) / 32 : j.nshots;
+    g.hot = std::max(g.hot, ops.hot_bytes(j.c->n));
+    g.big = std::max(g.big, ops.big_bytes(j.c->n));
+    g.block = std::max(g.block, ops.cta ? cta_block_for(j.c->n) : 32);
     g.end = (int)k + 1;
   }
   CircuitDesc* ddesc = static_cast<CircuitDesc*>(ctx->descs.p);
@@ -277,20 +286,19 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
     if ((rc = set_smem_attr(ctx, g.variant)) != SDIM_OK) return rc;
     const VariantOps& ops = variant_ops(g.variant);
     if (plain) {
-      const bool sm = !force_gmem && g.slot <= smem_usable(ctx);
-      if (!sm && (rc = ensure(ctx, ctx->gslots, g.slot)) != SDIM_OK) return rc;
+      const bool sm = !force_gmem && g.big <= smem_usable(ctx);
+      if (!sm && (rc = ensure(ctx, ctx->gslots, g.big)) != SDIM_OK) return rc;
       for (int k = g.begin; k < g.end; ++k)
         for (long long sh = 0; sh < hd[k].nshots; ++sh)
-          ops.single(sm ? g.slot : 0, s, ddesc + k, sh, static_cast<uint8_t*>(ctx->gslots.p), sm ? 1 : 0, status);
+          ops.single(sm ? g.big : 0, s, ddesc + k, sh, static_cast<uint8_t*>(ctx->gslots.p), sm ? 1 : 0, status);
     } else {
-      const Plan p = plan_launch(ctx, g.variant, g.slot, g.items, g.block, force_gmem);
-      if (!p.smem_slots &&
-          (rc = ensure(ctx, ctx->gslots, p.slot * p.slots_per_block * (size_t)p.blocks)) != SDIM_OK)
+      const Plan p = plan_launch(ctx, g.variant, g.hot, g.big, g.items, g.block, force_gmem);
+      if (!p.in_smem && (rc = ensure(ctx, ctx->gslots, p.big * p.slots_per_block * (size_t)p.blocks)) != SDIM_OK)
         return rc;
       unsigned long long* counter = static_cast<unsigned long long*>(ctx->counters.p) + g.variant;
-      ops.persistent(dim3(p.blocks), dim3(p.team_threads * p.slots_per_block),
-                     p.smem_slots ? p.slot * p.slots_per_block : 0, s, ddesc + g.begin, g.end - g.begin, g.items,
-                     counter, static_cast<uint8_t*>(ctx->gslots.p), p.slot, p.smem_slots ? 1 : 0, status);
+      ops.persistent(dim3(p.blocks), dim3(p.team_threads * p.slots_per_block), p.smem_per_block, s,
+                     ddesc + g.begin, g.end - g.begin, g.items, counter, static_cast<uint8_t*>(ctx->gslots.p),
+                     p.big, p.hot, p.in_smem ? 1 : 0, status);
     }
     cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch");
@@ -469,9 +477,7 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
   c->nops_user = nops;
   c->nops = (int)dev.size();
   c->variant = variant_for(d);
-  c->slot_bytes = variant_ops(c->variant).slot_bytes(n);
-  c->gvariant = group_variant_for(d, n);
-  c->gslot_bytes = variant_ops(c->gvariant).slot_bytes(n);
+  c->gvariant = group_variant_for(d, n, 0);
   c->gblock = variant_ops(c->gvariant).cta ? cta_block_for(n) : 32;
   const size_t bytes = std::max<size_t>(dev.size(), 1) * sizeof(uint2);
   cudaError_t e = cudaMallocHost(&c->h_ops, bytes);
@@ -505,14 +511,15 @@ int sdim_circuit_destroy(sdim_circuit* c) {
 
 int sdim_circuit_info(const sdim_circuit* c, int64_t info[8]) {
   if (!c || !info) return SDIM_EINVAL;
+  const VariantOps& g = variant_ops(c->gvariant);
   info[0] = c->n;
   info[1] = c->d;
   info[2] = c->nmeas;
   info[3] = c->nops_user;
   info[4] = c->nops;
   info[5] = c->d == 2 ? 1 : 0;
-  info[6] = (int64_t)c->slot_bytes;
-  info[7] = (int64_t)c->gslot_bytes;
+  info[6] = (int64_t)variant_ops(c->variant).big_bytes(c->n);
+  info[7] = (int64_t)(g.hot_bytes(c->n) + g.big_bytes(c->n));
   return SDIM_OK;
 }
 
@@ -634,7 +641,7 @@ int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t s
   const int v = job_variant(c, flags);
   const VariantOps& ops = variant_ops(v);
   const bool grp = ops.group;
-  const size_t slot = grp ? c->gslot_bytes : c->slot_bytes;
+  const size_t hot = ops.hot_bytes(c->n), big = ops.big_bytes(c->n);
   // a group snapshot runs the 32 shots [shot - lane, shot - lane + 32) and exports lane's
   const int lane = grp ? (int)(shot % 32) : 0;
   int rc;
@@ -654,14 +661,15 @@ int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t s
   dsc.d = c->d;
   dsc.nmeas = c->nmeas;
   dsc.nshots = grp ? 32 : 1;
-  const bool sm = !(flags & SDIM_FLAG_FORCE_GMEM) && slot <= smem_usable(ctx);
-  if (!sm && (rc = ensure(ctx, ctx->gslots, slot)) != SDIM_OK) return rc;
+  const bool in_smem = !(flags & SDIM_FLAG_FORCE_GMEM) && hot + big <= smem_usable(ctx);
+  if (!in_smem && (rc = ensure(ctx, ctx->gslots, big)) != SDIM_OK) return rc;
   cudaStream_t s = ctx->stream;
   CK(cudaMemcpyAsync(ctx->descs.p, &dsc, sizeof(dsc), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(ctx->status.p, 0, sizeof(int), s));
-  ops.snapshot(dim3(ops.cta ? c->gblock : 32), sm ? slot : 0, s, static_cast<const CircuitDesc*>(ctx->descs.p),
-               0, static_cast<uint8_t*>(ctx->gslots.p), sm ? 1 : 0, static_cast<int8_t*>(ctx->snap.p), mode, lane,
-               static_cast<int*>(ctx->status.p));
+  const int block = ops.cta ? cta_block_for(c->n) : 32;
+  ops.snapshot(dim3(block), hot + (in_smem ? big : 0), s, static_cast<const CircuitDesc*>(ctx->descs.p), 0,
+               static_cast<uint8_t*>(ctx->gslots.p), big, hot, in_smem ? 1 : 0, static_cast<int8_t*>(ctx->snap.p),
+               mode, lane, static_cast<int*>(ctx->status.p));
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return cuda_fail(ctx, le, "snapshot launch");
   if (count * tb) CK(cudaMemcpyAsync(out, ctx->snap.p, count * tb, cudaMemcpyDeviceToHost, s));

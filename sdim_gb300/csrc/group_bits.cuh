@@ -1,17 +1,31 @@
 // Shot-group engine for d = 2 (bit planes), any team size.
 //
-// 32 shots of one program share X / Z and a common phase c (planes C0, C1);
-// shot s keeps delta_s (planes D0[s], D1[s]) with ph_s = c + delta_s mod 4.
-// Why that is exact, and how each update splits, is written out in
-// engine_group.cuh; the arithmetic per generator is that of engine_bits.cuh.
+// Every shot's tableau is (x, z, ph_s).  The x / z blocks do not depend on
+// measurement outcomes or noise: pivots, factors and the x / z rowsum of
+// sdim's measure (sdim/tableau/tableau_prime.py:262-334) read only x / z, and
+// RESET corrections and Paulis touch phases only (sdim/program.py:335-339,
+// sdim/tableau/tableau_gates.py:27-137).  So the 32 shots of a group share
+// X / Z after every instruction, and each phase vector splits as
+//     ph_s = c + delta_s   (mod 4, per generator)
+// where c (planes C0, C1) follows the shared updates (Clifford phase terms,
+// the rowsum phase terms, outcome 0, no RESET correction) and delta_s
+// (planes D0[s], D1[s]) is linear in the shot's own outcomes and noise:
+//   gates            : delta unchanged
+//   rowsum (g in F)  : delta_g += delta_p
+//   pivot columns    : delta_{n+p} = delta_p, delta_p = 2 m_s
+//   deterministic M  : aph_s = aph_c + sum_{i in f} delta_i
+//   RESET, noise     : delta += 2 (b x_q - a z_q) (only parity matters)
+// Shot s's full tableau is (X, Z, c + delta_s) at any instruction.  The
+// arithmetic per generator is that of engine_bits.cuh.
 //
-// Slot (32-bit words): X[n][RS], Z[n][RS], C0[RS], C1[RS], FW[RS] (factor
-// words of the last random measurement), CW[RS] (commute parities, CTA
-// teams), D0[32][RS], D1[32][RS], then ints shot_m[32], shot_dp[32],
-// shot_acc[32], shot_ab[32], red[40].  RS odd (see engine_bits.cuh), so
-// thread s reading word w of its own delta row hits bank (s RS + w) mod 32.
-// Per-shot work is spread over (shot, chunk) pairs: thread t serves shot
-// t % 32 and word chunk t / 32.
+// Two regions per group.  The x / z region X[n][RS], Z[n][RS] (32-bit
+// words) lives in shared memory when it fits, else in global memory; the hot
+// region always lives in shared memory: C0[RS], C1[RS], FW[RS] (factor words
+// of the last random measurement), CW[RS] (commute parities of CTA teams),
+// D0[32][RS], D1[32][RS], then ints shot_m[32], shot_dp[32], shot_acc[32],
+// shot_ab[32].  RS odd (see engine_bits.cuh), so thread s reading word w of
+// its own delta row hits bank (s RS + w) mod 32.  Per-shot work is spread
+// over (shot, chunk) pairs: thread t serves shot t % 32 and word chunk t / 32.
 #pragma once
 #include "engine_bits.cuh"
 #include "team.cuh"
@@ -20,43 +34,42 @@ namespace sdim {
 
 struct SlotGroupBits2 {
   static constexpr int kShots = 32;
-  __host__ __device__ static size_t words(int n) {
-    return (size_t)SlotBits::rs(n) * (2 * (size_t)n + 4 + 2 * kShots);
+  __host__ __device__ static size_t xz_bytes(int n) { return (size_t)4 * 2 * n * SlotBits::rs(n); }
+  __host__ __device__ static size_t hot_bytes(int n) {
+    return (size_t)4 * SlotBits::rs(n) * (4 + 2 * kShots) + 4 * 4 * kShots;
   }
-  __host__ __device__ static size_t bytes(int n) { return 4 * words(n) + 4 * (4 * kShots + 40); }
 };
 
 template <class Team>
 struct TGroupBits {
+  static constexpr int kWarpBlockMax = 1024;  // threads of a block of warp teams
   Team tm;
   uint32_t *X, *Z, *C0, *C1, *FW, *CW, *D0, *D1;
   int *shot_m, *shot_dp, *shot_acc, *shot_ab;
   int n, Wn, W2, RS;
   int nact;
 
-  __device__ TGroupBits(uint8_t* slot, int n_, int /*d*/, Team team) : tm(team), n(n_) {
+  __device__ TGroupBits(uint8_t* xz, uint8_t* hot, int n_, int /*d*/, Team team) : tm(team), n(n_) {
     Wn = SlotBits::wn(n_);
     W2 = 2 * Wn;
     RS = SlotBits::rs(n_);
-    X = reinterpret_cast<uint32_t*>(slot);
+    X = reinterpret_cast<uint32_t*>(xz);
     Z = X + (size_t)n * RS;
-    C0 = Z + (size_t)n * RS;
+    C0 = reinterpret_cast<uint32_t*>(hot);
     C1 = C0 + RS;
     FW = C1 + RS;
     CW = FW + RS;
     D0 = CW + RS;
     D1 = D0 + (size_t)SlotGroupBits2::kShots * RS;
-    int* ints = reinterpret_cast<int*>(slot + 4 * SlotGroupBits2::words(n_));
+    int* ints = reinterpret_cast<int*>(D1 + (size_t)SlotGroupBits2::kShots * RS);
     shot_m = ints;
     shot_dp = ints + 32;
     shot_acc = ints + 64;
     shot_ab = ints + 96;
     nact = 0;
   }
-  static __host__ __device__ size_t slot_bytes(int n) { return SlotGroupBits2::bytes(n); }
-  static __device__ int* red_of(uint8_t* slot, int n) {
-    return reinterpret_cast<int*>(slot + 4 * SlotGroupBits2::words(n)) + 128;
-  }
+  static __host__ __device__ size_t xz_bytes(int n) { return SlotGroupBits2::xz_bytes(n); }
+  static __host__ __device__ size_t hot_bytes(int n) { return SlotGroupBits2::hot_bytes(n); }
 
   __device__ __forceinline__ int shot_of() const { return tm.t & 31; }
   __device__ __forceinline__ int chunk_of() const { return tm.t >> 5; }
@@ -64,8 +77,8 @@ struct TGroupBits {
 
   __device__ void init(int active_shots) {
     nact = active_shots;
-    const size_t words = SlotGroupBits2::words(n);
-    for (size_t i = tm.t; i < words; i += tm.size()) X[i] = 0u;
+    for (size_t i = tm.t; i < 2 * (size_t)n * RS; i += tm.size()) X[i] = 0u;
+    for (size_t i = tm.t; i < (size_t)RS * (4 + 2 * SlotGroupBits2::kShots); i += tm.size()) C0[i] = 0u;
     tm.sync();
     for (int k = tm.t; k < n; k += tm.size()) {
       Z[(size_t)k * RS + (k >> 5)] |= 1u << (k & 31);
@@ -145,7 +158,7 @@ struct TGroupBits {
       while (W2p < W2) W2p <<= 1;
       const int R = size / W2p;
       const int w = t & (W2p - 1), r = t / W2p;
-      const bool act = w < W2;
+      const bool act = w < W2 && r < R;
       uint32_t F = act ? xq[w] : 0u;
       if (w == wp) F &= ~pbit;
       if (act && r == 0) {

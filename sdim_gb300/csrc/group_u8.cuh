@@ -1,6 +1,6 @@
 // Shot-group engine for odd prime d (residue bytes), any team size.
 //
-// Same decomposition as the d = 2 group engine (engine_group.cuh): the 32
+// Same decomposition as the d = 2 group engine (group_bits.cuh): the 32
 // shots of a group share the x / z blocks and a common phase vector c; shot
 // s keeps delta_s with ph_s = c + delta_s (mod d).  Every update of the
 // reference's ExtendedTableau (sdim/tableau/tableau_prime.py:262-380) is
@@ -12,13 +12,19 @@
 //   deterministic outcome    : aph_s = aph_c + sum_i f_i delta_i
 //   RESET (k = -m_s), noise  : delta += (cx x_q + cz z_q)
 //
-// Slot layout (bytes): X[n][S], Z[n][S], C[S], FW[S] (factors f_g), CX[NP],
-// CZ[NP], D[32][S] (deltas), then ints: shot_m[32], shot_dp[32], shot_acc[32],
-// shot_ab[32], red[40].  S as in engine_u8.cuh (S / 4 odd: 32 threads reading
-// the same generator of 32 different delta rows hit 32 banks).
+// Two regions per group.  The x / z region X[n][S], Z[n][S] (bytes; row k =
+// qudit k, column g = generator g) lives in shared memory when it fits, else
+// in global memory; the hot region always lives in shared memory:
+// C[S], FW[S] (factors), CX[NP], CZ[NP] (pivot column), D[32][S] (deltas),
+// DOT[S] ints (column dot products), then ints shot_m[32], shot_dp[32],
+// shot_acc[32], shot_ab[32].  S is a multiple of 4 with S / 4 odd, so 32
+// threads reading the same generator of 32 delta rows hit 32 banks.
 //
-// Per-shot work is spread over (shot, chunk) thread pairs: thread t serves
-// shot t % 32 and generator chunk t / 32 (one chunk in a warp team).
+// The rowsum of a random measurement is a rank-1 update of X and Z plus the
+// column dots Z^T x_p: threads own 32-bit words (4 generators) of a set of
+// rows and keep four rows in flight, so an x / z region in global memory is
+// read and written at full width.  Per-shot work is spread over (shot,
+// chunk) thread pairs: thread t serves shot t % 32 and chunk t / 32.
 #pragma once
 #include "engine_u8.cuh"
 #include "team.cuh"
@@ -27,52 +33,53 @@ namespace sdim {
 
 struct SlotGroupU8 {
   static constexpr int kShots = 32;
-  __host__ __device__ static size_t int_offset(int n) {
+  __host__ __device__ static size_t xz_bytes(int n) { return 2 * (size_t)n * SlotU8::stride(n); }
+  __host__ __device__ static size_t hot_bytes(int n) {
     const size_t s = (size_t)SlotU8::stride(n);
-    const size_t b = (2 * (size_t)n + 2 + kShots) * s + 2 * (size_t)SlotU8::npad(n);
-    return (b + 15) & ~(size_t)15;
+    const size_t b = (2 + kShots) * s + 2 * (size_t)SlotU8::npad(n) + 4 * s;
+    return ((b + 15) & ~(size_t)15) + 4 * 4 * kShots;
   }
-  __host__ __device__ static size_t bytes(int n) { return int_offset(n) + 4 * (4 * kShots + 40); }
 };
 
 template <int DD, class Team>
 struct TGroupU8 {
+  static constexpr int kWarpBlockMax = 512;  // threads of a block of warp teams
   Team tm;
   ModU8<DD> M;
   uint8_t *X, *Z, *C, *FW, *CX, *CZ, *D;
+  int* DOT;
   int *shot_m, *shot_dp, *shot_acc, *shot_ab;
   int n, S;
   int nact;  // shots of this group that exist
 
-  __device__ TGroupU8(uint8_t* slot, int n_, int d, Team team) : tm(team), M(d), n(n_) {
+  __device__ TGroupU8(uint8_t* xz, uint8_t* hot, int n_, int d, Team team) : tm(team), M(d), n(n_) {
     S = SlotU8::stride(n_);
     const int np = SlotU8::npad(n_);
-    X = slot;
+    X = xz;
     Z = X + (size_t)n * S;
-    C = Z + (size_t)n * S;
+    C = hot;
     FW = C + S;
     D = FW + S;
     CX = D + (size_t)SlotGroupU8::kShots * S;
     CZ = CX + np;
-    int* ints = reinterpret_cast<int*>(slot + SlotGroupU8::int_offset(n_));
+    DOT = reinterpret_cast<int*>(CZ + np);
+    const size_t b = (2 + SlotGroupU8::kShots) * (size_t)S + 2 * (size_t)np + 4 * (size_t)S;
+    int* ints = reinterpret_cast<int*>(hot + ((b + 15) & ~(size_t)15));
     shot_m = ints;
     shot_dp = ints + 32;
     shot_acc = ints + 64;
     shot_ab = ints + 96;
     nact = 0;
   }
-  static __host__ __device__ size_t slot_bytes(int n) { return SlotGroupU8::bytes(n); }
-  static __device__ int* red_of(uint8_t* slot, int n) {
-    return reinterpret_cast<int*>(slot + SlotGroupU8::int_offset(n)) + 128;
-  }
+  static __host__ __device__ size_t xz_bytes(int n) { return SlotGroupU8::xz_bytes(n); }
+  static __host__ __device__ size_t hot_bytes(int n) { return SlotGroupU8::hot_bytes(n); }
 
   __device__ void init(int active_shots) {
     nact = active_shots;
-    const size_t words = ((2 * (size_t)n + 2) * S) >> 2;  // X, Z, C, FW
-    uint32_t* w = reinterpret_cast<uint32_t*>(X);
-    for (size_t i = tm.t; i < words; i += tm.size()) w[i] = 0u;
-    uint32_t* dw = reinterpret_cast<uint32_t*>(D);
-    for (size_t i = tm.t; i < ((size_t)SlotGroupU8::kShots * S) >> 2; i += tm.size()) dw[i] = 0u;
+    uint32_t* xw = reinterpret_cast<uint32_t*>(X);
+    for (size_t i = tm.t; i < ((2 * (size_t)n * S) >> 2); i += tm.size()) xw[i] = 0u;
+    uint32_t* hw = reinterpret_cast<uint32_t*>(C);
+    for (size_t i = tm.t; i < (((2 + (size_t)SlotGroupU8::kShots) * S) >> 2); i += tm.size()) hw[i] = 0u;
     tm.sync();
     for (int k = tm.t; k < n; k += tm.size()) {
       Z[(size_t)k * S + k] = 1;
@@ -162,6 +169,86 @@ struct TGroupU8 {
   }
   __device__ __forceinline__ void set_shot_ab(int s, int cz, int cx) { shot_ab[s] = cz | (cx << 8); }
 
+  // One 32-bit word of 4 residues of a row absorbs the pivot entries (a, b):
+  // x_j += f_j a, z_j += f_j b; dots_j += z_j a (old z).
+  __device__ __forceinline__ void word_update(uint32_t& xw, uint32_t& zw, uint32_t fw, int a, int b, int* dots) const {
+    uint32_t xo = 0u, zo = 0u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int f = (fw >> (8 * j)) & 0xff;
+      const int x = (xw >> (8 * j)) & 0xff, z = (zw >> (8 * j)) & 0xff;
+      dots[j] += z * a;
+      xo |= (uint32_t)M.md(x + f * a) << (8 * j);
+      zo |= (uint32_t)M.md(z + f * b) << (8 * j);
+    }
+    xw = xo;
+    zw = zo;
+  }
+
+  // Shared rowsum (tableau_prime.py:308-322) as a rank-1 update of X and Z
+  // over the words with a nonzero factor, with the dots Z^T x_p in DOT.
+  // Needs FW (all 2n factors) and CX / CZ; leaves DOT[g] for every generator.
+  __device__ void rank1(int p) {
+    const int size = tm.size(), t = tm.t;
+    const int words = (2 * n + 3) >> 2;  // 32-bit words per row holding generators
+    for (int g = t; g < 2 * n; g += size) DOT[g] = 0;
+    tm.sync();
+    const int R = size >= words ? size / words : 1;     // row groups
+    const int act_threads = size >= words ? R * words : size;
+    if (t < act_threads) {
+      const int w0 = size >= words ? t % words : t;
+      const int r = size >= words ? t / words : 0;
+      const uint32_t* fws = reinterpret_cast<const uint32_t*>(FW);
+      for (int w = w0; w < words; w += (size >= words ? words : size)) {
+        const uint32_t fw = fws[w];
+        if (fw == 0u) continue;
+        int dots[4] = {0, 0, 0, 0};
+        uint32_t* xcol = reinterpret_cast<uint32_t*>(X) + w;
+        uint32_t* zcol = reinterpret_cast<uint32_t*>(Z) + w;
+        const int S4 = S >> 2;
+        int k = r;
+        for (; k + 3 * R < n; k += 4 * R) {
+          uint32_t x0 = xcol[(size_t)k * S4], x1 = xcol[(size_t)(k + R) * S4];
+          uint32_t x2 = xcol[(size_t)(k + 2 * R) * S4], x3 = xcol[(size_t)(k + 3 * R) * S4];
+          uint32_t z0 = zcol[(size_t)k * S4], z1 = zcol[(size_t)(k + R) * S4];
+          uint32_t z2 = zcol[(size_t)(k + 2 * R) * S4], z3 = zcol[(size_t)(k + 3 * R) * S4];
+          word_update(x0, z0, fw, CX[k], CZ[k], dots);
+          word_update(x1, z1, fw, CX[k + R], CZ[k + R], dots);
+          word_update(x2, z2, fw, CX[k + 2 * R], CZ[k + 2 * R], dots);
+          word_update(x3, z3, fw, CX[k + 3 * R], CZ[k + 3 * R], dots);
+          xcol[(size_t)k * S4] = x0;
+          xcol[(size_t)(k + R) * S4] = x1;
+          xcol[(size_t)(k + 2 * R) * S4] = x2;
+          xcol[(size_t)(k + 3 * R) * S4] = x3;
+          zcol[(size_t)k * S4] = z0;
+          zcol[(size_t)(k + R) * S4] = z1;
+          zcol[(size_t)(k + 2 * R) * S4] = z2;
+          zcol[(size_t)(k + 3 * R) * S4] = z3;
+          // keep the dot sums small: reduce every block of four rows
+#pragma unroll
+          for (int j = 0; j < 4; ++j) dots[j] = M.md(dots[j]);
+        }
+        for (; k < n; k += R) {
+          uint32_t x0 = xcol[(size_t)k * S4], z0 = zcol[(size_t)k * S4];
+          word_update(x0, z0, fw, CX[k], CZ[k], dots);
+          xcol[(size_t)k * S4] = x0;
+          zcol[(size_t)k * S4] = z0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int g = 4 * w + j;
+          if (g < 2 * n && ((fw >> (8 * j)) & 0xff)) {
+            if (R > 1)
+              atomicAdd(&DOT[g], M.md(dots[j]));
+            else
+              DOT[g] = M.md(dots[j]);
+          }
+        }
+      }
+    }
+    tm.sync();
+  }
+
   // ---------------- Z measurement of every shot of the group ----------------
   // Outcome of shot s left in shot_m[s]; returns the (shared) deterministic flag.
   __device__ int measure(int q, unsigned long long seed, long long group_shot0, uint32_t ordinal) {
@@ -199,29 +286,20 @@ struct TGroupU8 {
         CZ[k] = (uint8_t)b;
         sl += a * b;
       }
+      // factors of every generator; stabilizer p and the padding stay 0
+      for (int g = t; g < S; g += size) FW[g] = (g < 2 * n && g != p) ? (uint8_t)M.neg(xq[g]) : (uint8_t)0;
       const int s1 = M.md(tm.add(sl));
       const int phc = C[p];
       if (ch == 0) shot_dp[s] = live ? ds[p] : 0;
       tm.sync();
-      // shared rowsum over owned columns (tableau_prime.py:308-322)
+      rank1(p);
+      // common phases of the absorbing generators
       for (int g = t; g < 2 * n; g += size) {
-        const int f = (g == p) ? 0 : M.neg(xq[g]);
-        FW[g] = (uint8_t)f;
+        const int f = FW[g];
         if (f == 0) continue;
-        int dot = 0;
-        uint8_t* xc = X + g;
-        uint8_t* zc = Z + g;
-        for (int k = 0; k < n; ++k) {
-          const int x = xc[(size_t)k * S], z = zc[(size_t)k * S];
-          const int a = CX[k], b = CZ[k];
-          dot += z * a;
-          xc[(size_t)k * S] = (uint8_t)M.md(x + f * a);
-          zc[(size_t)k * S] = (uint8_t)M.md(z + f * b);
-        }
         const int half = M.md(s1 * ((f * (f - 1)) >> 1));
-        C[g] = (uint8_t)M.mo(C[g] + phc * f + M.phi * M.md(f * M.md(dot)) + M.phi * M.phi * half);
+        C[g] = (uint8_t)M.mo(C[g] + phc * f + M.phi * M.md(f * DOT[g]) + M.phi * M.phi * half);
       }
-      tm.sync();
       // per shot: delta_g += f_g delta_p
       const int dp = live ? shot_dp[s] : 0;
       if (dp) {
@@ -230,6 +308,7 @@ struct TGroupU8 {
           if (f) ds[g] = (uint8_t)M.mo(ds[g] + f * dp);
         }
       }
+      tm.sync();
       // shared pivot columns: destabilizer p <- stabilizer p, stabilizer p <- Z_q
       for (int k = t; k < n; k += size) {
         X[(size_t)k * S + n + p] = CX[k];
@@ -237,7 +316,6 @@ struct TGroupU8 {
         X[(size_t)k * S + p] = 0;
         Z[(size_t)k * S + p] = (uint8_t)(k == q);
       }
-      tm.sync();
       if (ch == 0) {
         int m = 0;
         if (live) {
@@ -254,8 +332,9 @@ struct TGroupU8 {
       tm.sync();
       return 0;
     }
-    // deterministic (tableau_prime.py:336-363), f_i = destab_x[q][i]
-    for (int i = t; i < n; i += size) CX[i] = xq[n + i];
+    // deterministic (tableau_prime.py:336-363), f_i = destab_x[q][i]; the
+    // factor row is read back as 32-bit words, so its padding is zeroed
+    for (int i = t; i < SlotU8::npad(n); i += size) CX[i] = i < n ? xq[n + i] : (uint8_t)0;
     if (ch == 0) shot_acc[s] = 0;
     tm.sync();
     int pl = 0, dl = 0;
@@ -263,20 +342,31 @@ struct TGroupU8 {
       const int f = CX[i];
       if (!f) continue;
       pl += f * C[i];
-      int cd = 0;
-      for (int k = 0; k < n; ++k) cd += X[(size_t)k * S + i] * Z[(size_t)k * S + i];
-      dl += M.md(M.md(cd) * ((f * (f - 1)) >> 1));
+      if (f > 1) {
+        int cd = 0;
+        for (int k = 0; k < n; ++k) cd += X[(size_t)k * S + i] * Z[(size_t)k * S + i];
+        dl += M.md(M.md(cd) * ((f * (f - 1)) >> 1));
+      }
     }
+    // cross term: rows over threads, each row read as 32-bit words
     int tl = 0;
+    const int nw = (n + 3) >> 2;
+    const uint32_t* fq = reinterpret_cast<const uint32_t*>(CX);
     for (int k = t; k < n; k += size) {
-      const uint8_t* xr = X + (size_t)k * S;
-      const uint8_t* zr = Z + (size_t)k * S;
+      const uint32_t* xr = reinterpret_cast<const uint32_t*>(X + (size_t)k * S);
+      const uint32_t* zr = reinterpret_cast<const uint32_t*>(Z + (size_t)k * S);
       int pre = 0, acc = 0;
-      for (int i = 0; i < n; ++i) {
-        const int f = CX[i];
-        if (f) {
-          acc = M.md(acc + f * xr[i] * pre);
-          pre = M.md(pre + f * zr[i]);
+      for (int w = 0; w < nw; ++w) {
+        const uint32_t fw = fq[w];
+        if (!fw) continue;
+        const uint32_t xw = xr[w], zw = zr[w];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int f = (fw >> (8 * j)) & 0xff;
+          if (f) {
+            acc = M.md(acc + f * (int)((xw >> (8 * j)) & 0xff) * pre);
+            pre = M.md(pre + f * (int)((zw >> (8 * j)) & 0xff));
+          }
         }
       }
       tl += acc;

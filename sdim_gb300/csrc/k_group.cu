@@ -9,7 +9,8 @@ namespace {
 
 template <class G, bool CTA>
 struct Group {
-  static size_t slot_bytes(int n) { return (G::slot_bytes(n) + 15) & ~(size_t)15; }
+  static size_t hot_bytes(int n) { return round16(G::hot_bytes(n)); }
+  static size_t big_bytes(int n) { return round16(G::xz_bytes(n)); }
   static cudaError_t set_smem(int bytes) {
     cudaError_t e;
     if constexpr (CTA)
@@ -33,20 +34,22 @@ struct Group {
     return nb < 1 ? 1 : nb;
   }
   static void persistent(dim3 g, dim3 b, size_t smem, cudaStream_t s, const CircuitDesc* descs, int nc,
-                         long long total, unsigned long long* counter, uint8_t* gslots, size_t slot, int smem_slots,
-                         int* status) {
+                         long long total, unsigned long long* counter, uint8_t* gbuf, size_t big, size_t hot,
+                         int in_smem, int* status) {
     if constexpr (CTA)
-      k_group_cta<G><<<g, b, smem, s>>>(descs, nc, total, counter, gslots, slot, smem_slots, status);
+      k_group_cta<G><<<g, b, smem, s>>>(descs, nc, total, counter, gbuf, big, hot, in_smem, status);
     else
-      k_group_warp<G><<<g, b, smem, s>>>(descs, nc, total, counter, gslots, slot, smem_slots, status);
+      k_group_warp<G><<<g, b, smem, s>>>(descs, nc, total, counter, gbuf, big, hot, in_smem, status);
   }
   static void snapshot(dim3 block, size_t smem, cudaStream_t s, const CircuitDesc* desc, long long group,
-                       uint8_t* gslot, int smem_slot, int8_t* snap, int mode, int lane, int* status) {
-    k_group_snapshot<G, CTA><<<1, CTA ? block : dim3(32), smem, s>>>(desc, group, gslot, smem_slot, snap, mode, lane,
-                                                                     status);
+                       uint8_t* gbuf, size_t big, size_t hot, int in_smem, int8_t* snap, int mode, int lane,
+                       int* status) {
+    k_group_snapshot<G, CTA><<<1, CTA ? block : dim3(32), smem, s>>>(desc, group, gbuf, big, hot, in_smem, snap,
+                                                                     mode, lane, status);
   }
   static const VariantOps& ops() {
-    static const VariantOps o = {1, CTA ? 1 : 0, slot_bytes, set_smem, occupancy, persistent, nullptr, snapshot};
+    static const VariantOps o = {1, CTA ? 1 : 0, CTA ? 512 : G::kWarpBlockMax, hot_bytes, big_bytes, set_smem,
+                                 occupancy, persistent, nullptr, snapshot};
     return o;
   }
 };

@@ -8,7 +8,8 @@ namespace {
 
 template <class E>
 struct PerShot {
-  static size_t slot_bytes(int n) { return (E::slot_bytes(n) + 15) & ~(size_t)15; }
+  static size_t hot_bytes(int) { return 0; }
+  static size_t big_bytes(int n) { return round16(E::slot_bytes(n)); }
   static cudaError_t set_smem(int bytes) {
     cudaError_t e = set_dynamic_smem(k_persistent<E>, bytes);
     if (e != cudaSuccess) return e;
@@ -25,20 +26,21 @@ struct PerShot {
     return nb < 1 ? 1 : nb;
   }
   static void persistent(dim3 g, dim3 b, size_t smem, cudaStream_t s, const CircuitDesc* descs, int nc,
-                         long long total, unsigned long long* counter, uint8_t* gslots, size_t slot, int smem_slots,
-                         int* status) {
-    k_persistent<E><<<g, b, smem, s>>>(descs, nc, total, counter, gslots, slot, smem_slots, status);
+                         long long total, unsigned long long* counter, uint8_t* gbuf, size_t big, size_t,
+                         int in_smem, int* status) {
+    k_persistent<E><<<g, b, smem, s>>>(descs, nc, total, counter, gbuf, big, in_smem, status);
   }
-  static void single(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gslot,
-                     int smem_slot, int* status) {
-    k_single<E><<<1, 32, smem, s>>>(desc, shot, gslot, smem_slot, status);
+  static void single(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gbuf,
+                     int in_smem, int* status) {
+    k_single<E><<<1, 32, smem, s>>>(desc, shot, gbuf, in_smem, status);
   }
-  static void snapshot(dim3, size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gslot,
-                       int smem_slot, int8_t* snap, int mode, int, int* status) {
-    k_snapshot<E><<<1, 32, smem, s>>>(desc, shot, gslot, smem_slot, snap, mode, status);
+  static void snapshot(dim3, size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gbuf,
+                       size_t, size_t, int in_smem, int8_t* snap, int mode, int, int* status) {
+    k_snapshot<E><<<1, 32, smem, s>>>(desc, shot, gbuf, in_smem, snap, mode, status);
   }
   static const VariantOps& ops() {
-    static const VariantOps o = {0, 0, slot_bytes, set_smem, occupancy, persistent, single, snapshot};
+    static const VariantOps o = {0, 0, 1024, hot_bytes, big_bytes, set_smem, occupancy, persistent, single,
+                                 snapshot};
     return o;
   }
 };

@@ -194,19 +194,22 @@ __device__ __forceinline__ int find_desc(const CircuitDesc* descs, int ncirc, lo
   return lo;
 }
 
+// Group slots: a hot region (hot_bytes, always shared memory) and an x / z
+// region (xz_bytes) in shared memory right after it when xz_in_smem, else in
+// global memory at gxz + slot * xz_bytes.
+
 // Persistent shot-group kernel, one warp per group: items are
-// (program, group of 32 shots); each warp owns one slot (shared memory when
-// smem_slots != 0, else global memory).
+// (program, group of 32 shots); each warp owns one slot.
 template <class G>
-__global__ void __launch_bounds__(1024) k_group_warp(const CircuitDesc* __restrict__ descs, int ncirc,
+__global__ void __launch_bounds__(G::kWarpBlockMax) k_group_warp(const CircuitDesc* __restrict__ descs, int ncirc,
                                                      long long total_items, unsigned long long* __restrict__ counter,
-                                                     uint8_t* gslots, size_t slot_bytes, int smem_slots,
+                                                     uint8_t* gxz, size_t xz_bytes, size_t hot_bytes, int xz_in_smem,
                                                      int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  uint8_t* slot = smem_slots ? smem + (size_t)warp * slot_bytes
-                             : gslots + ((size_t)blockIdx.x * wpb + warp) * slot_bytes;
+  uint8_t* hot = smem + (size_t)warp * (hot_bytes + (xz_in_smem ? xz_bytes : 0));
+  uint8_t* xz = xz_in_smem ? hot + hot_bytes : gxz + ((size_t)blockIdx.x * wpb + warp) * xz_bytes;
   for (;;) {
     unsigned long long it = 0;
     if (lane == 0) it = atomicAdd(counter, 1ull);
@@ -214,7 +217,7 @@ __global__ void __launch_bounds__(1024) k_group_warp(const CircuitDesc* __restri
     if ((long long)it >= total_items) break;
     const int ci = find_desc<G>(descs, ncirc, (long long)it);
     const CircuitDesc c = descs[ci];
-    G eng(slot, c.n, c.d, WarpTeam());
+    G eng(xz, hot, c.n, c.d, WarpTeam());
     run_tgroup<G, false>(c, (long long)it - c.item_begin, eng, nullptr, SNAP_NONE, 0, status);
     if (*(volatile int*)status != DEV_OK) break;
   }
@@ -225,11 +228,13 @@ __global__ void __launch_bounds__(1024) k_group_warp(const CircuitDesc* __restri
 template <class G>
 __global__ void __launch_bounds__(512) k_group_cta(const CircuitDesc* __restrict__ descs, int ncirc,
                                                    long long total_items, unsigned long long* __restrict__ counter,
-                                                   uint8_t* gslots, size_t slot_bytes, int smem_slots, int* status) {
+                                                   uint8_t* gxz, size_t xz_bytes, size_t hot_bytes, int xz_in_smem,
+                                                   int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int red[40];
   __shared__ long long item;
-  uint8_t* slot = smem_slots ? smem : gslots + (size_t)blockIdx.x * slot_bytes;
+  uint8_t* hot = smem;
+  uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
   for (;;) {
     if (threadIdx.x == 0) item = (long long)atomicAdd(counter, 1ull);
     __syncthreads();
@@ -238,7 +243,7 @@ __global__ void __launch_bounds__(512) k_group_cta(const CircuitDesc* __restrict
     if (it >= total_items) break;
     const int ci = find_desc<G>(descs, ncirc, it);
     const CircuitDesc c = descs[ci];
-    G eng(slot, c.n, c.d, CtaTeam(red));
+    G eng(xz, hot, c.n, c.d, CtaTeam(red));
     run_tgroup<G, false>(c, it - c.item_begin, eng, nullptr, SNAP_NONE, 0, status);
     __syncthreads();
     if (*(volatile int*)status != DEV_OK) break;
@@ -249,17 +254,20 @@ __global__ void __launch_bounds__(512) k_group_cta(const CircuitDesc* __restrict
 // CTA-team engines run with blockDim threads, warp-team engines with 32.
 template <class G, bool CTA>
 __global__ void __launch_bounds__(512) k_group_snapshot(const CircuitDesc* __restrict__ desc, long long group,
-                                                        uint8_t* gslot, int smem_slot, int8_t* snap, int snap_mode,
-                                                        int snap_lane, int* status) {
+                                                        uint8_t* gxz, size_t xz_bytes, size_t hot_bytes,
+                                                        int xz_in_smem, int8_t* snap, int snap_mode, int snap_lane,
+                                                        int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int red[40];
   const CircuitDesc c = *desc;
-  uint8_t* slot = smem_slot ? smem : gslot;
+  uint8_t* hot = smem;
+  uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz;
+  (void)xz_bytes;
   if constexpr (CTA) {
-    G eng(slot, c.n, c.d, CtaTeam(red));
+    G eng(xz, hot, c.n, c.d, CtaTeam(red));
     run_tgroup<G, true>(c, group, eng, snap, snap_mode, snap_lane, status);
   } else {
-    G eng(slot, c.n, c.d, WarpTeam());
+    G eng(xz, hot, c.n, c.d, WarpTeam());
     run_tgroup<G, true>(c, group, eng, snap, snap_mode, snap_lane, status);
   }
 }

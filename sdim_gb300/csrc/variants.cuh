@@ -30,22 +30,29 @@ enum Variant : int {
   V_COUNT
 };
 
+// A slot is a shared-memory part of `hot` bytes plus a part of `big` bytes
+// that sits in shared memory right after it (in_smem) or in global memory at
+// gbuf + slot_index * big.  Per-shot engines have hot = 0 and keep the whole
+// tableau in the big part; group engines keep the x / z blocks there.
 struct VariantOps {
-  int group;  // 1: items are 32-shot groups
-  int cta;    // 1: one CTA per slot (block threads given by the planner)
-  size_t (*slot_bytes)(int n);
+  int group;      // 1: items are 32-shot groups
+  int cta;        // 1: one CTA per slot (block threads given by the planner)
+  int max_block;  // threads per block of the persistent kernel
+  size_t (*hot_bytes)(int n);
+  size_t (*big_bytes)(int n);
   cudaError_t (*set_smem)(int bytes);
   int (*occupancy)(int block, size_t smem);
   void (*persistent)(dim3 grid, dim3 block, size_t smem, cudaStream_t s, const CircuitDesc* descs, int nc,
-                     long long total, unsigned long long* counter, uint8_t* gslots, size_t slot, int smem_slots,
-                     int* status);
+                     long long total, unsigned long long* counter, uint8_t* gbuf, size_t big, size_t hot,
+                     int in_smem, int* status);
   // per-shot engines: one shot, one warp
-  void (*single)(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gslot, int smem_slot,
+  void (*single)(size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot, uint8_t* gbuf, int in_smem,
                  int* status);
   // tableau export of one shot (per-shot engines: shot index; group engines:
   // group 0 of desc, exported lane)
   void (*snapshot)(dim3 block, size_t smem, cudaStream_t s, const CircuitDesc* desc, long long shot_or_group,
-                   uint8_t* gslot, int smem_slot, int8_t* snap, int mode, int lane, int* status);
+                   uint8_t* gbuf, size_t big, size_t hot, int in_smem, int8_t* snap, int mode, int lane,
+                   int* status);
 };
 
 // Shared memory the planner leaves for the kernels' static arrays.
@@ -61,6 +68,8 @@ inline cudaError_t set_dynamic_smem(K kernel, int optin_bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               optin_bytes - (int)a.sharedSizeBytes);
 }
+
+inline size_t round16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 const VariantOps& pershot_ops(int variant);
 const VariantOps& group_ops(int variant);
