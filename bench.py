@@ -57,7 +57,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="surface", choices=["surface", "pr1", "oddd5", "oddd7", "uneven"])
+    ap.add_argument("--workload", default="surface",
+                    choices=["surface", "pr1", "oddd5", "oddd7", "uneven", "serving"])
+    ap.add_argument("--rate", type=float, default=2000.0, help="serving: mean arrivals per second")
+    ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
+    ap.add_argument("--n-max", type=int, default=2048, help="serving: largest qudit count")
+    ap.add_argument("--shots-max", type=int, default=10_000, help="serving: largest shot count")
+    ap.add_argument("--lanes", type=int, default=4, help="serving: batches in flight")
     ap.add_argument("--shots", type=int, default=None, help="shots per GPU (single-program workloads)")
     ap.add_argument("--circuits", type=int, default=8192, help="programs of the uneven batch")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
@@ -594,6 +600,70 @@ def run_uneven(args, torch, dist, ws, rank, local):
     }
 
 
+def serving_trace(args, seed=0):
+    """Poisson arrivals: n log-uniform [16, n_max], d uniform {2,3,5}, 8n
+    random {H,P,CNOT} gates + MEASURE all, shots log-uniform [1, shots_max]."""
+    from sdim_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(seed))
+    trace, t = [], 0.0
+    while True:
+        t += float(rng.exponential(1.0 / args.rate))
+        if t >= args.duration:
+            break
+        n = int(round(np.exp(rng.uniform(np.log(16), np.log(args.n_max)))))
+        d = int((2, 3, 5)[rng.integers(3)])
+        shots = max(1, int(round(np.exp(rng.uniform(0.0, np.log(args.shots_max))))))
+        table = W.random_hpc_table(n, 8 * n, seed=rng)
+        trace.append((t, table, n, d, shots, len(trace)))
+    return trace
+
+
+def run_serving(args, rank, local):
+    from sdim_gb300.serving import Server, replay
+
+    trace = serving_trace(args)
+    units = sum(s * tb.shape[0] for _, tb, _, _, s, _ in trace)
+    # warm-up: compile paths and grow buffers on a few requests
+    warm = Server(device=local, lanes=args.lanes)
+    replay(warm, [(0.0, *r[1:]) for r in trace[:8]])
+    warm.close()
+    clocks = Clocks(local)
+    clocks.start()
+    server = Server(device=local, lanes=args.lanes)
+    t0 = time.perf_counter()
+    done = replay(server, trace)
+    wall = time.perf_counter() - t0
+    st = server.stats(done)
+    batches = server.batches
+    server.close()
+    clk = clocks.stop()
+    # plain: one request at a time, one lane, same arrivals
+    plain = Server(device=local, lanes=1, max_batch_requests=1)
+    tp = time.perf_counter()
+    pdone = replay(plain, trace)
+    pwall = time.perf_counter() - tp
+    pst = plain.stats(pdone)
+    plain.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": METRIC, "value": units / wall, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 bit planes (d=2) / u8 residues (odd d)", "data": "synthetic Poisson trace (seeded)",
+        "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s, n log-uniform "
+                               f"[16,{args.n_max}], d in {{2,3,5}}, 8n gates + MEASURE all, shots log-uniform "
+                               f"[1,{args.shots_max}]", "requests": len(trace), "lanes": args.lanes},
+        "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "mean": st["mean_ms"]},
+        "shots_per_s": st["shots_per_s"], "batches": batches,
+        "plain_gpu": {"value": units / pwall, "unit": UNIT, "form": "one request at a time, one lane",
+                      "latency_ms": {"p50": pst["p50_ms"], "p99": pst["p99_ms"]}},
+        "batched_vs_plain": (units / wall) / (units / pwall),
+        "e2e": {"value": units / wall, "unit": UNIT, "note": "requests submitted as host op tables, records "
+                                                            "returned to host memory"},
+        "clocks": clk,
+    }
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
@@ -604,6 +674,8 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     if args.workload == "uneven":
         line = run_uneven(args, torch, dist, ws, rank, local)
+    elif args.workload == "serving":
+        line = run_serving(args, rank, local)
     else:
         line = run_single(args, torch, dist, ws, rank, local)
     if ws > 1:

@@ -63,6 +63,12 @@ const char* sdim_last_error(const sdim_ctx* ctx);
 /* info[0] = SM count, [1] = opt-in shared memory per block (bytes),
  * [2] = L2 bytes, [3] = total global memory (bytes). */
 int sdim_device_info(sdim_ctx* ctx, int64_t info[4]);
+/* info[0] = free device bytes, [1] = total device bytes, [2] = bytes this
+ * context holds in its buffers.  Used by the serving loop's admission. */
+int sdim_memory_info(sdim_ctx* ctx, int64_t info[3]);
+/* Device bytes a run of nshots shots of circ needs: out[0] records,
+ * out[1] one shot-group slot (shared-memory part plus x / z part). */
+int sdim_program_bytes(const sdim_circuit* circ, int64_t nshots, int64_t out[2]);
 
 /* Encodes one program.  ops is nops rows of 4 int32:
  *   gate id (sdim/gatedata.py:55-102: I 0, X 1, X_INV 2, Z 3, Z_INV 4, H 5,
@@ -98,12 +104,34 @@ int sdim_run_device(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int6
 int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, const uint64_t* seeds,
                    const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs, void* stream,
                    unsigned flags);
+/* Many programs given as op tables, encoded and run in one call: the serving
+ * path.  Program i is rows[row_begin[i] .. row_begin[i+1]) (4 int32 per row as
+ * in sdim_encode_circuit), noise_prob (may be NULL) is indexed like rows, and
+ * n[i], d[i], seeds[i], shot0[i], nshots[i], outs[i] as in sdim_run_batch.
+ * The instruction streams go through a pinned staging buffer and a device
+ * arena owned by the context, so no device memory is allocated per program;
+ * at most one call may be in flight per context.  With SDIM_FLAG_ASYNC and
+ * host outputs, the call returns once the work is queued (see sdim_query).
+ * No counterpart in the reference (one Program.simulate per request). */
+int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t* row_begin,
+                    const double* noise_prob, const int32_t* n, const int32_t* d, const uint64_t* seeds,
+                    const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs, void* stream,
+                    unsigned flags);
 /* Measured shared-memory read bandwidth of the device in GB/s (all SMs):
  * the roofline denominator for tableaux resident in shared memory.  No
  * counterpart in the reference (which has no device code). */
 int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs);
-/* Waits for the context's work and reports a device-side error, if any. */
+/* Waits for the context's last launch stream and reports a device-side
+ * error, if any.  With SDIM_FLAG_ASYNC, sdim_run_batch with host outputs
+ * returns after queueing the kernels and the record copies; the host buffers
+ * (pinned, e.g. from sdim_host_alloc) must stay alive until sdim_query
+ * returns 1 or sdim_sync returns. */
 int sdim_sync(sdim_ctx* ctx);
+/* 1 when the context's last launch stream is idle, 0 while it runs, < 0 on error. */
+int sdim_query(sdim_ctx* ctx);
+/* Pinned host memory for asynchronous record copies. */
+int sdim_host_alloc(size_t bytes, void** out);
+int sdim_host_free(void* p);
 /* Milliseconds of the kernels of the last call made with SDIM_FLAG_TIME. */
 double sdim_last_kernel_ms(const sdim_ctx* ctx);
 

@@ -38,6 +38,8 @@ SIGNATURES = {
     "sdim_ctx_destroy": (C.c_int, [_P]),
     "sdim_last_error": (C.c_char_p, [_P]),
     "sdim_device_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sdim_memory_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sdim_program_bytes": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int64)]),
     "sdim_encode_circuit": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int, C.c_int, C.POINTER(_P)]),
     "sdim_circuit_destroy": (C.c_int, [_P]),
     "sdim_circuit_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
@@ -45,6 +47,10 @@ SIGNATURES = {
     "sdim_run_device": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, _P, C.c_uint]),
     "sdim_run_batch": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.c_uint]),
     "sdim_sync": (C.c_int, [_P]),
+    "sdim_query": (C.c_int, [_P]),
+    "sdim_run_tables": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_uint]),
+    "sdim_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
+    "sdim_host_free": (C.c_int, [_P]),
     "sdim_last_kernel_ms": (C.c_double, [_P]),
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),

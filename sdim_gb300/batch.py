@@ -14,7 +14,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _lib
-from .encode import DeviceProgram, encode_program
+from .encode import DeviceProgram, encode_program, encode_table
 
 
 @dataclass
@@ -31,8 +31,10 @@ class BatchRunner:
         self.entries: List[BatchEntry] = []
 
     def add_spec(self, spec, shots: int, seed: int, shot0: int = 0, noise: bool = True) -> BatchEntry:
-        circuit = spec.build()
-        enc = encode_program([circuit], spec.num_qudits, spec.dimension, noise=noise)
+        if getattr(spec, "table", None) is not None:
+            enc = encode_table(spec.table, spec.num_qudits, spec.dimension)
+        else:
+            enc = encode_program([spec.build()], spec.num_qudits, spec.dimension, noise=noise)
         e = BatchEntry(DeviceProgram(self.ctx, enc), int(shots), int(seed), int(shot0))
         self.entries.append(e)
         return e

@@ -26,13 +26,16 @@ struct DevBuf {
 struct sdim_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t last_stream = nullptr;  // stream of the last launch (sdim_sync / sdim_query)
   int num_sms = 0;
   int smem_optin = 0;
   int64_t l2_bytes = 0;
   int64_t gmem_bytes = 0;
   size_t gmem_slot_budget = (size_t)8 << 30;
   std::string err;
-  DevBuf descs, counters, status, gslots, out, snap;
+  DevBuf descs, counters, status, gslots, out, snap, arena;
+  void* staging = nullptr;  // pinned host staging of sdim_run_tables
+  size_t staging_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timing_pending = false;
   double last_ms = 0.0;
@@ -71,10 +74,11 @@ int cuda_fail(sdim_ctx* ctx, cudaError_t e, const char* what) {
 
 int ensure(sdim_ctx* ctx, DevBuf& b, size_t bytes) {
   if (bytes <= b.cap) return SDIM_OK;
+  // grow geometrically: a reallocation (cudaFree) waits for the device
+  size_t cap = std::max(std::max(bytes, (size_t)256), b.cap + b.cap / 2);
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.cap = 0;
-  size_t cap = std::max(bytes, (size_t)256);
   cudaError_t e = cudaMalloc(&b.p, cap);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -232,6 +236,7 @@ int job_variant(const sdim_circuit* c, unsigned flags) {
 int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned flags) {
   const bool plain = flags & SDIM_FLAG_PLAIN;
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
+  ctx->last_stream = s;
   int rc;
   if ((rc = ensure(ctx, ctx->status, sizeof(int))) != SDIM_OK) return rc;
   if ((rc = ensure(ctx, ctx->counters, sizeof(unsigned long long) * V_COUNT)) != SDIM_OK) return rc;
@@ -322,6 +327,77 @@ __global__ void __launch_bounds__(1024) k_smem_probe(int iters, uint4* sink) {
   if ((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9e3779b9u) sink[blockIdx.x] = acc;
 }
 
+// Op-table rows (gate id, qudit, target, channel) -> device instruction
+// words appended to dev (sdim/program.py:13-32 dispatch table, with CZ /
+// CZ_INV / SWAP / M_X expanded as sdim/tableau/tableau_gates.py:229-329 does).
+int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* noise_prob, int n, int d,
+                std::vector<uint2>& dev, int& nmeas) {
+  if (n < 1) return fail(ctx, SDIM_EINVAL, "Number of qudits must be greater than 0");
+  if (d < 2) return fail(ctx, SDIM_EINVAL, "Dimension must be greater than 1");
+  if (!is_prime(d)) return fail(ctx, SDIM_EUNSUPPORTED, "composite dimension: only prime d has a tableau path here");
+  if (d > 127) return fail(ctx, SDIM_EUNSUPPORTED, "dimension above 127 is not supported");
+  if (n > (1 << 20)) return fail(ctx, SDIM_EINVAL, "too many qudits");
+  dev.reserve(dev.size() + (size_t)nops + 8);
+  nmeas = 0;
+  auto emit = [&](uint32_t op, int q, uint32_t y) { dev.push_back(make_uint2(op | ((uint32_t)q << 8), y)); };
+  for (int64_t i = 0; i < nops; ++i) {
+    const int id = ops[4 * i], q = ops[4 * i + 1], t = ops[4 * i + 2], ch = ops[4 * i + 3];
+    if (id < 0 || id > 17) return fail(ctx, SDIM_EINVAL, "Invalid gate value " + std::to_string(id));
+    if (q < 0 || q >= n)
+      return fail(ctx, SDIM_EINVAL, "qudit index " + std::to_string(q) + " out of range at instruction " +
+                                        std::to_string(i));
+    const bool two = id >= 9 && id <= 13;
+    if (two && (t < 0 || t >= n))
+      return fail(ctx, SDIM_EINVAL, "target index " + std::to_string(t) + " out of range at instruction " +
+                                        std::to_string(i));
+    switch (id) {
+      case 0: emit(OP_NOP, q, 0); break;
+      case 1: emit(OP_X, q, 0); break;
+      case 2: emit(OP_X_INV, q, 0); break;
+      case 3: emit(OP_Z, q, 0); break;
+      case 4: emit(OP_Z_INV, q, 0); break;
+      case 5: emit(OP_H, q, 0); break;
+      case 6: emit(OP_H_INV, q, 0); break;
+      case 7: emit(OP_P, q, 0); break;
+      case 8: emit(OP_P_INV, q, 0); break;
+      case 9: emit(OP_CNOT, q, t); break;
+      case 10: emit(OP_CNOT_INV, q, t); break;
+      case 11:  // CZ = H_INV(t) CNOT(c,t) H(t)   (tableau_gates.py:229-244)
+        emit(OP_H_INV, t, 0); emit(OP_CNOT, q, t); emit(OP_H, t, 0);
+        break;
+      case 12:  // CZ_INV = H_INV(t) CNOT_INV(c,t) H(t)   (tableau_gates.py:246-261)
+        emit(OP_H_INV, t, 0); emit(OP_CNOT_INV, q, t); emit(OP_H, t, 0);
+        break;
+      case 13:  // SWAP, prime-d sequence (tableau_gates.py:320-328)
+        emit(OP_CNOT, q, t); emit(OP_H, q, 0); emit(OP_H, t, 0);
+        emit(OP_CNOT, q, t); emit(OP_H, q, 0); emit(OP_H, t, 0);
+        emit(OP_CNOT, q, t); emit(OP_H, t, 0); emit(OP_H, t, 0);
+        break;
+      case 14: emit(OP_M, q, 0); ++nmeas; break;
+      case 15:  // M_X = H_INV then measure (tableau_gates.py:280-296)
+        emit(OP_H_INV, q, 0); emit(OP_M, q, 0); ++nmeas;
+        break;
+      case 16: emit(OP_RESET, q, 0); ++nmeas; break;
+      case 17: {
+        const double p = noise_prob ? noise_prob[i] : 0.01;
+        if (!(p == p)) return fail(ctx, SDIM_EINVAL, "noise probability is NaN");
+        if (ch < 1 || ch > 3) return fail(ctx, SDIM_EINVAL, "Must specify a valid noise channel.");
+        const double thr = std::floor((1.0 - p) * 4294967296.0);
+        if (thr >= 4294967296.0) {
+          emit(OP_N1OFF, q, 0);
+        } else {
+          const uint32_t th = thr <= 0.0 ? 0u : (uint32_t)thr;
+          emit(ch == 1 ? OP_N1D : ch == 2 ? OP_N1F : OP_N1P, q, th);
+        }
+        break;
+      }
+    }
+    dev.back().x |= kOpEnd;
+  }
+  if (dev.size() > (size_t)0x7fffffff) return fail(ctx, SDIM_EINVAL, "program too long");
+  return SDIM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -379,9 +455,10 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   if (!ctx) return SDIM_EINVAL;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap};
+  DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
+  if (ctx->staging) cudaFreeHost(ctx->staging);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   cudaStreamDestroy(ctx->stream);
@@ -400,74 +477,34 @@ int sdim_device_info(sdim_ctx* ctx, int64_t info[4]) {
   return SDIM_OK;
 }
 
+int sdim_memory_info(sdim_ctx* ctx, int64_t info[3]) {
+  if (!ctx || !info) return SDIM_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  info[0] = (int64_t)free_b;
+  info[1] = (int64_t)total_b;
+  info[2] = (int64_t)(ctx->descs.cap + ctx->counters.cap + ctx->status.cap + ctx->gslots.cap + ctx->out.cap +
+                      ctx->snap.cap);
+  return SDIM_OK;
+}
+
+int sdim_program_bytes(const sdim_circuit* c, int64_t nshots, int64_t out[2]) {
+  if (!c || !out || nshots < 0) return SDIM_EINVAL;
+  const VariantOps& g = variant_ops(c->gvariant);
+  out[0] = (int64_t)nshots * c->nmeas;                   // records
+  out[1] = (int64_t)(g.hot_bytes(c->n) + g.big_bytes(c->n));  // one group slot
+  return SDIM_OK;
+}
+
 int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* noise_prob, int n, int d,
                         sdim_circuit** out) {
   if (!ctx || !out || (nops > 0 && !ops) || nops < 0) return fail(ctx, SDIM_EINVAL, "null argument");
   *out = nullptr;
-  if (n < 1) return fail(ctx, SDIM_EINVAL, "Number of qudits must be greater than 0");
-  if (d < 2) return fail(ctx, SDIM_EINVAL, "Dimension must be greater than 1");
-  if (!is_prime(d)) return fail(ctx, SDIM_EUNSUPPORTED, "composite dimension: only prime d has a tableau path here");
-  if (d > 127) return fail(ctx, SDIM_EUNSUPPORTED, "dimension above 127 is not supported");
-  if (n > (1 << 20)) return fail(ctx, SDIM_EINVAL, "too many qudits");
   std::vector<uint2> dev;
-  dev.reserve((size_t)nops + 8);
   int nmeas = 0;
-  auto emit = [&](uint32_t op, int q, uint32_t y) { dev.push_back(make_uint2(op | ((uint32_t)q << 8), y)); };
-  for (int64_t i = 0; i < nops; ++i) {
-    const int id = ops[4 * i], q = ops[4 * i + 1], t = ops[4 * i + 2], ch = ops[4 * i + 3];
-    if (id < 0 || id > 17) return fail(ctx, SDIM_EINVAL, "Invalid gate value " + std::to_string(id));
-    if (q < 0 || q >= n)
-      return fail(ctx, SDIM_EINVAL, "qudit index " + std::to_string(q) + " out of range at instruction " +
-                                        std::to_string(i));
-    const bool two = id >= 9 && id <= 13;
-    if (two && (t < 0 || t >= n))
-      return fail(ctx, SDIM_EINVAL, "target index " + std::to_string(t) + " out of range at instruction " +
-                                        std::to_string(i));
-    switch (id) {
-      case 0: emit(OP_NOP, q, 0); break;
-      case 1: emit(OP_X, q, 0); break;
-      case 2: emit(OP_X_INV, q, 0); break;
-      case 3: emit(OP_Z, q, 0); break;
-      case 4: emit(OP_Z_INV, q, 0); break;
-      case 5: emit(OP_H, q, 0); break;
-      case 6: emit(OP_H_INV, q, 0); break;
-      case 7: emit(OP_P, q, 0); break;
-      case 8: emit(OP_P_INV, q, 0); break;
-      case 9: emit(OP_CNOT, q, t); break;
-      case 10: emit(OP_CNOT_INV, q, t); break;
-      case 11:  // CZ = H_INV(t) CNOT(c,t) H(t)   (tableau_gates.py:229-244)
-        emit(OP_H_INV, t, 0); emit(OP_CNOT, q, t); emit(OP_H, t, 0);
-        break;
-      case 12:  // CZ_INV = H_INV(t) CNOT_INV(c,t) H(t)   (tableau_gates.py:246-261)
-        emit(OP_H_INV, t, 0); emit(OP_CNOT_INV, q, t); emit(OP_H, t, 0);
-        break;
-      case 13:  // SWAP, prime-d sequence (tableau_gates.py:320-328)
-        emit(OP_CNOT, q, t); emit(OP_H, q, 0); emit(OP_H, t, 0);
-        emit(OP_CNOT, q, t); emit(OP_H, q, 0); emit(OP_H, t, 0);
-        emit(OP_CNOT, q, t); emit(OP_H, t, 0); emit(OP_H, t, 0);
-        break;
-      case 14: emit(OP_M, q, 0); ++nmeas; break;
-      case 15:  // M_X = H_INV then measure (tableau_gates.py:280-296)
-        emit(OP_H_INV, q, 0); emit(OP_M, q, 0); ++nmeas;
-        break;
-      case 16: emit(OP_RESET, q, 0); ++nmeas; break;
-      case 17: {
-        const double p = noise_prob ? noise_prob[i] : 0.01;
-        if (!(p == p)) return fail(ctx, SDIM_EINVAL, "noise probability is NaN");
-        if (ch < 1 || ch > 3) return fail(ctx, SDIM_EINVAL, "Must specify a valid noise channel.");
-        const double thr = std::floor((1.0 - p) * 4294967296.0);
-        if (thr >= 4294967296.0) {
-          emit(OP_N1OFF, q, 0);
-        } else {
-          const uint32_t th = thr <= 0.0 ? 0u : (uint32_t)thr;
-          emit(ch == 1 ? OP_N1D : ch == 2 ? OP_N1F : OP_N1P, q, th);
-        }
-        break;
-      }
-    }
-    dev.back().x |= kOpEnd;
-  }
-  if (dev.size() > (size_t)0x7fffffff) return fail(ctx, SDIM_EINVAL, "program too long");
+  const int rc = encode_rows(ctx, ops, nops, noise_prob, n, d, dev, nmeas);
+  if (rc != SDIM_OK) return rc;
   cudaSetDevice(ctx->device);
   sdim_circuit* c = new sdim_circuit();
   c->device = ctx->device;
@@ -603,6 +640,11 @@ int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, c
     const size_t b = (size_t)nshots[i] * circs[i]->nmeas;
     if (b) CK(cudaMemcpyAsync(outs[i], static_cast<uint8_t*>(ctx->out.p) + offs[i], b, cudaMemcpyDeviceToHost, s));
   }
+  if (flags & SDIM_FLAG_ASYNC) {
+    // the caller keeps the (pinned) host buffers alive until sdim_query / sdim_sync
+    ctx->last_stream = s;
+    return SDIM_OK;
+  }
   CK(cudaStreamSynchronize(s));
   if (ctx->timing_pending) {
     float ms = 0.f;
@@ -613,10 +655,124 @@ int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, c
   return read_status(ctx);
 }
 
+int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t* row_begin,
+                    const double* noise_prob, const int32_t* n, const int32_t* d, const uint64_t* seeds,
+                    const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs, void* stream,
+                    unsigned flags) {
+  if (!ctx || ncirc < 0 || (ncirc > 0 && (!rows || !row_begin || !n || !d || !seeds || !shot0 || !nshots || !outs)))
+    return fail(ctx, SDIM_EINVAL, "bad argument to sdim_run_tables");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  std::vector<uint2> dev;
+  std::vector<size_t> op_off(ncirc);
+  std::vector<sdim_circuit> circs(ncirc);
+  int rc;
+  for (int i = 0; i < ncirc; ++i) {
+    op_off[i] = dev.size();
+    int nmeas = 0;
+    const int64_t r0 = row_begin[i], r1 = row_begin[i + 1];
+    if (r1 < r0) return fail(ctx, SDIM_EINVAL, "row offsets must not decrease");
+    rc = encode_rows(ctx, rows + 4 * r0, r1 - r0, noise_prob ? noise_prob + r0 : nullptr, n[i], d[i], dev, nmeas);
+    if (rc != SDIM_OK) return rc;
+    sdim_circuit& c = circs[i];
+    c.device = ctx->device;
+    c.n = n[i];
+    c.d = d[i];
+    c.nmeas = nmeas;
+    c.nops_user = r1 - r0;
+    c.nops = (int)(dev.size() - op_off[i]);
+    c.variant = variant_for(d[i]);
+    c.gvariant = group_variant_for(d[i], n[i], 0);
+    c.gblock = variant_ops(c.gvariant).cta ? cta_block_for(n[i]) : 32;
+  }
+  // instruction streams: pinned staging -> device arena, both owned by the context
+  const size_t ob = std::max<size_t>(dev.size(), 1) * sizeof(uint2);
+  if ((rc = ensure(ctx, ctx->arena, ob)) != SDIM_OK) return rc;
+  if (ctx->staging_cap < ob) {
+    const size_t cap = std::max(ob, ctx->staging_cap + ctx->staging_cap / 2);
+    if (ctx->staging) cudaFreeHost(ctx->staging);
+    ctx->staging = nullptr;
+    ctx->staging_cap = 0;
+    if (cudaMallocHost(&ctx->staging, cap) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, SDIM_ENOMEM, "pinned staging allocation failed");
+    }
+    ctx->staging_cap = cap;
+  }
+  if (!dev.empty()) std::memcpy(ctx->staging, dev.data(), dev.size() * sizeof(uint2));
+  CK(cudaMemcpyAsync(ctx->arena.p, ctx->staging, dev.size() * sizeof(uint2), cudaMemcpyHostToDevice, s));
+  uint2* base = static_cast<uint2*>(ctx->arena.p);
+  for (int i = 0; i < ncirc; ++i) circs[i].d_ops = base + op_off[i];
+  const bool on_dev = flags & SDIM_FLAG_OUT_DEVICE;
+  std::vector<size_t> offs(ncirc);
+  size_t total = 0;
+  for (int i = 0; i < ncirc; ++i) {
+    if (nshots[i] < 0 || nshots[i] > 0x7fffffffLL)
+      return fail(ctx, SDIM_EINVAL, "bad shot count at index " + std::to_string(i));
+    if (nshots[i] > 0 && circs[i].nmeas > 0 && !outs[i])
+      return fail(ctx, SDIM_EINVAL, "null output at index " + std::to_string(i));
+    offs[i] = total;
+    total += (size_t)nshots[i] * circs[i].nmeas;
+  }
+  if (!on_dev && (rc = ensure(ctx, ctx->out, std::max<size_t>(total, 1))) != SDIM_OK) return rc;
+  std::vector<Job> jobs;
+  jobs.reserve(ncirc);
+  for (int i = 0; i < ncirc; ++i)
+    jobs.push_back(Job{&circs[i], seeds[i], shot0[i], nshots[i],
+                       on_dev ? outs[i] : static_cast<uint8_t*>(ctx->out.p) + offs[i]});
+  rc = launch_jobs(ctx, jobs, s, flags);
+  if (rc != SDIM_OK) return rc;
+  if (on_dev) return finish(ctx, s, flags);
+  if (flags & SDIM_FLAG_TIME) {
+    CK(cudaEventRecord(ctx->ev1, s));
+    ctx->timing_pending = true;
+  }
+  for (int i = 0; i < ncirc; ++i) {
+    const size_t b = (size_t)nshots[i] * circs[i].nmeas;
+    if (b) CK(cudaMemcpyAsync(outs[i], static_cast<uint8_t*>(ctx->out.p) + offs[i], b, cudaMemcpyDeviceToHost, s));
+  }
+  if (flags & SDIM_FLAG_ASYNC) return SDIM_OK;
+  CK(cudaStreamSynchronize(s));
+  if (ctx->timing_pending) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->last_ms = ms;
+    ctx->timing_pending = false;
+  }
+  return read_status(ctx);
+}
+
+int sdim_query(sdim_ctx* ctx) {
+  if (!ctx) return SDIM_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  const cudaError_t e = cudaStreamQuery(ctx->last_stream ? ctx->last_stream : ctx->stream);
+  if (e == cudaErrorNotReady) return 0;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamQuery");
+  return 1;
+}
+
+int sdim_host_alloc(size_t bytes, void** out) {
+  if (!out) return SDIM_EINVAL;
+  *out = nullptr;
+  if (cudaMallocHost(out, std::max<size_t>(bytes, 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return SDIM_ENOMEM;
+  }
+  return SDIM_OK;
+}
+
+int sdim_host_free(void* p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) {
+    cudaGetLastError();
+    return SDIM_ECUDA;
+  }
+  return SDIM_OK;
+}
+
 int sdim_sync(sdim_ctx* ctx) {
   if (!ctx) return SDIM_EINVAL;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaDeviceSynchronize());
+  CK(cudaStreamSynchronize(ctx->last_stream ? ctx->last_stream : ctx->stream));
   if (ctx->timing_pending) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));

@@ -90,6 +90,27 @@ def encode_program(circuits: Sequence, n: int, d: int, noise: bool = True) -> En
     return EncodedProgram(n, d, ops, np.asarray(probs, dtype=np.float64), mq, mr, counts)
 
 
+def encode_table(table: np.ndarray, n: int, d: int, probs: np.ndarray = None) -> EncodedProgram:
+    """EncodedProgram straight from an op table (rows gate id, qudit, target,
+    channel) -- the path for callers that generate programs as arrays."""
+    ops = np.ascontiguousarray(table, dtype=np.int32).reshape(-1, 4)
+    if probs is None:
+        probs = np.zeros(ops.shape[0], dtype=np.float64)
+    meas = np.isin(ops[:, 0], (14, 15, 16))
+    mq = ops[meas, 1].astype(np.int64)
+    # round of each record: how many earlier records the same qudit has
+    order = np.argsort(mq, kind="stable")
+    sq = mq[order]
+    starts = np.r_[0, np.flatnonzero(np.diff(sq)) + 1]
+    counts = np.diff(np.r_[starts, len(sq)])
+    rr = np.arange(len(sq)) - np.repeat(starts, counts)
+    mr = np.empty_like(mq)
+    mr[order] = rr
+    gids, cnt = np.unique(ops[:, 0], return_counts=True)
+    return EncodedProgram(int(n), int(d), ops, np.ascontiguousarray(probs, dtype=np.float64), mq, mr,
+                          {int(g): int(c) for g, c in zip(gids, cnt)})
+
+
 class DeviceProgram:
     """An encoded program resident on the device (``sdim_circuit``)."""
 

@@ -34,8 +34,30 @@ Op = Tuple[str, int, Optional[int], dict]
 class CircuitSpec:
     num_qudits: int
     dimension: int
-    ops: List[Op] = field(default_factory=list)
+    ops_list: Optional[List[Op]] = None
     name: str = ""
+    table: Optional[np.ndarray] = None  # int32 op table, when generated as arrays
+
+    @property
+    def ops(self) -> List[Op]:
+        if self.ops_list is None:
+            self.ops_list = table_to_ops(self.table) if self.table is not None else []
+        return self.ops_list
+
+    def op_table(self) -> np.ndarray:
+        """int32 rows (gate id, qudit, target, channel); N1 probabilities are
+        not part of the table (tables are only generated for N1-free programs)."""
+        if self.table is None:
+            from .gatedata import GateData
+            gd = GateData(self.dimension)
+            rows = []
+            for name, q, t, params in self.ops:
+                gid = gd.get_gate_id(gd.aliasMap.get(name.upper(), name.upper()))
+                if gid == 17:
+                    raise ValueError("op_table() holds no noise parameters; build a Circuit instead")
+                rows.append((gid, q, -1 if t is None else t, 0))
+            self.table = np.asarray(rows, dtype=np.int32).reshape(-1, 4)
+        return self.table
 
     def build(self, circuit_cls=None):
         """Circuit object with every op added through ``add_gate``."""
@@ -75,31 +97,55 @@ def _pair(rng: np.random.Generator, n: int) -> Tuple[int, int]:
     return c, t
 
 
-def random_hpc(n: int, d: int, num_gates: int, seed=0, weights=(1 / 3, 1 / 3, 1 / 3),
-               mr_every: int = 0, mr_fraction: float = 0.0, final_measure: bool = True,
-               name: str = "") -> CircuitSpec:
-    """Random {H, P, CNOT} circuit, optional periodic MEASURE+RESET, final MEASURE."""
+_GID_NAME = {5: "H", 7: "P", 9: "CNOT", 14: "M", 16: "RESET"}
+
+
+def random_hpc_table(n: int, num_gates: int, seed=0, weights=(1 / 3, 1 / 3, 1 / 3), mr_every: int = 0,
+                     mr_fraction: float = 0.0, final_measure: bool = True) -> np.ndarray:
+    """Op table (int32 rows gate id, qudit, target, channel) of a random
+    {H, P, CNOT} circuit: kinds drawn with ``weights``, single-qudit targets
+    uniform, CNOT on a uniform ordered pair of distinct qudits; MEASURE+RESET
+    on a uniformly random ``mr_fraction`` of the qudits after every
+    ``mr_every`` gates; MEASURE on all qudits at the end."""
     rng = _rng(seed)
-    ops: List[Op] = []
     cum = np.cumsum(np.asarray(weights, dtype=np.float64))
     cum /= cum[-1]
     kinds = np.searchsorted(cum, rng.random(num_gates), side="right")
+    q = rng.integers(n, size=num_gates)
+    t = rng.integers(max(n - 1, 1), size=num_gates)
+    t = t + (t >= q)
+    if n < 2:
+        kinds[kinds == 2] = 1
+    gid = np.where(kinds == 0, 5, np.where(kinds == 1, 7, 9))
+    gates = np.stack([gid, q, np.where(gid == 9, t, -1), np.zeros_like(gid)], axis=1).astype(np.int32)
     mr_count = int(round(mr_fraction * n)) if mr_every else 0
-    for g in range(num_gates):
-        k = int(kinds[g])
-        if k == 2 and n >= 2:
-            c, t = _pair(rng, n)
-            ops.append(("CNOT", c, t, {}))
-        else:
-            q = int(rng.integers(n))
-            ops.append(("H" if k == 0 else "P", q, None, {}))
-        if mr_every and (g + 1) % mr_every == 0 and mr_count > 0:
-            for q in sorted(int(v) for v in rng.choice(n, size=mr_count, replace=False)):
-                ops.append(("RESET", q, None, {}))
+    parts = []
+    if mr_every and mr_count > 0:
+        for start in range(0, num_gates, mr_every):
+            stop = min(start + mr_every, num_gates)
+            parts.append(gates[start:stop])
+            if stop - start == mr_every:
+                sel = np.sort(rng.choice(n, size=mr_count, replace=False))
+                parts.append(np.stack([np.full(mr_count, 16), sel, np.full(mr_count, -1), np.zeros(mr_count)],
+                                      axis=1).astype(np.int32))
+    else:
+        parts.append(gates)
     if final_measure:
-        for q in range(n):
-            ops.append(("M", q, None, {}))
-    return CircuitSpec(n, d, ops, name)
+        parts.append(np.stack([np.full(n, 14), np.arange(n), np.full(n, -1), np.zeros(n)], axis=1).astype(np.int32))
+    return np.concatenate(parts, axis=0) if parts else np.zeros((0, 4), np.int32)
+
+
+def table_to_ops(table: np.ndarray) -> List[Op]:
+    return [(_GID_NAME[g], q, None if t < 0 else t, {}) for g, q, t, _ in table.tolist()]
+
+
+def random_hpc(n: int, d: int, num_gates: int, seed=0, weights=(1 / 3, 1 / 3, 1 / 3),
+               mr_every: int = 0, mr_fraction: float = 0.0, final_measure: bool = True,
+               name: str = "") -> CircuitSpec:
+    """Random {H, P, CNOT} circuit, optional periodic MEASURE+RESET, final
+    MEASURE (the spec of :func:`random_hpc_table`)."""
+    table = random_hpc_table(n, num_gates, seed, weights, mr_every, mr_fraction, final_measure)
+    return CircuitSpec(n, d, None, name, table)
 
 
 def pr1(seed: int = 0) -> CircuitSpec:

@@ -82,8 +82,8 @@ def test_oracle_plants_detected():
     s = pr1(0)
     base = oracle_run([s], 0, 0, 16)["records"]
     ops = list(s.ops)
-    ops[10] = ("P" if ops[10][0] == "H" else "H", ops[10][1], None, {}) if ops[10][0] != "CNOT" else ops[10]
-    ops[11] = ("P" if ops[11][0] == "H" else "H", ops[11][1], None, {}) if ops[11][0] != "CNOT" else ops[11]
+    k = next(i for i, o in enumerate(ops) if o[0] == "H")
+    ops[k] = ("P", ops[k][1], None, {})
     s2 = type(s)(s.num_qudits, s.dimension, ops, "planted")
     other = oracle_run([s2], 0, 0, 16)["records"]
     assert not np.array_equal(base, other)
