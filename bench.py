@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-shots", type=int, default=256)
+    ap.add_argument("--engine", default="auto", choices=["auto", "trace", "group", "per_shot"],
+                    help="batched engine of the timed run (auto: the library's choice)")
     return ap.parse_args()
 
 
@@ -339,6 +341,7 @@ class Timer:
     def run(self, steps, step_fn, clocks=None):
         torch = self.torch
         step_ms, kern_ms = [], []
+        self.stage_ms = []
         if self.ws > 1:
             self.dist.barrier()
         torch.cuda.synchronize()
@@ -353,6 +356,7 @@ class Timer:
             self.ctx.sync()
             step_ms.append(e0.elapsed_time(e1))
             kern_ms.append(self.ctx.last_kernel_ms())
+            self.stage_ms.append(self.ctx.last_stage_ms())
         torch.cuda.synchronize()
         return step_ms, kern_ms, (clocks.stop() if clocks else None)
 
@@ -380,9 +384,11 @@ def run_single(args, torch, dist, ws, rank, local):
     torch.cuda.set_stream(stream)
     timer = Timer(torch, stream, ctx, ws, dist)
 
-    def step(extra=0):
+    engine_flags = _lib.engine_flags(None if args.engine == "auto" else args.engine)
+
+    def step(extra=None):
         rc = ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 0, shot0, shots, out.data_ptr(), stream.cuda_stream,
-                                     _lib.FLAG_ASYNC | _lib.FLAG_TIME | extra)
+                                     _lib.FLAG_ASYNC | _lib.FLAG_TIME | (engine_flags if extra is None else extra))
         _lib.check(rc, ctx.ptr, "run")
 
     # per-shot engine (one warp, one full tableau per shot) on the same inputs
@@ -396,13 +402,29 @@ def run_single(args, torch, dist, ws, rank, local):
         step()
     ctx.sync()
     step_ms, kern_ms, clk = timer.run(args.steps, step, Clocks(local))
+    stages = [statistics.mean(v) for v in zip(*timer.stage_ms)]
     total_ms = timer.max_over_ranks(sum(step_ms))
     units_per_step = len(spec.ops) * shots
     value = units_per_step * ws * args.steps / (total_ms / 1e3)
 
     rec = out[:64, :nrec].cpu().numpy()
     if not np.array_equal(rec, ps_records):
-        raise AssertionError("shot-group and per-shot engines disagree")
+        raise AssertionError("batched and per-shot engines disagree")
+    full = out[:, :nrec].cpu().numpy()
+    engines = {}
+    if d == 2:
+        # the shot-group engine on the same inputs, for comparison
+        for name, fl in (("group", _lib.FLAG_NO_TRACE), ("trace", _lib.FLAG_TRACE)):
+            step(fl)
+            ctx.sync()
+            g_ms, g_kern, _ = timer.run(2, lambda: step(fl))
+            if not np.array_equal(out[:, :nrec].cpu().numpy(), full):
+                raise AssertionError(f"{name} engine disagrees with the timed run")
+            engines[name] = {"value": units_per_step * 2 / (sum(g_ms) / 1e3), "unit": UNIT,
+                             "kernel_ms": statistics.mean(g_kern),
+                             "stages_ms": [statistics.mean(v) for v in zip(*timer.stage_ms)]}
+        step()
+        ctx.sync()
     det_row = (rec[0] >> 7).astype(bool) if nrec else np.zeros(0, bool)
     assert np.all((rec >> 7) == (rec[0] >> 7)), "deterministic flags differ across shots"
     meas_ids = [g for g in enc.ops[:, 0].tolist() if g in (14, 15, 16)]
@@ -489,6 +511,9 @@ def run_single(args, torch, dist, ws, rank, local):
         "cpu_baseline": cpu,
         "gpu_launches": args.steps,
         "clocks": clk,
+        "engine": args.engine,
+        "stages_ms": {"xz_pass": stages[0], "phase_pass": stages[1], "other_engines": stages[2]},
+        "engines": engines,
     }
 
 

@@ -46,6 +46,9 @@ extern "C" {
 #define SDIM_FLAG_PER_SHOT 32u   /* batched runs use one warp per shot instead of the shot-group engine */
 #define SDIM_FLAG_TEAM_WARP 64u  /* shot groups on one warp each, whatever n */
 #define SDIM_FLAG_TEAM_CTA 128u  /* shot groups on one CTA each, whatever n */
+#define SDIM_FLAG_TRACE 256u     /* d = 2: trace engine (one x / z pass per program, one lane per shot)
+                                    whatever the shot count; by default it runs from 64 shots */
+#define SDIM_FLAG_NO_TRACE 512u  /* d = 2: shot-group engine only */
 
 /* snapshot modes for sdim_snapshot */
 #define SDIM_SNAP_EVERY_INSTRUCTION 1
@@ -67,7 +70,8 @@ int sdim_device_info(sdim_ctx* ctx, int64_t info[4]);
  * context holds in its buffers.  Used by the serving loop's admission. */
 int sdim_memory_info(sdim_ctx* ctx, int64_t info[3]);
 /* Device bytes a run of nshots shots of circ needs: out[0] records,
- * out[1] one shot-group slot (shared-memory part plus x / z part). */
+ * out[1] one shot-group slot (shared-memory part plus x / z part) plus,
+ * for d = 2, the trace the trace engine writes. */
 int sdim_program_bytes(const sdim_circuit* circ, int64_t nshots, int64_t out[2]);
 
 /* Encodes one program.  ops is nops rows of 4 int32:
@@ -134,6 +138,10 @@ int sdim_host_alloc(size_t bytes, void** out);
 int sdim_host_free(void* p);
 /* Milliseconds of the kernels of the last call made with SDIM_FLAG_TIME. */
 double sdim_last_kernel_ms(const sdim_ctx* ctx);
+/* The same span split by stage: out[0] the trace engine's x / z passes,
+ * out[1] its phase passes, out[2] every other engine's kernels.  No
+ * counterpart in the reference (its shot loop is not staged). */
+int sdim_last_stage_ms(const sdim_ctx* ctx, double out[3]);
 
 /* Tableau export of one shot in the reference's int8 block order
  * x[n][n], z[n][n], phase[n], destab_x[n][n], destab_z[n][n], destab_phase[n]

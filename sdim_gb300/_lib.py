@@ -26,6 +26,18 @@ FLAG_FORCE_GMEM = 16
 FLAG_PER_SHOT = 32
 FLAG_TEAM_WARP = 64
 FLAG_TEAM_CTA = 128
+FLAG_TRACE = 256
+FLAG_NO_TRACE = 512
+
+
+def engine_flags(engine) -> int:
+    """Run flags that select a batched engine by name (None: the library's
+    choice by shot count and dimension)."""
+    table = {None: 0, "auto": 0, "trace": FLAG_TRACE, "group": FLAG_NO_TRACE, "per_shot": FLAG_PER_SHOT,
+             "group_warp": FLAG_TEAM_WARP, "group_cta": FLAG_TEAM_CTA}
+    if engine not in table:
+        raise ValueError(f"unknown engine {engine!r}; expected one of {sorted(k for k in table if k)}")
+    return table[engine]
 
 SNAP_EVERY_INSTRUCTION = 1
 SNAP_AT_MEASUREMENT = 2
@@ -52,6 +64,7 @@ SIGNATURES = {
     "sdim_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "sdim_host_free": (C.c_int, [_P]),
     "sdim_last_kernel_ms": (C.c_double, [_P]),
+    "sdim_last_stage_ms": (C.c_int, [_P, _P]),
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_run_noalloc": (C.c_int, [_P, C.c_int64, _P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_int64, _P,
@@ -138,6 +151,12 @@ class Context:
 
     def last_kernel_ms(self) -> float:
         return float(self.lib.sdim_last_kernel_ms(self.ptr))
+
+    def last_stage_ms(self):
+        """(x / z passes, phase passes, other engines) of the last timed call."""
+        buf = (C.c_double * 3)()
+        check(self.lib.sdim_last_stage_ms(self.ptr, buf), self.ptr, "sdim_last_stage_ms")
+        return tuple(float(v) for v in buf)
 
     def sync(self):
         check(self.lib.sdim_sync(self.ptr), self.ptr, "sdim_sync")

@@ -54,14 +54,14 @@ class BatchRunner:
         return circs, seeds, shot0, nshots
 
     @staticmethod
-    def _flags(plain=False, per_shot=False, time_kernels=False, asynchronous=False, device=False):
+    def _flags(plain=False, per_shot=False, time_kernels=False, asynchronous=False, device=False, engine=None):
         return ((_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_PER_SHOT if per_shot else 0)
                 | (_lib.FLAG_TIME if time_kernels else 0) | (_lib.FLAG_ASYNC if asynchronous else 0)
-                | (_lib.FLAG_OUT_DEVICE if device else 0))
+                | (_lib.FLAG_OUT_DEVICE if device else 0) | _lib.engine_flags(engine))
 
     def run(self, plain: bool = False, per_shot: bool = False, time_kernels: bool = False,
             entries: Optional[Sequence[BatchEntry]] = None,
-            outs: Optional[Sequence[np.ndarray]] = None) -> List[np.ndarray]:
+            outs: Optional[Sequence[np.ndarray]] = None, engine: Optional[str] = None) -> List[np.ndarray]:
         """Runs every entry; returns one (shots, records) uint8 array each
         (into ``outs`` when given, e.g. views of a pinned buffer)."""
         entries = list(self.entries if entries is None else entries)
@@ -70,20 +70,20 @@ class BatchRunner:
         ptrs = (C.c_void_p * len(entries))(*[o.ctypes.data for o in outs])
         circs, seeds, shot0, nshots = self._arrays(entries)
         rc = self.ctx.lib.sdim_run_batch(self.ctx.ptr, len(entries), circs, seeds, shot0, nshots, ptrs, None,
-                                         self._flags(plain, per_shot, time_kernels))
+                                         self._flags(plain, per_shot, time_kernels, engine=engine))
         _lib.check(rc, self.ctx.ptr, "batch")
         return list(outs)
 
     def run_device(self, outs_dev: Sequence[int], stream: Optional[int] = None, plain: bool = False,
                    per_shot: bool = False, time_kernels: bool = False, asynchronous: bool = False,
-                   entries: Optional[Sequence[BatchEntry]] = None):
+                   entries: Optional[Sequence[BatchEntry]] = None, engine: Optional[str] = None):
         """Same with device output pointers (e.g. ``tensor.data_ptr()``)."""
         entries = list(self.entries if entries is None else entries)
         ptrs = (C.c_void_p * len(entries))(*[int(p) for p in outs_dev])
         circs, seeds, shot0, nshots = self._arrays(entries)
         rc = self.ctx.lib.sdim_run_batch(self.ctx.ptr, len(entries), circs, seeds, shot0, nshots, ptrs,
                                          C.c_void_p(stream) if stream else None,
-                                         self._flags(plain, per_shot, time_kernels, asynchronous, True))
+                                         self._flags(plain, per_shot, time_kernels, asynchronous, True, engine))
         _lib.check(rc, self.ctx.ptr, "batch")
 
     def total_shots(self) -> int:

@@ -10,6 +10,7 @@
 
 #include "../../include/sdim_gb300.h"
 #include "kernels.cuh"
+#include "trace.cuh"
 #include "variants.cuh"
 
 using namespace sdim;
@@ -33,25 +34,41 @@ struct sdim_ctx {
   int64_t gmem_bytes = 0;
   size_t gmem_slot_budget = (size_t)8 << 30;
   std::string err;
-  DevBuf descs, counters, status, gslots, out, snap, arena;
+  DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace;
   void* staging = nullptr;  // pinned host staging of sdim_run_tables
   size_t staging_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_xz = nullptr, ev_phase = nullptr;  // trace engine stage ends (SDIM_FLAG_TIME)
   bool timing_pending = false;
+  bool stages_recorded = false;  // ev_xz / ev_phase belong to the pending span
   double last_ms = 0.0;
+  double stage_ms[3] = {0.0, 0.0, 0.0};  // x / z passes, phase passes, other engines
   int smem_attr_set[V_COUNT] = {};
+  bool trace_smem_set = false;
+};
+
+// Where the trace schedule of a program sits in its blob (uint2 words).
+struct TraceSchedule {
+  int64_t steps_off = -1, lops_off = -1, wins_off = -1;
+  int nsteps = 0, nwins = 0;
 };
 
 struct sdim_circuit {
   int device = 0;
   int n = 0, d = 0, nmeas = 0;
+  int nn1 = 0;        // N1 instructions (noise ordinals)
   int64_t nops_user = 0;
   int nops = 0;
   int variant = 0;    // per-shot engine (plain form, per-shot snapshots)
   int gvariant = 0;   // shot-group engine for batched runs
   int gblock = 32;    // threads of one group team
-  uint2* h_ops = nullptr;  // pinned host copy
-  uint2* d_ops = nullptr;
+  uint2* h_ops = nullptr;  // pinned host copy of the blob: instruction words, then the trace schedule
+  uint2* d_ops = nullptr;  // device copy of the same blob
+  int64_t blob_words = 0;  // uint2 words of the blob
+  const uint4* d_steps = nullptr;  // trace schedule (d = 2, n <= 512), inside the blob
+  const uint4* d_lops = nullptr;
+  const uint4* d_wins = nullptr;
+  int nsteps = 0, nwins = 0;
 };
 
 namespace {
@@ -195,6 +212,26 @@ int read_status(sdim_ctx* ctx) {
   return fail(ctx, SDIM_EDEVICE, std::string("device reported: ") + why);
 }
 
+// Kernel times of the last SDIM_FLAG_TIME call: the whole span and its stages.
+int collect_times(sdim_ctx* ctx) {
+  float all = 0.f, a = 0.f, b = 0.f, c = 0.f;
+  CK(cudaEventElapsedTime(&all, ctx->ev0, ctx->ev1));
+  if (ctx->stages_recorded) {
+    CK(cudaEventElapsedTime(&a, ctx->ev0, ctx->ev_xz));
+    CK(cudaEventElapsedTime(&b, ctx->ev_xz, ctx->ev_phase));
+    CK(cudaEventElapsedTime(&c, ctx->ev_phase, ctx->ev1));
+  } else {
+    c = all;
+  }
+  ctx->stages_recorded = false;
+  ctx->last_ms = all;
+  ctx->stage_ms[0] = a;
+  ctx->stage_ms[1] = b;
+  ctx->stage_ms[2] = c;
+  ctx->timing_pending = false;
+  return SDIM_OK;
+}
+
 int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
   if (flags & SDIM_FLAG_TIME) {
     CK(cudaEventRecord(ctx->ev1, s));
@@ -205,10 +242,8 @@ int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
   if (flags & SDIM_FLAG_ASYNC) return SDIM_OK;
   CK(cudaStreamSynchronize(s));
   if (ctx->timing_pending) {
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->last_ms = ms;
-    ctx->timing_pending = false;
+    const int trc = collect_times(ctx);
+    if (trc != SDIM_OK) return trc;
   }
   return read_status(ctx);
 }
@@ -229,14 +264,146 @@ int job_variant(const sdim_circuit* c, unsigned flags) {
   return c->gvariant;
 }
 
+// Below this many shots a d = 2 program runs on the shot-group engine: one
+// x / z pass per program plus a phase pass only pays once there are several
+// 32-shot groups to share it.
+constexpr int64_t kTraceMinShots = 64;
+
+// Jobs for the trace engine: d = 2, batched form, trace rows of at most
+// kTraceMaxWords words (n <= 512) and kTraceMinShots shots, unless
+// SDIM_FLAG_TRACE (any shot count) or a flag that names another engine.
+bool use_trace(const Job& j, unsigned flags) {
+  if (flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT | SDIM_FLAG_TEAM_WARP | SDIM_FLAG_TEAM_CTA |
+               SDIM_FLAG_NO_TRACE))
+    return false;
+  if (j.c->d != 2 || trace_words(j.c->n) == 0 || !j.c->d_steps || j.nshots <= 0) return false;
+  return (flags & SDIM_FLAG_TRACE) || j.nshots >= kTraceMinShots;
+}
+
+// Trace-engine launches for jobs (all use_trace): the x / z pass of every
+// program (warp teams below kCtaTeamQudits qudits, CTA teams above), then one
+// phase pass per trace-row width.  Programs are ordered by n, which orders
+// both the team split and the row widths.
+int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsigned flags, int* status) {
+  const bool timed = flags & SDIM_FLAG_TIME;
+  if (jobs.empty()) {
+    if (timed) {
+      CK(cudaEventRecord(ctx->ev_xz, s));
+      CK(cudaEventRecord(ctx->ev_phase, s));
+      ctx->stages_recorded = true;
+    }
+    return SDIM_OK;
+  }
+  const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
+  int rc;
+  if (!ctx->trace_smem_set) {
+    const cudaError_t e = trace_set_smem(ctx->smem_optin);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFuncSetAttribute");
+    ctx->trace_smem_set = true;
+  }
+  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& b) { return a.c->n < b.c->n; });
+  const size_t k = jobs.size();
+  std::vector<size_t> off(k);
+  size_t total = 0;
+  for (size_t i = 0; i < k; ++i) {
+    off[i] = total;
+    total += trace_bytes(jobs[i].c->nmeas, jobs[i].c->nn1, trace_words(jobs[i].c->n));
+  }
+  if ((rc = ensure(ctx, ctx->trace, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
+  if ((rc = ensure(ctx, ctx->tdescs, sizeof(TraceDesc) * k)) != SDIM_OK) return rc;
+  std::vector<TraceDesc> hd(k);
+  long long groups = 0;
+  for (size_t i = 0; i < k; ++i) {
+    const Job& j = jobs[i];
+    const int tw = trace_words(j.c->n);
+    if (i > 0 && tw != trace_words(jobs[i - 1].c->n)) groups = 0;  // item numbers restart per phase launch
+    TraceDesc& td = hd[i];
+    std::memset(&td, 0, sizeof(td));
+    td.c.ops = j.c->d_ops;
+    td.c.out = j.out_dev;
+    td.c.seed = j.seed;
+    td.c.shot0 = j.shot0;
+    td.c.item_begin = groups;
+    td.c.nops = j.c->nops;
+    td.c.n = j.c->n;
+    td.c.d = j.c->d;
+    td.c.nmeas = j.c->nmeas;
+    td.c.nshots = (int)j.nshots;
+    groups += (j.nshots + 31) / 32;
+    uint8_t* b = static_cast<uint8_t*>(ctx->trace.p) + off[i];
+    size_t o[6];
+    trace_offsets(j.c->nmeas, j.c->nn1, tw, o);
+    td.steps = j.c->d_steps;
+    td.lops = j.c->d_lops;
+    td.wins = j.c->d_wins;
+    td.nsteps = j.c->nsteps;
+    td.nwins = j.c->nwins;
+    td.mhdr = reinterpret_cast<uint4*>(b + o[0]);
+    td.mrow = reinterpret_cast<uint32_t*>(b + o[1]);
+    td.nhdr = reinterpret_cast<uint2*>(b + o[2]);
+    td.nthr = reinterpret_cast<uint32_t*>(b + o[3]);
+    td.nrow = reinterpret_cast<uint32_t*>(b + o[4]);
+    td.nm = j.c->nmeas;
+    td.nn1 = j.c->nn1;
+    td.tw = tw;
+    td.wn = (j.c->n + 31) >> 5;
+  }
+  TraceDesc* dd = static_cast<TraceDesc*>(ctx->tdescs.p);
+  CK(cudaMemcpyAsync(dd, hd.data(), sizeof(TraceDesc) * k, cudaMemcpyHostToDevice, s));
+  // x / z pass: one CTA per program
+  {
+    const int nmax = jobs[k - 1].c->n;
+    const size_t hot = trace_pass_hot_bytes(nmax), xz = trace_pass_xz_bytes(nmax);
+    // after the tableau: the schedule window; about 3.2 KB of static shared memory besides
+    const size_t win = trace_pass_window_bytes();
+    const bool in_smem = !force_gmem && hot + xz + win + 4096 <= (size_t)ctx->smem_optin;
+    int grid = (int)std::min<size_t>(k, 65535);
+    if (!in_smem) {
+      grid = std::min(grid, 2 * ctx->num_sms);
+      if ((rc = ensure(ctx, ctx->gslots, xz * (size_t)grid)) != SDIM_OK) return rc;
+    }
+    launch_trace_pass(grid, hot + (in_smem ? xz : 0) + win, s, dd, (int)k, static_cast<uint8_t*>(ctx->gslots.p), xz,
+                      hot, in_smem ? 1 : 0, status);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
+  }
+  if (timed) CK(cudaEventRecord(ctx->ev_xz, s));
+  // phase passes, one per row width
+  for (size_t b = 0; b < k;) {
+    const int tw = hd[b].tw;
+    size_t e = b;
+    long long items = 0;
+    while (e < k && hd[e].tw == tw) {
+      items = hd[e].c.item_begin + (hd[e].c.nshots + 31) / 32;
+      ++e;
+    }
+    const int warps = 8;
+    const long long grid = (items + warps - 1) / warps;
+    if (grid > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one phase pass");
+    if (!launch_phase_pass(tw, (int)grid, 32 * warps, s, dd + b, (int)(e - b), items, status))
+      return fail(ctx, SDIM_EINVAL, "no phase pass for trace rows of " + std::to_string(tw) + " words");
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "phase pass launch");
+    b = e;
+  }
+  if (timed) {
+    CK(cudaEventRecord(ctx->ev_phase, s));
+    ctx->stages_recorded = true;
+  }
+  return SDIM_OK;
+}
+
 // Launches every job, grouped by engine variant: one persistent launch per
 // variant (or one single-warp launch per shot with SDIM_FLAG_PLAIN).  Work
 // items are shots for per-shot engines and 32-shot groups for group engines;
-// inside a variant the most expensive programs are queued first.
-int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned flags) {
+// inside a variant the most expensive programs are queued first.  d = 2 jobs
+// with enough shots go to the trace engine first (use_trace).
+int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsigned flags) {
   const bool plain = flags & SDIM_FLAG_PLAIN;
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
   ctx->last_stream = s;
+  std::vector<Job> jobs, tjobs;
+  for (const Job& j : all_jobs) (use_trace(j, flags) ? tjobs : jobs).push_back(j);
   int rc;
   if ((rc = ensure(ctx, ctx->status, sizeof(int))) != SDIM_OK) return rc;
   if ((rc = ensure(ctx, ctx->counters, sizeof(unsigned long long) * V_COUNT)) != SDIM_OK) return rc;
@@ -285,6 +452,7 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& jobs, cudaStream_t s, unsigned 
   CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * V_COUNT, s));
   if (flags & SDIM_FLAG_TIME) CK(cudaEventRecord(ctx->ev0, s));
   int* status = static_cast<int*>(ctx->status.p);
+  if ((rc = launch_trace_jobs(ctx, tjobs, s, flags, status)) != SDIM_OK) return rc;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const Group& g = groups[gi];
     if (g.items == 0) continue;
@@ -331,7 +499,7 @@ __global__ void __launch_bounds__(1024) k_smem_probe(int iters, uint4* sink) {
 // words appended to dev (sdim/program.py:13-32 dispatch table, with CZ /
 // CZ_INV / SWAP / M_X expanded as sdim/tableau/tableau_gates.py:229-329 does).
 int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* noise_prob, int n, int d,
-                std::vector<uint2>& dev, int& nmeas) {
+                std::vector<uint2>& dev, int& nmeas, int& nn1) {
   if (n < 1) return fail(ctx, SDIM_EINVAL, "Number of qudits must be greater than 0");
   if (d < 2) return fail(ctx, SDIM_EINVAL, "Dimension must be greater than 1");
   if (!is_prime(d)) return fail(ctx, SDIM_EUNSUPPORTED, "composite dimension: only prime d has a tableau path here");
@@ -339,6 +507,7 @@ int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* n
   if (n > (1 << 20)) return fail(ctx, SDIM_EINVAL, "too many qudits");
   dev.reserve(dev.size() + (size_t)nops + 8);
   nmeas = 0;
+  nn1 = 0;
   auto emit = [&](uint32_t op, int q, uint32_t y) { dev.push_back(make_uint2(op | ((uint32_t)q << 8), y)); };
   for (int64_t i = 0; i < nops; ++i) {
     const int id = ops[4 * i], q = ops[4 * i + 1], t = ops[4 * i + 2], ch = ops[4 * i + 3];
@@ -383,6 +552,7 @@ int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* n
         if (!(p == p)) return fail(ctx, SDIM_EINVAL, "noise probability is NaN");
         if (ch < 1 || ch > 3) return fail(ctx, SDIM_EINVAL, "Must specify a valid noise channel.");
         const double thr = std::floor((1.0 - p) * 4294967296.0);
+        ++nn1;
         if (thr >= 4294967296.0) {
           emit(OP_N1OFF, q, 0);
         } else {
@@ -396,6 +566,108 @@ int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* n
   }
   if (dev.size() > (size_t)0x7fffffff) return fail(ctx, SDIM_EINVAL, "program too long");
   return SDIM_OK;
+}
+
+// Layered schedule of a d = 2 program for the trace engine's x / z pass,
+// appended to dev after the instruction words (16-byte aligned):
+//   steps[s] = {kind, first, count, 0}: kind 0 is a gate layer -- ops on
+//     pairwise disjoint qudits with at most one P / P_INV, the only ops
+//     whose common-phase update is not a plain xor -- and kind 1 a block of
+//     consecutive M / RESET, with the N1 between them (an N1 only reads its
+//     rows, so it can wait for the measurements around it);
+//   lops[i] = {instruction word, y, ordinal (measurement index of M /
+//     RESET, noise ordinal of N1), N1 ordinals before it (M / RESET)};
+//   wins[i] = {first step, steps, first op, ops}: windows of at most
+//     kTraceWinSteps steps and kTraceWinOps ops that the pass stages in
+//     shared memory (a longer step is a window of its own, read in place).
+// Between two measurements only ops that share a qudit (or two P's) are
+// ordered, so each op goes one level after the last op it follows.
+void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int n, TraceSchedule& out) {
+  std::vector<uint4> steps, lops, wins;
+  std::vector<std::vector<uint4>> layers;
+  std::vector<int> last(n, -1), gen(n, -1);
+  int window = 0, last_p = -1;
+  bool in_block = false;
+  uint32_t mord = 0, nord = 0;
+  auto flush = [&]() {
+    for (auto& l : layers) {
+      steps.push_back(make_uint4(0u, (uint32_t)lops.size(), (uint32_t)l.size(), 0u));
+      lops.insert(lops.end(), l.begin(), l.end());
+    }
+    layers.clear();
+    ++window;
+    last_p = -1;
+  };
+  auto level = [&](int q) { return gen[q] == window ? last[q] : -1; };
+  for (size_t i = op_begin; i < op_begin + nops; ++i) {
+    const uint2 w = dev[i];
+    const uint32_t op = w.x & kOpMask;
+    const int q = (int)(w.x >> 8);
+    if (op == OP_NOP) continue;
+    const bool noise = op == OP_N1D || op == OP_N1F || op == OP_N1P || op == OP_N1OFF;
+    if (op == OP_M || op == OP_RESET) {
+      if (!layers.empty()) {
+        flush();
+        in_block = false;
+      }
+      if (!in_block) {
+        steps.push_back(make_uint4(1u, (uint32_t)lops.size(), 0u, 0u));
+        in_block = true;
+        ++window;
+      }
+      lops.push_back(make_uint4(w.x, w.y, mord++, nord));
+      ++steps.back().z;
+      continue;
+    }
+    if (noise && in_block) {
+      lops.push_back(make_uint4(w.x, w.y, nord++, 0u));
+      ++steps.back().z;
+      continue;
+    }
+    in_block = false;
+    const bool two = op == OP_CNOT || op == OP_CNOT_INV;
+    const bool is_p = op == OP_P || op == OP_P_INV;
+    int lv = level(q) + 1;
+    if (two) lv = std::max(lv, level((int)w.y) + 1);
+    if (is_p) lv = std::max(lv, last_p + 1);
+    if (lv == (int)layers.size()) layers.emplace_back();
+    layers[lv].push_back(make_uint4(w.x, w.y, noise ? nord++ : 0u, 0u));
+    last[q] = lv;
+    gen[q] = window;
+    if (two) {
+      last[w.y] = lv;
+      gen[w.y] = window;
+    }
+    if (is_p) last_p = lv;
+  }
+  if (!layers.empty()) flush();
+  for (size_t s = 0; s < steps.size();) {
+    if (steps[s].z > (uint32_t)kTraceWinOps) {
+      wins.push_back(make_uint4((uint32_t)s, 1u, steps[s].y, steps[s].z));
+      ++s;
+      continue;
+    }
+    size_t e = s;
+    uint32_t cnt = 0;
+    while (e < steps.size() && e - s < (size_t)kTraceWinSteps && cnt + steps[e].z <= (uint32_t)kTraceWinOps)
+      cnt += steps[e++].z;
+    wins.push_back(make_uint4((uint32_t)s, (uint32_t)(e - s), steps[s].y, cnt));
+    s = e;
+  }
+  if (dev.size() & 1) dev.push_back(make_uint2(0u, 0u));
+  auto put = [&](const std::vector<uint4>& v) {
+    const int64_t off = (int64_t)dev.size();
+    for (const uint4& x : v) {
+      dev.push_back(make_uint2(x.x, x.y));
+      dev.push_back(make_uint2(x.z, x.w));
+    }
+    return off;
+  };
+  out.steps_off = put(steps);
+  out.lops_off = put(lops);
+  out.wins_off = put(wins);
+  out.nsteps = (int)steps.size();
+  out.nwins = (int)wins.size();
 }
 
 }  // namespace
@@ -437,7 +709,8 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+      cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev_xz) != cudaSuccess || cudaEventCreate(&ctx->ev_phase) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return SDIM_ECUDA;
@@ -455,12 +728,15 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   if (!ctx) return SDIM_EINVAL;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena};
+  DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
+                    &ctx->tdescs, &ctx->trace};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
+  cudaEventDestroy(ctx->ev_xz);
+  cudaEventDestroy(ctx->ev_phase);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SDIM_OK;
@@ -494,6 +770,8 @@ int sdim_program_bytes(const sdim_circuit* c, int64_t nshots, int64_t out[2]) {
   const VariantOps& g = variant_ops(c->gvariant);
   out[0] = (int64_t)nshots * c->nmeas;                   // records
   out[1] = (int64_t)(g.hot_bytes(c->n) + g.big_bytes(c->n));  // one group slot
+  const int tw = c->d == 2 ? trace_words(c->n) : 0;
+  if (tw) out[1] += (int64_t)trace_bytes(c->nmeas, c->nn1, tw);
   return SDIM_OK;
 }
 
@@ -502,17 +780,22 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
   if (!ctx || !out || (nops > 0 && !ops) || nops < 0) return fail(ctx, SDIM_EINVAL, "null argument");
   *out = nullptr;
   std::vector<uint2> dev;
-  int nmeas = 0;
-  const int rc = encode_rows(ctx, ops, nops, noise_prob, n, d, dev, nmeas);
+  int nmeas = 0, nn1 = 0;
+  const int rc = encode_rows(ctx, ops, nops, noise_prob, n, d, dev, nmeas, nn1);
   if (rc != SDIM_OK) return rc;
+  const size_t ndev = dev.size();
+  TraceSchedule sch;
+  if (d == 2 && trace_words(n)) append_schedule(dev, 0, ndev, n, sch);
   cudaSetDevice(ctx->device);
   sdim_circuit* c = new sdim_circuit();
   c->device = ctx->device;
   c->n = n;
   c->d = d;
   c->nmeas = nmeas;
+  c->nn1 = nn1;
   c->nops_user = nops;
-  c->nops = (int)dev.size();
+  c->nops = (int)ndev;
+  c->blob_words = (int64_t)dev.size();
   c->variant = variant_for(d);
   c->gvariant = group_variant_for(d, n, 0);
   c->gblock = variant_ops(c->gvariant).cta ? cta_block_for(n) : 32;
@@ -532,6 +815,13 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
     cudaFreeHost(c->h_ops);
     delete c;
     return cuda_fail(ctx, e, "circuit upload");
+  }
+  if (sch.steps_off >= 0) {
+    c->d_steps = reinterpret_cast<const uint4*>(c->d_ops + sch.steps_off);
+    c->d_lops = reinterpret_cast<const uint4*>(c->d_ops + sch.lops_off);
+    c->d_wins = reinterpret_cast<const uint4*>(c->d_ops + sch.wins_off);
+    c->nsteps = sch.nsteps;
+    c->nwins = sch.nwins;
   }
   *out = c;
   return SDIM_OK;
@@ -584,7 +874,8 @@ int sdim_run(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot0,
   int rc = ensure(ctx, ctx->out, std::max<size_t>(bytes, 1));
   if (rc != SDIM_OK) return rc;
   // host -> device: the program's instruction stream; device -> host: records
-  CK(cudaMemcpyAsync(c->d_ops, c->h_ops, (size_t)c->nops * sizeof(uint2), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(c->d_ops, c->h_ops, (size_t)c->blob_words * sizeof(uint2), cudaMemcpyHostToDevice,
+                     ctx->stream));
   std::vector<Job> jobs{Job{c, seed, shot0, nshots, static_cast<uint8_t*>(ctx->out.p)}};
   rc = launch_jobs(ctx, jobs, ctx->stream, flags & ~SDIM_FLAG_ASYNC);
   if (rc != SDIM_OK) return rc;
@@ -595,10 +886,8 @@ int sdim_run(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot0,
   if (bytes) CK(cudaMemcpyAsync(out, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->timing_pending) {
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->last_ms = ms;
-    ctx->timing_pending = false;
+    const int trc = collect_times(ctx);
+    if (trc != SDIM_OK) return trc;
   }
   return read_status(ctx);
 }
@@ -647,10 +936,8 @@ int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, c
   }
   CK(cudaStreamSynchronize(s));
   if (ctx->timing_pending) {
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->last_ms = ms;
-    ctx->timing_pending = false;
+    const int trc = collect_times(ctx);
+    if (trc != SDIM_OK) return trc;
   }
   return read_status(ctx);
 }
@@ -665,22 +952,25 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
   std::vector<uint2> dev;
   std::vector<size_t> op_off(ncirc);
+  std::vector<TraceSchedule> sch(ncirc);
   std::vector<sdim_circuit> circs(ncirc);
   int rc;
   for (int i = 0; i < ncirc; ++i) {
     op_off[i] = dev.size();
-    int nmeas = 0;
+    int nmeas = 0, nn1 = 0;
     const int64_t r0 = row_begin[i], r1 = row_begin[i + 1];
     if (r1 < r0) return fail(ctx, SDIM_EINVAL, "row offsets must not decrease");
-    rc = encode_rows(ctx, rows + 4 * r0, r1 - r0, noise_prob ? noise_prob + r0 : nullptr, n[i], d[i], dev, nmeas);
+    rc = encode_rows(ctx, rows + 4 * r0, r1 - r0, noise_prob ? noise_prob + r0 : nullptr, n[i], d[i], dev, nmeas, nn1);
     if (rc != SDIM_OK) return rc;
     sdim_circuit& c = circs[i];
     c.device = ctx->device;
     c.n = n[i];
     c.d = d[i];
     c.nmeas = nmeas;
+    c.nn1 = nn1;
     c.nops_user = r1 - r0;
     c.nops = (int)(dev.size() - op_off[i]);
+    if (d[i] == 2 && trace_words(n[i])) append_schedule(dev, op_off[i], (size_t)c.nops, n[i], sch[i]);
     c.variant = variant_for(d[i]);
     c.gvariant = group_variant_for(d[i], n[i], 0);
     c.gblock = variant_ops(c.gvariant).cta ? cta_block_for(n[i]) : 32;
@@ -702,7 +992,16 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
   if (!dev.empty()) std::memcpy(ctx->staging, dev.data(), dev.size() * sizeof(uint2));
   CK(cudaMemcpyAsync(ctx->arena.p, ctx->staging, dev.size() * sizeof(uint2), cudaMemcpyHostToDevice, s));
   uint2* base = static_cast<uint2*>(ctx->arena.p);
-  for (int i = 0; i < ncirc; ++i) circs[i].d_ops = base + op_off[i];
+  for (int i = 0; i < ncirc; ++i) {
+    circs[i].d_ops = base + op_off[i];
+    if (sch[i].steps_off >= 0) {
+      circs[i].d_steps = reinterpret_cast<const uint4*>(base + sch[i].steps_off);
+      circs[i].d_lops = reinterpret_cast<const uint4*>(base + sch[i].lops_off);
+      circs[i].d_wins = reinterpret_cast<const uint4*>(base + sch[i].wins_off);
+      circs[i].nsteps = sch[i].nsteps;
+      circs[i].nwins = sch[i].nwins;
+    }
+  }
   const bool on_dev = flags & SDIM_FLAG_OUT_DEVICE;
   std::vector<size_t> offs(ncirc);
   size_t total = 0;
@@ -734,10 +1033,8 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
   if (flags & SDIM_FLAG_ASYNC) return SDIM_OK;
   CK(cudaStreamSynchronize(s));
   if (ctx->timing_pending) {
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->last_ms = ms;
-    ctx->timing_pending = false;
+    const int trc = collect_times(ctx);
+    if (trc != SDIM_OK) return trc;
   }
   return read_status(ctx);
 }
@@ -774,15 +1071,19 @@ int sdim_sync(sdim_ctx* ctx) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->last_stream ? ctx->last_stream : ctx->stream));
   if (ctx->timing_pending) {
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->last_ms = ms;
-    ctx->timing_pending = false;
+    const int trc = collect_times(ctx);
+    if (trc != SDIM_OK) return trc;
   }
   return ctx->status.p ? read_status(ctx) : SDIM_OK;
 }
 
 double sdim_last_kernel_ms(const sdim_ctx* ctx) { return ctx ? ctx->last_ms : -1.0; }
+
+int sdim_last_stage_ms(const sdim_ctx* ctx, double out[3]) {
+  if (!ctx || !out) return SDIM_EINVAL;
+  for (int i = 0; i < 3; ++i) out[i] = ctx->stage_ms[i];
+  return SDIM_OK;
+}
 
 int sdim_snapshot(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot, int mode, int8_t* out,
                   uint8_t* records_out, unsigned flags) {

@@ -1,0 +1,101 @@
+// Trace engine for d = 2: the shot-independent part of a program (x / z
+// blocks and the common phase c) runs once per program; every shot then
+// replays only its own phase deltas from a trace of what those read.  This
+// header is what the host side sees: the per-program descriptor and the two
+// launchers (k_trace.cu).
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sdim {
+
+// Trace of one program, written by the x / z pass, read by the phase pass.
+//   mhdr[k] (measurement k, M or RESET in program order):
+//     x = bit 0 deterministic, bit 1 RESET
+//     y = pivot generator p (random measurements)
+//     z = number of N1 ordinals before the measurement
+//     w = common outcome phase aph_c (deterministic measurements)
+//   mrow[k][0][tw]: factor words -- random: x_q over the 2n generators with
+//     bit p cleared; deterministic: the destabilizer half of x_q (Wn words)
+//   mrow[k][1][tw]: z_q after the measurement (RESET only)
+//   nhdr[j] (N1 ordinal j): x = coin threshold, y = opcode
+//   nthr[j]: the coin threshold again, padded to a multiple of 64 ordinals
+//     with 0xffffffff, for the phase pass's 64-coin masks
+//   nrow[j][0][tw], nrow[j][1][tw]: x_q and z_q at the N1
+// Rows are tw words (a power of two >= 2 Wn), zero past 2 Wn.  The x / z
+// pass reads the program's layered schedule (steps, lops, windows; built by
+// the host encoder, see append_schedule in abi.cu).
+struct TraceDesc {
+  CircuitDesc c;  // item_begin counts 32-shot groups of the phase pass
+  const uint4* steps;
+  const uint4* lops;
+  const uint4* wins;
+  uint4* mhdr;
+  uint32_t* mrow;
+  uint2* nhdr;
+  uint32_t* nthr;
+  uint32_t* nrow;
+  int nsteps;
+  int nwins;
+  int nm;   // measurements (M and RESET)
+  int nn1;  // N1 ordinals
+  int tw;   // words per trace row
+  int wn;   // words per generator half
+};
+
+__host__ __device__ inline size_t round_up(size_t b, size_t a) { return (b + a - 1) / a * a; }
+
+// Byte offsets of the trace arrays inside one program's trace (each array
+// 256-byte aligned); o[5] is the total.
+__host__ __device__ inline void trace_offsets(int nm, int nn1, int tw, size_t o[6]) {
+  o[0] = 0;                                                        // mhdr
+  o[1] = o[0] + round_up((size_t)nm * 16, 256);                    // mrow
+  o[2] = o[1] + round_up((size_t)nm * 8 * tw, 256);                // nhdr
+  o[3] = o[2] + round_up((size_t)nn1 * 8, 256);                    // nthr
+  o[4] = o[3] + round_up(round_up((size_t)nn1, 64) * 4, 256);      // nrow
+  o[5] = o[4] + round_up((size_t)nn1 * 8 * tw, 256);
+}
+
+__host__ __device__ inline size_t trace_bytes(int nm, int nn1, int tw) {
+  size_t o[6];
+  trace_offsets(nm, nn1, tw, o);
+  return o[5];
+}
+
+// Widest trace row the phase pass has an instance for (n <= 512).
+constexpr int kTraceMaxWords = 32;
+
+// Words per trace row for n qudits, 0 when n is too large for the phase pass.
+__host__ __device__ inline int trace_words(int n) {
+  const int w2 = 2 * ((n + 31) >> 5);
+  int tw = 2;
+  while (tw < w2) tw <<= 1;
+  return tw <= kTraceMaxWords ? tw : 0;
+}
+
+// Threads of the x / z pass (one CTA per program).
+constexpr int kTracePassThreads = 512;
+
+// Schedule window the x / z pass stages in shared memory: steps and ops.
+constexpr int kTraceWinSteps = 512;
+constexpr int kTraceWinOps = 2048;
+inline size_t trace_pass_window_bytes() { return (size_t)16 * (kTraceWinSteps + kTraceWinOps); }
+
+// Shared-memory bytes of one x / z pass CTA (hot part, x / z part).
+size_t trace_pass_hot_bytes(int n);
+size_t trace_pass_xz_bytes(int n);
+cudaError_t trace_set_smem(int optin);
+
+// x / z pass: one CTA of kTracePassThreads per program, x / z in shared
+// memory when xz_in_smem, else at gxz + blockIdx.x * xz_bytes.
+void launch_trace_pass(int grid, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc, uint8_t* gxz,
+                       size_t xz_bytes, size_t hot_bytes, int xz_in_smem, int* status);
+
+// Phase pass: one lane per shot, one warp per 32-shot group; every program of
+// descs has trace rows of tw words.  Returns false for an unsupported tw.
+bool launch_phase_pass(int tw, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
+                       long long total_groups, int* status);
+
+}  // namespace sdim

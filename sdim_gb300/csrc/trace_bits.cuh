@@ -1,0 +1,492 @@
+// Trace engine for d = 2, device side.
+//
+// The shot-group engine (group_bits.cuh) rests on x / z and the common phase
+// c following the same updates in every shot, with only delta_s (ph_s = c +
+// delta_s mod 4) depending on the shot's outcomes and noise.  Nothing forces
+// the sharing to stop at 32 shots: the x / z pass runs x / z / c once per
+// program and records in a trace (trace.cuh) every value the delta updates
+// read; the phase pass then gives every shot one lane, delta_s in registers
+// (two bit planes over the 2n generators, TW words each), and replays
+//   N1 before measurement k : coin per ordinal; on a fire with Pauli
+//                             X^a Z^b, delta ^= 2 (a z_q + b x_q)
+//   random M (pivot p)      : delta_g += delta_p for g in FW;
+//                             delta_{n+p} = delta_p; delta_p = 2 m_s with
+//                             m_s from the outcome stream
+//   deterministic M         : m_s = (aph_c + sum_{i in f} delta_i) / 2
+//   RESET                   : delta ^= 2 m_s z_q
+// exactly as the group engine applies them, so records are identical to the
+// group and per-shot engines (same streams, same arithmetic).  N1 after the
+// last measurement changes no record and is not replayed.
+//
+// The x / z pass is one CTA per program walking the host-built layered
+// schedule instead of the instruction stream:
+//   gate layer : ops on pairwise disjoint qudits touch disjoint rows; their
+//                common-phase updates are xors into C1 (atomicXor), except a
+//                P's carry into C0, and a layer holds at most one P.  Every
+//                (op, word) pair is one task.
+//   measurement block (consecutive M / RESET): a deterministic measurement
+//                only reads the tableau, so the pivot searches of the whole
+//                block run at once, every deterministic measurement before
+//                the first random one is evaluated in parallel (one task per
+//                (measurement, qudit row) for the cross term), the random one
+//                runs on the whole CTA, and the rest of the block repeats.
+#pragma once
+#include "group_bits.cuh"
+#include "kernels.cuh"
+#include "trace.cuh"
+
+namespace sdim {
+
+// Measurements of a block handled per round of the block loop (scratch size).
+constexpr int kTraceBlockMeas = 256;
+
+using TraceTab = TGroupBits<CtaTeam>;
+
+// ---------------------------------------------------------------- x / z pass
+
+// Word w of one op of a gate layer (w in [0, tw); words past 2 Wn only pad
+// the N1 rows with zeros).
+__device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, const uint4 lo, int w, int* status) {
+  const uint32_t op = lo.x & kOpMask;
+  const int q = (int)(lo.x >> 8);
+  const int n = e.n, W2 = e.W2, RS = e.RS, tw = td.tw;
+  if (q >= n) {
+    atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+    return;
+  }
+  const bool in = w < W2;
+  uint32_t* xr = e.X + (size_t)q * RS;
+  uint32_t* zr = e.Z + (size_t)q * RS;
+  switch (op) {
+    case OP_H:
+    case OP_H_INV:
+      if (in) {
+        const uint32_t x = xr[w], z = zr[w];
+        if (x & z) atomicXor(&e.C1[w], x & z);
+        xr[w] = z;
+        zr[w] = x;
+      }
+      break;
+    case OP_P:
+    case OP_P_INV:
+      if (in) {
+        const uint32_t x = xr[w], lo0 = e.C0[w];
+        const uint32_t c = (op == OP_P_INV) ? (~lo0 & x) : (lo0 & x);
+        e.C0[w] = lo0 ^ x;  // the layer's only P
+        if (c) atomicXor(&e.C1[w], c);
+        zr[w] ^= x;
+      }
+      break;
+    case OP_CNOT:
+    case OP_CNOT_INV: {
+      const int tq = (int)lo.y;
+      if (tq >= n) {
+        atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+        return;
+      }
+      if (in) {
+        e.X[(size_t)tq * RS + w] ^= xr[w];
+        zr[w] ^= e.Z[(size_t)tq * RS + w];
+      }
+      break;
+    }
+    case OP_X:
+    case OP_X_INV:  // d = 2: phase += 2 z_q
+      if (in) {
+        const uint32_t v = zr[w];
+        if (v) atomicXor(&e.C1[w], v);
+      }
+      break;
+    case OP_Z:
+    case OP_Z_INV:  // d = 2: phase += 2 x_q
+      if (in) {
+        const uint32_t v = xr[w];
+        if (v) atomicXor(&e.C1[w], v);
+      }
+      break;
+    case OP_N1D:
+    case OP_N1F:
+    case OP_N1P:
+    case OP_N1OFF: {
+      const uint32_t j = lo.z;
+      if ((int)j >= td.nn1) {
+        atomicCAS(status, DEV_OK, DEV_SLOT_TOO_SMALL);
+        return;
+      }
+      const bool off = op == OP_N1OFF;
+      if (!off) {
+        uint32_t* dst = td.nrow + (size_t)j * 2 * tw;
+        dst[w] = in ? xr[w] : 0u;
+        dst[tw + w] = in ? zr[w] : 0u;
+      }
+      if (w == 0) {
+        const uint32_t thr = off ? 0xffffffffu : lo.y;
+        td.nhdr[j] = make_uint2(thr, op);
+        td.nthr[j] = thr;
+      }
+      break;
+    }
+    case OP_NOP:
+      break;
+    default:
+      atomicCAS(status, DEV_OK, DEV_BAD_OPCODE);
+  }
+}
+
+// Entries M[s..r) of a block -- deterministic measurements and N1 -- all on
+// the current tableau.  M may point into shared memory (plain loads).
+__device__ void trace_det_range(TraceTab& e, const TraceDesc& td, const uint4* M, int s, int r, int* tacc,
+                                int* pacc, int* status) {
+  const int t = e.tm.t, size = e.tm.size();
+  const int n = e.n, Wn = e.Wn, W2 = e.W2, RS = e.RS, tw = td.tw;
+  for (int k = s + t; k < r; k += size) {
+    tacc[k] = 0;
+    pacc[k] = 0;
+  }
+  e.tm.sync();
+  const int cnt = r - s;
+  const int lg = __ffs(tw) - 1;
+  // N1 rows; common part of the factor sum, factor rows, RESET rows
+  for (int task = t; task < (cnt << lg); task += size) {
+    const int k = s + (task >> lg), w = task & (tw - 1);
+    const uint4 m = M[k];
+    const uint32_t op = m.x & kOpMask;
+    if (op != OP_M && op != OP_RESET) {
+      layer_word(e, td, m, w, status);
+      continue;
+    }
+    const int q = (int)(m.x >> 8);
+    uint32_t* row = td.mrow + (size_t)m.z * 2 * tw;
+    uint32_t f = 0u;
+    if (w < Wn) {
+      f = e.X[(size_t)q * RS + Wn + w];
+      const int pl = __popc(f & e.C0[w]) + 2 * __popc(f & e.C1[w]);
+      if (pl) atomicAdd(&pacc[k], pl);
+    }
+    row[w] = f;
+    if (op == OP_RESET) row[tw + w] = w < W2 ? e.Z[(size_t)q * RS + w] : 0u;
+  }
+  // cross term T: one task per (measurement, qudit row)
+  for (int task = t; task < cnt * n; task += size) {
+    const int kk = task / n, kr = task - kk * n;
+    const uint4 m = M[s + kk];
+    const uint32_t op = m.x & kOpMask;
+    if (op != OP_M && op != OP_RESET) continue;
+    const uint32_t* fq = e.X + (size_t)(m.x >> 8) * RS + Wn;
+    const uint32_t* xr = e.X + (size_t)kr * RS;
+    const uint32_t* zr = e.Z + (size_t)kr * RS;
+    uint32_t carry = 0u, tpar = 0u;
+    for (int w = 0; w < Wn; ++w) {
+      const uint32_t f = fq[w];
+      if (!f) continue;
+      const uint32_t a = xr[w] & f, b = zr[w] & f;
+      uint32_t v = b;
+      v ^= v << 1;
+      v ^= v << 2;
+      v ^= v << 4;
+      v ^= v << 8;
+      v ^= v << 16;
+      const uint32_t excl = (v ^ b) ^ (0u - carry);
+      tpar ^= (uint32_t)__popc(a & excl) & 1u;
+      carry ^= (uint32_t)__popc(b) & 1u;
+    }
+    if (tpar) atomicXor(&tacc[s + kk], 1);
+  }
+  e.tm.sync();
+  for (int k = s + t; k < r; k += size) {
+    const uint4 m = M[k];
+    const uint32_t op = m.x & kOpMask;
+    if (op != OP_M && op != OP_RESET) continue;
+    td.mhdr[m.z] = make_uint4(op == OP_RESET ? 3u : 1u, 0u, m.w, (uint32_t)((pacc[k] + 2 * tacc[k]) & 3));
+  }
+  e.tm.sync();
+}
+
+// A random measurement with pivot p, on the whole CTA.
+__device__ void trace_random(TraceTab& e, const TraceDesc& td, const uint4 m, int p) {
+  const int t = e.tm.t, size = e.tm.size();
+  const int n = e.n, Wn = e.Wn, W2 = e.W2, RS = e.RS, tw = td.tw;
+  const int q = (int)(m.x >> 8);
+  const bool reset = (m.x & kOpMask) == OP_RESET;
+  const int wp = p >> 5, bp = p & 31, wd = Wn + wp;
+  const uint32_t pbit = 1u << bp;
+  const int phc = (int)((e.C0[wp] >> bp) & 1u) | (int)(((e.C1[wp] >> bp) & 1u) << 1);
+  e.rowsum(q, p, phc);
+  e.tm.sync();
+  uint32_t* row = td.mrow + (size_t)m.z * 2 * tw;
+  for (int w = t; w < tw; w += size) row[w] = w < W2 ? e.FW[w] : 0u;
+  for (int k = t; k < n; k += size) {
+    uint32_t* xr = e.X + (size_t)k * RS;
+    uint32_t* zr = e.Z + (size_t)k * RS;
+    const uint32_t xs = xr[wp], zs = zr[wp];
+    xr[wd] = (xr[wd] & ~pbit) | (xs & pbit);
+    zr[wd] = (zr[wd] & ~pbit) | (zs & pbit);
+    xr[wp] = xs & ~pbit;
+    zr[wp] = (zs & ~pbit) | ((k == q) ? pbit : 0u);
+  }
+  e.tm.sync();
+  if (e.tm.leader()) {
+    e.C0[wd] = (e.C0[wd] & ~pbit) | ((uint32_t)(phc & 1) << bp);
+    e.C1[wd] = (e.C1[wd] & ~pbit) | ((uint32_t)(phc >> 1) << bp);
+    e.C0[wp] &= ~pbit;
+    e.C1[wp] &= ~pbit;
+    td.mhdr[m.z] = make_uint4(reset ? 2u : 0u, (uint32_t)p, m.w, 0u);
+  }
+  if (reset) {
+    e.tm.sync();
+    const uint32_t* zq = e.Z + (size_t)q * RS;
+    for (int w = t; w < tw; w += size) row[tw + w] = w < W2 ? zq[w] : 0u;
+  }
+  e.tm.sync();
+}
+
+// A block of consecutive M / RESET with the N1 between them (schedule ops
+// L[0..count), in shared or global memory).
+__device__ void trace_block(TraceTab& e, const TraceDesc& td, const uint4* L, int count, int* piv, int* tacc,
+                            int* pacc, int* status) {
+  const int t = e.tm.t, size = e.tm.size();
+  const int n = e.n, Wn = e.Wn, RS = e.RS;
+  for (int c0 = 0; c0 < count; c0 += kTraceBlockMeas) {
+    const int B = min(kTraceBlockMeas, count - c0);
+    const uint4* M = L + c0;
+    for (int k = t; k < B; k += size) {
+      const uint4 m = M[k];
+      const uint32_t op = m.x & kOpMask;
+      const bool meas = op == OP_M || op == OP_RESET;
+      if ((int)(m.x >> 8) >= n || (meas ? (int)m.z >= td.nm : (int)m.z >= td.nn1))
+        atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+    }
+    if (e.tm.any(*(volatile int*)status != DEV_OK)) return;
+    int s = 0;
+    while (s < B) {
+      for (int k = s + t; k < B; k += size) piv[k] = INT_MAX;
+      e.tm.sync();
+      for (int task = t; task < (B - s) * Wn; task += size) {
+        const int kk = task / Wn, w = task - kk * Wn;
+        const uint4 m = M[s + kk];
+        const uint32_t op = m.x & kOpMask;
+        if (op != OP_M && op != OP_RESET) continue;
+        const uint32_t v = e.X[(size_t)(m.x >> 8) * RS + w];
+        if (v) atomicMin(&piv[s + kk], (w << 5) + __ffs(v) - 1);
+      }
+      e.tm.sync();
+      int mine = INT_MAX;
+      for (int k = s + t; k < B; k += size)
+        if (piv[k] != INT_MAX) {
+          mine = k;
+          break;
+        }
+      const int first = e.tm.min(mine);
+      const int r = first == INT_MAX ? B : first;
+      if (r > s) trace_det_range(e, td, M, s, r, tacc, pacc, status);
+      if (r < B) trace_random(e, td, M[r], piv[r]);
+      s = r + 1;
+    }
+  }
+}
+
+// Runs the shared part of td's program over its layered schedule and writes
+// the trace.  Each schedule window is staged in shared memory (win: room for
+// kTraceWinSteps steps, then kTraceWinOps ops) with one cooperative load.
+__device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int* piv, int* tacc, int* pacc,
+                              int* status) {
+  e.init(0);
+  const int t = e.tm.t, size = e.tm.size(), tw = td.tw;
+  const int lg = __ffs(tw) - 1;
+  uint4* wsteps = win;
+  uint4* wops = win + kTraceWinSteps;
+  for (int wi = 0; wi < td.nwins; ++wi) {
+    const uint4 wd = __ldg(td.wins + wi);
+    const int nst = min((int)wd.y, kTraceWinSteps);
+    const bool staged = wd.w <= (uint32_t)kTraceWinOps;
+    for (int i = t; i < nst; i += size) wsteps[i] = __ldg(td.steps + wd.x + i);
+    if (staged)
+      for (int i = t; i < (int)wd.w; i += size) wops[i] = __ldg(td.lops + wd.z + i);
+    e.tm.sync();
+    for (int si = 0; si < nst; ++si) {
+      const uint4 st = wsteps[si];
+      if (staged && (st.y < wd.z || st.y - wd.z + st.z > wd.w)) {
+        if (t == 0) atomicCAS(status, DEV_OK, DEV_SLOT_TOO_SMALL);
+        break;
+      }
+      const uint4* L = staged ? wops + (st.y - wd.z) : td.lops + st.y;
+      if (st.x == 0u) {
+        const int total = (int)st.z << lg;
+        for (int task = t; task < total; task += size) layer_word(e, td, L[task >> lg], task & (tw - 1), status);
+        e.tm.sync();
+      } else {
+        trace_block(e, td, L, (int)st.z, piv, tacc, pacc, status);
+      }
+    }
+    e.tm.sync();
+  }
+  const int pad = (int)round_up((size_t)td.nn1, 64);
+  for (int j = td.nn1 + t; j < pad; j += size) td.nthr[j] = 0xffffffffu;
+  e.tm.sync();
+}
+
+// ---------------------------------------------------------------- phase pass
+
+// Philox4x32-10 keyed by the seed (philox4x32_10 with the key held here).
+struct PhiloxKeys {
+  uint2 key;
+  __device__ explicit PhiloxKeys(unsigned long long seed) : key(make_uint2((uint32_t)seed, (uint32_t)(seed >> 32))) {}
+  __device__ __forceinline__ uint4 block(uint4 c) const { return philox4x32_10(c, key); }
+};
+
+// Fire mask of N1 ordinals [cb, cb + 64) of one shot: 16 coin blocks against
+// the thresholds, four independent blocks at a time (overlapped by the
+// unrolled inner loop without running out of registers).
+__device__ __forceinline__ unsigned long long coin_mask(const PhiloxKeys& K, const uint32_t* nthr, uint32_t cb,
+                                                        uint32_t shot_lo, uint32_t shot_hi) {
+  unsigned long long m = 0ull;
+  const uint4* t4 = reinterpret_cast<const uint4*>(nthr + cb);
+#pragma unroll 1
+  for (int g = 0; g < 4; ++g) {
+    uint32_t bits = 0u;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const uint4 c = K.block(make_uint4((cb >> 2) + (uint32_t)(4 * g + b), shot_lo, shot_hi, 1u));
+      const uint4 th = __ldg(t4 + 4 * g + b);
+      bits |= ((uint32_t)(c.x >= th.x) | ((uint32_t)(c.y >= th.y) << 1) | ((uint32_t)(c.z >= th.z) << 2) |
+               ((uint32_t)(c.w >= th.w) << 3)) << (4 * b);
+    }
+    m |= (unsigned long long)bits << (16 * g);
+  }
+  return m;
+}
+
+template <int N>
+__device__ __forceinline__ void load_row(const uint32_t* p, uint32_t (&r)[N]) {
+  if constexpr (N % 4 == 0) {
+    const uint4* p4 = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) {
+      const uint4 v = __ldg(p4 + i);
+      r[4 * i] = v.x;
+      r[4 * i + 1] = v.y;
+      r[4 * i + 2] = v.z;
+      r[4 * i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) r[i] = __ldg(p + i);
+  }
+}
+
+// The descriptor is read once into registers: the byte stores of the records
+// could alias it, which would make every field a reload.
+template <int TW>
+__device__ __forceinline__ void phase_program(const TraceDesc& tdesc, long long group, int lane) {
+  const uint4* __restrict__ mhdr = tdesc.mhdr;
+  const uint32_t* __restrict__ mrow = tdesc.mrow;
+  const uint2* __restrict__ nhdr = tdesc.nhdr;
+  const uint32_t* __restrict__ nthr = tdesc.nthr;
+  const uint32_t* __restrict__ nrow = tdesc.nrow;
+  const int nm = tdesc.nm, wn = tdesc.wn, nmeas = tdesc.c.nmeas;
+  const uint32_t nn1 = (uint32_t)tdesc.nn1;
+  const unsigned long long seed = tdesc.c.seed;
+  const long long rel = group * 32 + lane;
+  const bool active = rel < (long long)tdesc.c.nshots;
+  const long long shot = tdesc.c.shot0 + rel;
+  const uint32_t shot_lo = (uint32_t)(unsigned long long)shot, shot_hi = (uint32_t)((unsigned long long)shot >> 32);
+  uint8_t* __restrict__ out = tdesc.c.out + (active ? rel : 0) * (long long)nmeas;
+  const PhiloxKeys K(seed);
+  uint32_t d0[TW], d1[TW];
+#pragma unroll
+  for (int w = 0; w < TW; ++w) d0[w] = d1[w] = 0u;
+  uint32_t nord = 0, cbase = 0xffffffffu;
+  unsigned long long fire = 0ull;
+  for (int k = 0; k < nm; ++k) {
+    const uint4 h = __ldg(mhdr + k);
+    const uint32_t nend = h.z < nn1 ? h.z : nn1;
+    while (nord < nend) {
+      const uint32_t cb = nord & ~63u;
+      if (cb != cbase) {
+        cbase = cb;
+        fire = coin_mask(K, nthr, cb, shot_lo, shot_hi);
+      }
+      const uint32_t hi = nend < cb + 64 ? nend : cb + 64;
+      unsigned long long m = fire >> (nord - cb);
+      if (hi - nord < 64) m &= (1ull << (hi - nord)) - 1ull;
+      if (!active) m = 0ull;
+      while (m) {
+        const uint32_t j = nord + (uint32_t)(__ffsll((long long)m) - 1);
+        m &= m - 1ull;
+        const uint2 nh = __ldg(nhdr + j);
+        if (nh.y == OP_N1OFF) continue;  // threshold 0xffffffff: a coin of 0xffffffff is not a fire
+        const int2 ab = noise_choice(nh.y, 2, seed, shot, j);
+        const uint32_t mz = ab.x ? 0xffffffffu : 0u, mx = (ab.y & 1) ? 0xffffffffu : 0u;
+        uint32_t xr[TW], zr[TW];
+        load_row<TW>(nrow + (size_t)j * 2 * TW, xr);
+        load_row<TW>(nrow + (size_t)j * 2 * TW + TW, zr);
+#pragma unroll
+        for (int w = 0; w < TW; ++w) d1[w] ^= (zr[w] & mz) ^ (xr[w] & mx);
+      }
+      nord = hi;
+    }
+    const uint32_t* row = mrow + (size_t)k * 2 * TW;
+    const uint32_t det = h.x & 1u;
+    int m;
+    if (!det) {
+      const int p = (int)h.y, wp = p >> 5, bp = p & 31, wd = wn + wp;
+      const uint32_t pbit = 1u << bp;
+      uint32_t a0 = 0u, a1 = 0u;
+#pragma unroll
+      for (int w = 0; w < TW; ++w)
+        if (w == wp) {
+          a0 = d0[w];
+          a1 = d1[w];
+        }
+      const uint32_t dp0 = (a0 >> bp) & 1u, dp1 = (a1 >> bp) & 1u;
+      if (dp0 | dp1) {
+        const uint32_t m0 = 0u - dp0, m1 = 0u - dp1;
+        uint32_t F[TW];
+        load_row<TW>(row, F);
+#pragma unroll
+        for (int w = 0; w < TW; ++w) {
+          const uint32_t lo = d0[w], a = F[w] & m0;
+          d0[w] = lo ^ a;
+          d1[w] ^= (F[w] & m1) ^ (lo & a);
+        }
+      }
+      m = active ? mulshift(K.block(make_uint4((uint32_t)k, shot_lo, shot_hi, 0u)).x, 2u) : 0;
+#pragma unroll
+      for (int w = 0; w < TW; ++w) {
+        if (w == wd) {
+          d0[w] = (d0[w] & ~pbit) | (dp0 << bp);
+          d1[w] = (d1[w] & ~pbit) | (dp1 << bp);
+        }
+        if (w == wp) {
+          d0[w] &= ~pbit;
+          d1[w] = (d1[w] & ~pbit) | ((uint32_t)m << bp);
+        }
+      }
+    } else {
+      uint32_t f[TW / 2];
+      load_row<TW / 2>(row, f);
+      int sacc = 0;
+#pragma unroll
+      for (int w = 0; w < TW / 2; ++w) sacc += __popc(f[w] & d0[w]) + 2 * __popc(f[w] & d1[w]);
+      m = (((((int)h.w + sacc) & 3) + 1) >> 1) & 1;
+    }
+    if ((h.x & 2u) && (m & 1)) {
+      uint32_t z[TW];
+      load_row<TW>(row + TW, z);
+#pragma unroll
+      for (int w = 0; w < TW; ++w) d1[w] ^= z[w];
+    }
+    if (active && k < nmeas) out[k] = (uint8_t)(m | (int)(det << 7));
+  }
+}
+
+__device__ __forceinline__ int find_trace_desc(const TraceDesc* descs, int ndesc, long long it) {
+  int lo = 0, hi = ndesc - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (descs[mid].c.item_begin <= it) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace sdim

@@ -119,14 +119,20 @@ class Program:
 
     # ------------------------------------------------------------------
     def sample(self, shots: int, seed: Optional[int] = None, shot0: int = 0, noise: bool = True,
-               plain: bool = False, out: Optional[np.ndarray] = None, per_shot: bool = False) -> np.ndarray:
+               plain: bool = False, out: Optional[np.ndarray] = None, per_shot: bool = False,
+               engine: Optional[str] = None) -> np.ndarray:
         """Records of shots [shot0, shot0 + shots) as a (shots, records) uint8
-        array, value | deterministic << 7 -- the fast path without Python objects."""
+        array, value | deterministic << 7 -- the fast path without Python objects.
+
+        ``engine`` picks the batched engine: None (by shot count and d),
+        "trace" (d = 2: one x / z pass, one lane per shot), "group" (32-shot
+        groups), "per_shot" (one warp per shot; same as ``per_shot=True``)."""
         dp = self.compile(noise)
         s = self._seed(seed)
         if out is None:
             out = np.empty((int(shots), dp.num_records), dtype=np.uint8)
         flags = (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_PER_SHOT if per_shot else 0)
+        flags |= _lib.engine_flags(engine)
         if shots > 0 and dp.num_records > 0:
             rc = self.context.lib.sdim_run(self.context.ptr, dp.ptr, s, int(shot0), int(shots),
                                            out.ctypes.data, flags)

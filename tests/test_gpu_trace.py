@@ -1,0 +1,103 @@
+"""GPU: the d = 2 trace engine (one x / z pass per program, one lane per shot
+replaying its phase deltas) against the oracle and the other engines, for
+every trace-row width, both x / z pass teams, partial shot groups, every
+noise channel (including p = 0 and p = 1), mixed batches and global-memory
+x / z slots."""
+import numpy as np
+import pytest
+
+from sdim_gb300 import Program, _lib, workloads
+from sdim_gb300.batch import BatchRunner
+from tests.conftest import oracle_run
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("distance,rounds,prob,shots,shot0", [(3, 3, 0.05, 200, 5), (5, 2, 0.02, 100, 0),
+                                                              (7, 2, 0.01, 65, 31)])
+def test_surface_codes_match_oracle(distance, rounds, prob, shots, shot0):
+    spec = workloads.surface_memory(distance, rounds, prob=prob)
+    prog = Program(spec.build())
+    rec = prog.sample(shots, seed=4, shot0=shot0, engine="trace")
+    assert np.array_equal(rec, oracle_run([spec], 4, shot0, shots)["records"])
+    assert np.array_equal(rec, prog.sample(shots, seed=4, shot0=shot0, engine="group"))
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 31, 32, 33, 64, 65, 97, 128, 129, 159])
+def test_every_row_width_small_n_against_oracle(n):
+    spec = workloads.random_hpc(n, 2, 6 * n + 20, seed=700 + n, mr_every=max(1, n // 2), mr_fraction=0.3)
+    prog = Program(spec.build())
+    rec = prog.sample(70, seed=n, engine="trace")
+    assert np.array_equal(rec, oracle_run([spec], n, 0, 70)["records"]), n
+
+
+@pytest.mark.parametrize("n", [160, 200, 256, 257, 400, 512])
+def test_cta_pass_and_wide_rows_against_group_engine(n):
+    spec = workloads.random_hpc(n, 2, 4 * n, seed=900 + n, mr_every=n, mr_fraction=0.2)
+    prog = Program(spec.build())
+    rec = prog.sample(96, seed=n, engine="trace")
+    assert np.array_equal(rec, prog.sample(96, seed=n, engine="group")), n
+    if n <= 200:
+        assert np.array_equal(rec, oracle_run([spec], n, 0, 96)["records"]), n
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_all_gates_and_noise_channels(seed):
+    spec = workloads.all_gates_random(7, 2, 300, seed=seed, noise_probs=(0.0, 0.35, 1.0))
+    prog = Program(spec.build())
+    rec = prog.sample(130, seed=seed, shot0=11, engine="trace")
+    assert np.array_equal(rec, oracle_run([spec], seed, 11, 130)["records"])
+
+
+def test_records_do_not_depend_on_the_split():
+    spec = workloads.surface_memory(5, 3, prob=0.03)
+    prog = Program(spec.build())
+    whole = prog.sample(150, seed=8, engine="trace")
+    parts = np.concatenate([prog.sample(37, seed=8, engine="trace"),
+                            prog.sample(113, seed=8, shot0=37, engine="trace")])
+    assert np.array_equal(whole, parts)
+    assert np.array_equal(whole[:20], prog.sample(20, seed=8))        # group engine below 64 shots
+    assert np.array_equal(whole[:3], prog.sample(3, seed=8, per_shot=True))
+
+
+def test_mixed_batch_routes_each_program():
+    """d = 2 programs with many shots run on the trace engine, the others on
+    their group engines, all in one call; every result equals the oracle."""
+    rng = np.random.default_rng(3)
+    specs = [workloads.surface_memory(3, 2, prob=0.04), workloads.random_hpc(40, 2, 200, seed=5, mr_every=20),
+             workloads.random_hpc(12, 3, 120, seed=6, mr_every=6), workloads.random_hpc(300, 2, 900, seed=7,
+                                                                                        mr_every=300),
+             workloads.random_hpc(70, 2, 300, seed=8, mr_every=35)]
+    shots = [300, 10, 80, 64, 129]
+    runner = BatchRunner()
+    for i, (s, k) in enumerate(zip(specs, shots)):
+        runner.add_spec(s, k, seed=int(rng.integers(1 << 30)), shot0=i)
+    outs = runner.run()
+    for e, s, out in zip(runner.entries, specs, outs):
+        if s.num_qudits <= 70:
+            assert np.array_equal(out, oracle_run([s], e.seed, e.shot0, e.shots)["records"]), s.name
+    alone = Program(specs[3].build()).sample(64, seed=runner.entries[3].seed, shot0=3, engine="group")
+    assert np.array_equal(outs[3], alone)
+
+
+def test_xz_pass_in_global_memory():
+    spec = workloads.random_hpc(300, 2, 1200, seed=31, mr_every=150, mr_fraction=0.2)
+    prog = Program(spec.build())
+    dp = prog.compile(True)
+    ctx = prog.context
+    out = np.empty((72, dp.num_records), dtype=np.uint8)
+    rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 6, 0, 72, out.ctypes.data, _lib.FLAG_TRACE | _lib.FLAG_FORCE_GMEM)
+    _lib.check(rc, ctx.ptr, "trace, x / z in global memory")
+    assert np.array_equal(out, prog.sample(72, seed=6, engine="group"))
+
+
+def test_full_size_noisy_surface_against_group_engine_and_oracle():
+    """The bench workload at full size (distance 7, 7 rounds, p = 1e-3,
+    100k shots): trace and group engines agree on every record, and the
+    first and last 64 shots equal the oracle."""
+    spec = workloads.surface_memory(7, 7, prob=1e-3)
+    prog = Program(spec.build())
+    rec = prog.sample(100_000, seed=2, engine="trace")
+    assert np.array_equal(rec, prog.sample(100_000, seed=2, engine="group"))
+    assert np.array_equal(rec[:64], oracle_run([spec], 2, 0, 64)["records"])
+    assert np.array_equal(rec[-64:], oracle_run([spec], 2, 100_000 - 64, 64)["records"])
