@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -45,6 +46,7 @@ struct sdim_ctx {
   double stage_ms[3] = {0.0, 0.0, 0.0};  // x / z passes, phase passes, other engines
   int smem_attr_set[V_COUNT] = {};
   bool trace_smem_set = false;
+  int trace_threads = kTracePassThreads;  // x / z pass CTA size (SDIM_TRACE_PASS_THREADS: 256 or 512)
 };
 
 // Where the trace schedule of a program sits in its blob (uint2 words).
@@ -362,8 +364,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
       grid = std::min(grid, 2 * ctx->num_sms);
       if ((rc = ensure(ctx, ctx->gslots, xz * (size_t)grid)) != SDIM_OK) return rc;
     }
-    launch_trace_pass(grid, hot + (in_smem ? xz : 0) + win, s, dd, (int)k, static_cast<uint8_t*>(ctx->gslots.p), xz,
-                      hot, in_smem ? 1 : 0, status);
+    launch_trace_pass(ctx->trace_threads, grid, hot + (in_smem ? xz : 0) + win, s, dd, (int)k,
+                      static_cast<uint8_t*>(ctx->gslots.p), xz, hot, in_smem ? 1 : 0, status);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
   }
@@ -377,7 +379,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
       items = hd[e].c.item_begin + (hd[e].c.nshots + 31) / 32;
       ++e;
     }
-    const int warps = 8;
+    const int warps = kPhaseThreads / 32;
     const long long grid = (items + warps - 1) / warps;
     if (grid > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one phase pass");
     if (!launch_phase_pass(tw, (int)grid, 32 * warps, s, dd + b, (int)(e - b), items, status))
@@ -720,6 +722,7 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
   ctx->l2_bytes = prop.l2CacheSize;
   ctx->gmem_bytes = (int64_t)prop.totalGlobalMem;
   ctx->gmem_slot_budget = std::min<size_t>((size_t)8 << 30, (size_t)(prop.totalGlobalMem / 8));
+  if (const char* v = std::getenv("SDIM_TRACE_PASS_THREADS")) ctx->trace_threads = std::atoi(v) >= 512 ? 512 : 256;
   *out = ctx;
   return SDIM_OK;
 }

@@ -75,8 +75,11 @@ __host__ __device__ inline int trace_words(int n) {
   return tw <= kTraceMaxWords ? tw : 0;
 }
 
-// Threads of the x / z pass (one CTA per program).
+// Threads of the x / z pass (one CTA per program): 256 or 512.
 constexpr int kTracePassThreads = 512;
+
+// Threads of a phase-pass block (one warp: one 32-shot group).
+constexpr int kPhaseThreads = 32;
 
 // Schedule window the x / z pass stages in shared memory: steps and ops.
 constexpr int kTraceWinSteps = 512;
@@ -88,10 +91,10 @@ size_t trace_pass_hot_bytes(int n);
 size_t trace_pass_xz_bytes(int n);
 cudaError_t trace_set_smem(int optin);
 
-// x / z pass: one CTA of kTracePassThreads per program, x / z in shared
-// memory when xz_in_smem, else at gxz + blockIdx.x * xz_bytes.
-void launch_trace_pass(int grid, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc, uint8_t* gxz,
-                       size_t xz_bytes, size_t hot_bytes, int xz_in_smem, int* status);
+// x / z pass: one CTA of `threads` (256 or 512) per program, x / z in
+// shared memory when xz_in_smem, else at gxz + blockIdx.x * xz_bytes.
+void launch_trace_pass(int threads, int grid, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc,
+                       uint8_t* gxz, size_t xz_bytes, size_t hot_bytes, int xz_in_smem, int* status);
 
 // Phase pass: one lane per shot, one warp per 32-shot group; every program of
 // descs has trace rows of tw words.  Returns false for an unsupported tw.

@@ -133,17 +133,13 @@ __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, con
   }
 }
 
-// Entries M[s..r) of a block -- deterministic measurements and N1 -- all on
-// the current tableau.  M may point into shared memory (plain loads).
-__device__ void trace_det_range(TraceTab& e, const TraceDesc& td, const uint4* M, int s, int r, int* tacc,
-                                int* pacc, int* status) {
+// Work of entries M[s..r) of a block -- deterministic measurements and N1 --
+// all on the current tableau, without barriers (M may point into shared
+// memory: plain loads).  tacc / pacc of the entries must be zero.
+__device__ __forceinline__ void trace_det_tasks(TraceTab& e, const TraceDesc& td, const uint4* M, int s, int r,
+                                                int* tacc, int* pacc, int* status) {
   const int t = e.tm.t, size = e.tm.size();
   const int n = e.n, Wn = e.Wn, W2 = e.W2, RS = e.RS, tw = td.tw;
-  for (int k = s + t; k < r; k += size) {
-    tacc[k] = 0;
-    pacc[k] = 0;
-  }
-  e.tm.sync();
   const int cnt = r - s;
   const int lg = __ffs(tw) - 1;
   // N1 rows; common part of the factor sum, factor rows, RESET rows
@@ -166,9 +162,15 @@ __device__ void trace_det_range(TraceTab& e, const TraceDesc& td, const uint4* M
     row[w] = f;
     if (op == OP_RESET) row[tw + w] = w < W2 ? e.Z[(size_t)q * RS + w] : 0u;
   }
-  // cross term T: one task per (measurement, qudit row)
-  for (int task = t; task < cnt * n; task += size) {
-    const int kk = task / n, kr = task - kk * n;
+  // cross term T: one task per (entry, qudit row), walked without divisions
+  int kk = t / n, kr = t - (t / n) * n;
+  const int dk = size / n, dr = size - (size / n) * n;
+  for (; kk < cnt; kk += dk, kr += dr) {
+    if (kr >= n) {
+      kr -= n;
+      ++kk;
+      if (kk >= cnt) break;
+    }
     const uint4 m = M[s + kk];
     const uint32_t op = m.x & kOpMask;
     if (op != OP_M && op != OP_RESET) continue;
@@ -192,17 +194,24 @@ __device__ void trace_det_range(TraceTab& e, const TraceDesc& td, const uint4* M
     }
     if (tpar) atomicXor(&tacc[s + kk], 1);
   }
-  e.tm.sync();
-  for (int k = s + t; k < r; k += size) {
+}
+
+// Trace headers of the deterministic measurements among M[s..r) (after the
+// barrier that ends trace_det_tasks).
+__device__ __forceinline__ void trace_det_headers(TraceTab& e, const TraceDesc& td, const uint4* M, int s, int r,
+                                                  const int* tacc, const int* pacc) {
+  for (int k = s + e.tm.t; k < r; k += e.tm.size()) {
     const uint4 m = M[k];
     const uint32_t op = m.x & kOpMask;
     if (op != OP_M && op != OP_RESET) continue;
     td.mhdr[m.z] = make_uint4(op == OP_RESET ? 3u : 1u, 0u, m.w, (uint32_t)((pacc[k] + 2 * tacc[k]) & 3));
   }
-  e.tm.sync();
 }
 
-// A random measurement with pivot p, on the whole CTA.
+// A random measurement with pivot p, on the whole CTA: the rowsum (two
+// barriers inside), one barrier, then the pivot columns, the factor row and
+// the header in one phase (and the RESET row after one more barrier).  The
+// caller's next phase must not touch x / z before its own barrier.
 __device__ void trace_random(TraceTab& e, const TraceDesc& td, const uint4 m, int p) {
   const int t = e.tm.t, size = e.tm.size();
   const int n = e.n, Wn = e.Wn, W2 = e.W2, RS = e.RS, tw = td.tw;
@@ -224,7 +233,6 @@ __device__ void trace_random(TraceTab& e, const TraceDesc& td, const uint4 m, in
     xr[wp] = xs & ~pbit;
     zr[wp] = (zs & ~pbit) | ((k == q) ? pbit : 0u);
   }
-  e.tm.sync();
   if (e.tm.leader()) {
     e.C0[wd] = (e.C0[wd] & ~pbit) | ((uint32_t)(phc & 1) << bp);
     e.C1[wd] = (e.C1[wd] & ~pbit) | ((uint32_t)(phc >> 1) << bp);
@@ -237,12 +245,14 @@ __device__ void trace_random(TraceTab& e, const TraceDesc& td, const uint4 m, in
     const uint32_t* zq = e.Z + (size_t)q * RS;
     for (int w = t; w < tw; w += size) row[tw + w] = w < W2 ? zq[w] : 0u;
   }
-  e.tm.sync();
 }
 
 // A block of consecutive M / RESET with the N1 between them (schedule ops
-// L[0..count), in shared or global memory).
-__device__ void trace_block(TraceTab& e, const TraceDesc& td, const uint4* L, int count, int* piv, int* tacc,
+// L[0..count), in shared or global memory).  Per round of the loop: find the
+// first random measurement r at or after s (one atomicMin), evaluate the
+// deterministic entries before it and r's pivot in the same phase, write
+// their headers and run r.  sc: two ints of scratch.
+__device__ void trace_block(TraceTab& e, const TraceDesc& td, const uint4* L, int count, int* sc, int* tacc,
                             int* pacc, int* status) {
   const int t = e.tm.t, size = e.tm.size();
   const int n = e.n, Wn = e.Wn, RS = e.RS;
@@ -259,36 +269,43 @@ __device__ void trace_block(TraceTab& e, const TraceDesc& td, const uint4* L, in
     if (e.tm.any(*(volatile int*)status != DEV_OK)) return;
     int s = 0;
     while (s < B) {
-      for (int k = s + t; k < B; k += size) piv[k] = INT_MAX;
+      if (t == 0) {
+        sc[0] = INT_MAX;
+        sc[1] = INT_MAX;
+      }
+      for (int k = s + t; k < B; k += size) {
+        tacc[k] = 0;
+        pacc[k] = 0;
+      }
       e.tm.sync();
       for (int task = t; task < (B - s) * Wn; task += size) {
         const int kk = task / Wn, w = task - kk * Wn;
         const uint4 m = M[s + kk];
         const uint32_t op = m.x & kOpMask;
         if (op != OP_M && op != OP_RESET) continue;
-        const uint32_t v = e.X[(size_t)(m.x >> 8) * RS + w];
-        if (v) atomicMin(&piv[s + kk], (w << 5) + __ffs(v) - 1);
+        if (e.X[(size_t)(m.x >> 8) * RS + w]) atomicMin(&sc[0], s + kk);
       }
       e.tm.sync();
-      int mine = INT_MAX;
-      for (int k = s + t; k < B; k += size)
-        if (piv[k] != INT_MAX) {
-          mine = k;
-          break;
-        }
-      const int first = e.tm.min(mine);
+      const int first = sc[0];
       const int r = first == INT_MAX ? B : first;
-      if (r > s) trace_det_range(e, td, M, s, r, tacc, pacc, status);
-      if (r < B) trace_random(e, td, M[r], piv[r]);
+      if (r < B && t < Wn) {
+        const uint32_t v = e.X[(size_t)(M[r].x >> 8) * RS + t];
+        if (v) atomicMin(&sc[1], (t << 5) + __ffs(v) - 1);
+      }
+      if (r > s) trace_det_tasks(e, td, M, s, r, tacc, pacc, status);
+      e.tm.sync();
+      if (r > s) trace_det_headers(e, td, M, s, r, tacc, pacc);
+      if (r < B) trace_random(e, td, M[r], sc[1]);
       s = r + 1;
     }
+    e.tm.sync();
   }
 }
 
 // Runs the shared part of td's program over its layered schedule and writes
 // the trace.  Each schedule window is staged in shared memory (win: room for
 // kTraceWinSteps steps, then kTraceWinOps ops) with one cooperative load.
-__device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int* piv, int* tacc, int* pacc,
+__device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int* sc, int* tacc, int* pacc,
                               int* status) {
   e.init(0);
   const int t = e.tm.t, size = e.tm.size(), tw = td.tw;
@@ -315,7 +332,7 @@ __device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int*
         for (int task = t; task < total; task += size) layer_word(e, td, L[task >> lg], task & (tw - 1), status);
         e.tm.sync();
       } else {
-        trace_block(e, td, L, (int)st.z, piv, tacc, pacc, status);
+        trace_block(e, td, L, (int)st.z, sc, tacc, pacc, status);
       }
     }
     e.tm.sync();
@@ -327,31 +344,49 @@ __device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int*
 
 // ---------------------------------------------------------------- phase pass
 
-// Philox4x32-10 keyed by the seed (philox4x32_10 with the key held here).
+// Philox4x32-10 (the function of philox4x32_10) with its round keys
+// precomputed from the seed.  In a phase-pass warp the seed is uniform, so
+// the keys sit in uniform registers and each round is two 32x32->64
+// multiplies and two three-input xors.
 struct PhiloxKeys {
-  uint2 key;
-  __device__ explicit PhiloxKeys(unsigned long long seed) : key(make_uint2((uint32_t)seed, (uint32_t)(seed >> 32))) {}
-  __device__ __forceinline__ uint4 block(uint4 c) const { return philox4x32_10(c, key); }
+  uint32_t k0[10], k1[10];
+  __device__ explicit PhiloxKeys(unsigned long long seed) {
+    uint32_t a = (uint32_t)seed, b = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+      k0[r] = a;
+      k1[r] = b;
+      a += 0x9E3779B9u;
+      b += 0xBB67AE85u;
+    }
+  }
+  __device__ __forceinline__ uint4 block(uint4 c) const {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+      unsigned long long p0, p1;  // one 32x32->64 multiply each
+      asm("mul.wide.u32 %0, %1, %2;" : "=l"(p0) : "r"(c.x), "r"(0xD2511F53u));
+      asm("mul.wide.u32 %0, %1, %2;" : "=l"(p1) : "r"(c.z), "r"(0xCD9E8D57u));
+      c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k0[r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1[r],
+                     (uint32_t)p0);
+    }
+    return c;
+  }
 };
 
-// Fire mask of N1 ordinals [cb, cb + 64) of one shot: 16 coin blocks against
-// the thresholds, four independent blocks at a time (overlapped by the
-// unrolled inner loop without running out of registers).
-__device__ __forceinline__ unsigned long long coin_mask(const PhiloxKeys& K, const uint32_t* nthr, uint32_t cb,
-                                                        uint32_t shot_lo, uint32_t shot_hi) {
-  unsigned long long m = 0ull;
+// Fire mask of N1 ordinals [cb, cb + 32) of one shot (cb a multiple of 32):
+// eight coin blocks, unrolled so their Philox chains overlap, against the
+// thresholds; the exact bits are built only when a block has a fire.
+__device__ __forceinline__ uint32_t coin_mask(const PhiloxKeys& K, const uint32_t* nthr, uint32_t cb, uint32_t shot_lo,
+                                              uint32_t shot_hi) {
+  uint32_t m = 0u;
   const uint4* t4 = reinterpret_cast<const uint4*>(nthr + cb);
-#pragma unroll 1
-  for (int g = 0; g < 4; ++g) {
-    uint32_t bits = 0u;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const uint4 c = K.block(make_uint4((cb >> 2) + (uint32_t)(4 * g + b), shot_lo, shot_hi, 1u));
-      const uint4 th = __ldg(t4 + 4 * g + b);
-      bits |= ((uint32_t)(c.x >= th.x) | ((uint32_t)(c.y >= th.y) << 1) | ((uint32_t)(c.z >= th.z) << 2) |
-               ((uint32_t)(c.w >= th.w) << 3)) << (4 * b);
-    }
-    m |= (unsigned long long)bits << (16 * g);
+  for (int b = 0; b < 8; ++b) {
+    const uint4 c = K.block(make_uint4((cb >> 2) + (uint32_t)b, shot_lo, shot_hi, 1u));
+    const uint4 th = __ldg(t4 + b);
+    if ((c.x >= th.x) | (c.y >= th.y) | (c.z >= th.z) | (c.w >= th.w))
+      m |= ((uint32_t)(c.x >= th.x) | ((uint32_t)(c.y >= th.y) << 1) | ((uint32_t)(c.z >= th.z) << 2) |
+            ((uint32_t)(c.w >= th.w) << 3)) << (4 * b);
   }
   return m;
 }
@@ -374,54 +409,96 @@ __device__ __forceinline__ void load_row(const uint32_t* p, uint32_t (&r)[N]) {
   }
 }
 
-// The descriptor is read once into registers: the byte stores of the records
-// could alias it, which would make every field a reload.
+// Registers hold what every measurement uses (header and row pointers, the
+// shot, delta); the arrays of the N1 paths are read from the descriptor when
+// a coin chunk or a fire needs them.  The next measurement's header and
+// factor half-row are loaded one iteration ahead.
+// Records are staged per warp in shared memory, rec[32][kRecStride] bytes
+// (row = lane, column = measurement mod 64; 17 words per row keep the lanes
+// on distinct banks), and every 64 measurements the warp writes each shot's
+// 64-byte run with contiguous byte stores: the group's rows are adjacent in
+// the output, so one store instruction covers one or two 32-byte sectors
+// instead of 32.
+constexpr int kRecWindow = 64;
+constexpr int kRecStride = 68;
+
+__device__ __forceinline__ void flush_records(const uint8_t* rec, uint8_t* __restrict__ g, int nmeas, int rows,
+                                              int k0, int cnt, int lane) {
+  __syncwarp();
+  for (int r = 0; r < rows; ++r) {
+    const uint8_t* b = rec + r * kRecStride;
+    uint8_t* o = g + (size_t)r * nmeas + k0;
+    if (lane < cnt) o[lane] = b[lane];
+    if (lane + 32 < cnt) o[lane + 32] = b[lane + 32];
+  }
+  __syncwarp();
+}
+
 template <int TW>
-__device__ __forceinline__ void phase_program(const TraceDesc& tdesc, long long group, int lane) {
-  const uint4* __restrict__ mhdr = tdesc.mhdr;
-  const uint32_t* __restrict__ mrow = tdesc.mrow;
-  const uint2* __restrict__ nhdr = tdesc.nhdr;
-  const uint32_t* __restrict__ nthr = tdesc.nthr;
-  const uint32_t* __restrict__ nrow = tdesc.nrow;
-  const int nm = tdesc.nm, wn = tdesc.wn, nmeas = tdesc.c.nmeas;
-  const uint32_t nn1 = (uint32_t)tdesc.nn1;
-  const unsigned long long seed = tdesc.c.seed;
+__device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp, long long group, int lane,
+                                              uint8_t* rec) {
+  constexpr int FH = TW / 2;  // factor words of a deterministic measurement
+  constexpr bool kAhead = FH <= 8;
+  const uint4* __restrict__ mhdr = tdp->mhdr;
+  const uint32_t* __restrict__ mrow = tdp->mrow;
+  const int nm = tdp->nm, wn = tdp->wn, nmeas = tdp->c.nmeas;
+  const uint32_t nn1 = (uint32_t)tdp->nn1;
+  const unsigned long long seed = tdp->c.seed;
   const long long rel = group * 32 + lane;
-  const bool active = rel < (long long)tdesc.c.nshots;
-  const long long shot = tdesc.c.shot0 + rel;
+  const bool active = rel < (long long)tdp->c.nshots;
+  const long long shot = tdp->c.shot0 + rel;
   const uint32_t shot_lo = (uint32_t)(unsigned long long)shot, shot_hi = (uint32_t)((unsigned long long)shot >> 32);
-  uint8_t* __restrict__ out = tdesc.c.out + (active ? rel : 0) * (long long)nmeas;
+  const long long first = group * 32;
+  const int rows = (int)min(32LL, (long long)tdp->c.nshots - first);  // shots of this group
+  uint8_t* __restrict__ gout = tdp->c.out + first * (long long)nmeas;
+  uint8_t* myrec = rec + lane * kRecStride;
   const PhiloxKeys K(seed);
   uint32_t d0[TW], d1[TW];
 #pragma unroll
   for (int w = 0; w < TW; ++w) d0[w] = d1[w] = 0u;
-  uint32_t nord = 0, cbase = 0xffffffffu;
-  unsigned long long fire = 0ull;
+  // N1 ordinals [nord, cend) of the current 32-ordinal chunk are not yet
+  // replayed; bit i of pend is ordinal nord + i.
+  uint32_t nord = 0, cend = 0, pend = 0u;
+  uint4 hn = make_uint4(0u, 0u, 0u, 0u);
+  uint32_t fn[FH];
+  if (nm > 0) {
+    hn = __ldg(mhdr);
+    if constexpr (kAhead) load_row<FH>(mrow, fn);
+  }
   for (int k = 0; k < nm; ++k) {
-    const uint4 h = __ldg(mhdr + k);
+    const uint4 h = hn;
+    uint32_t f[FH];
+    if constexpr (kAhead) {
+#pragma unroll
+      for (int w = 0; w < FH; ++w) f[w] = fn[w];
+      if (k + 1 < nm) {
+        hn = __ldg(mhdr + k + 1);
+        load_row<FH>(mrow + (size_t)(k + 1) * 2 * TW, fn);
+      }
+    } else {
+      if (k + 1 < nm) hn = __ldg(mhdr + k + 1);
+    }
     const uint32_t nend = h.z < nn1 ? h.z : nn1;
     while (nord < nend) {
-      const uint32_t cb = nord & ~63u;
-      if (cb != cbase) {
-        cbase = cb;
-        fire = coin_mask(K, nthr, cb, shot_lo, shot_hi);
+      if (nord == cend) {
+        pend = coin_mask(K, tdp->nthr, nord, shot_lo, shot_hi);
+        cend = nord + 32;
       }
-      const uint32_t hi = nend < cb + 64 ? nend : cb + 64;
-      unsigned long long m = fire >> (nord - cb);
-      if (hi - nord < 64) m &= (1ull << (hi - nord)) - 1ull;
-      if (!active) m = 0ull;
-      while (m) {
-        const uint32_t j = nord + (uint32_t)(__ffsll((long long)m) - 1);
-        m &= m - 1ull;
-        const uint2 nh = __ldg(nhdr + j);
+      const uint32_t hi = nend < cend ? nend : cend;
+      const uint32_t take = hi - nord;  // 1 .. 32
+      uint32_t due = take >= 32 ? pend : (pend & ((1u << take) - 1u));
+      pend = take >= 32 ? 0u : (pend >> take);
+      if (!active) due = 0u;
+      while (due) {
+        const uint32_t j = nord + (uint32_t)(__ffs(due) - 1);
+        due &= due - 1u;
+        const uint2 nh = __ldg(tdp->nhdr + j);
         if (nh.y == OP_N1OFF) continue;  // threshold 0xffffffff: a coin of 0xffffffff is not a fire
         const int2 ab = noise_choice(nh.y, 2, seed, shot, j);
         const uint32_t mz = ab.x ? 0xffffffffu : 0u, mx = (ab.y & 1) ? 0xffffffffu : 0u;
-        uint32_t xr[TW], zr[TW];
-        load_row<TW>(nrow + (size_t)j * 2 * TW, xr);
-        load_row<TW>(nrow + (size_t)j * 2 * TW + TW, zr);
+        const uint32_t* nr = tdp->nrow + (size_t)j * 2 * TW;
 #pragma unroll
-        for (int w = 0; w < TW; ++w) d1[w] ^= (zr[w] & mz) ^ (xr[w] & mx);
+        for (int w = 0; w < TW; ++w) d1[w] ^= (__ldg(nr + TW + w) & mz) ^ (__ldg(nr + w) & mx);
       }
       nord = hi;
     }
@@ -441,13 +518,12 @@ __device__ __forceinline__ void phase_program(const TraceDesc& tdesc, long long 
       const uint32_t dp0 = (a0 >> bp) & 1u, dp1 = (a1 >> bp) & 1u;
       if (dp0 | dp1) {
         const uint32_t m0 = 0u - dp0, m1 = 0u - dp1;
-        uint32_t F[TW];
-        load_row<TW>(row, F);
 #pragma unroll
         for (int w = 0; w < TW; ++w) {
-          const uint32_t lo = d0[w], a = F[w] & m0;
+          const uint32_t F = __ldg(row + w);
+          const uint32_t lo = d0[w], a = F & m0;
           d0[w] = lo ^ a;
-          d1[w] ^= (F[w] & m1) ^ (lo & a);
+          d1[w] ^= (F & m1) ^ (lo & a);
         }
       }
       m = active ? mulshift(K.block(make_uint4((uint32_t)k, shot_lo, shot_hi, 0u)).x, 2u) : 0;
@@ -463,20 +539,21 @@ __device__ __forceinline__ void phase_program(const TraceDesc& tdesc, long long 
         }
       }
     } else {
-      uint32_t f[TW / 2];
-      load_row<TW / 2>(row, f);
+      if constexpr (!kAhead) load_row<FH>(row, f);
       int sacc = 0;
 #pragma unroll
-      for (int w = 0; w < TW / 2; ++w) sacc += __popc(f[w] & d0[w]) + 2 * __popc(f[w] & d1[w]);
+      for (int w = 0; w < FH; ++w) sacc += __popc(f[w] & d0[w]) + 2 * __popc(f[w] & d1[w]);
       m = (((((int)h.w + sacc) & 3) + 1) >> 1) & 1;
     }
     if ((h.x & 2u) && (m & 1)) {
-      uint32_t z[TW];
-      load_row<TW>(row + TW, z);
 #pragma unroll
-      for (int w = 0; w < TW; ++w) d1[w] ^= z[w];
+      for (int w = 0; w < TW; ++w) d1[w] ^= __ldg(row + TW + w);
     }
-    if (active && k < nmeas) out[k] = (uint8_t)(m | (int)(det << 7));
+    myrec[k & (kRecWindow - 1)] = (uint8_t)(m | (int)(det << 7));
+    if ((k & (kRecWindow - 1)) == kRecWindow - 1 || k == nm - 1) {
+      const int k0 = k & ~(kRecWindow - 1);
+      flush_records(rec, gout, nmeas, rows, k0, min(k + 1, nmeas) - k0, lane);
+    }
   }
 }
 
