@@ -4,6 +4,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <climits>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -35,7 +37,9 @@ struct sdim_ctx {
   int64_t gmem_bytes = 0;
   size_t gmem_slot_budget = (size_t)8 << 30;
   std::string err;
-  DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace;
+  DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace, masks;
+  cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void* staging = nullptr;  // pinned host staging of sdim_run_tables
   size_t staging_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -51,8 +55,9 @@ struct sdim_ctx {
 
 // Where the trace schedule of a program sits in its blob (uint2 words).
 struct TraceSchedule {
-  int64_t steps_off = -1, lops_off = -1, wins_off = -1;
+  int64_t steps_off = -1, lops_off = -1, wins_off = -1, nthr_off = -1, nhdr_off = -1;
   int nsteps = 0, nwins = 0;
+  int nn1_used = 0;  // N1 ordinals before the last measurement (the only ones a record can see)
 };
 
 struct sdim_circuit {
@@ -70,7 +75,9 @@ struct sdim_circuit {
   const uint4* d_steps = nullptr;  // trace schedule (d = 2, n <= 512), inside the blob
   const uint4* d_lops = nullptr;
   const uint4* d_wins = nullptr;
-  int nsteps = 0, nwins = 0;
+  const uint32_t* d_nthr = nullptr;  // N1 coin thresholds, padded to a multiple of 64 with 0xffffffff
+  const uint2* d_nhdr = nullptr;     // N1 (threshold, opcode)
+  int nsteps = 0, nwins = 0, nn1_used = 0;
 };
 
 namespace {
@@ -313,8 +320,21 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
   }
   if ((rc = ensure(ctx, ctx->trace, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
   if ((rc = ensure(ctx, ctx->tdescs, sizeof(TraceDesc) * k)) != SDIM_OK) return rc;
+  // fire masks: one word per 32 N1 ordinals per shot, within a budget
+  constexpr size_t kMaskBudget = (size_t)1 << 30;
+  std::vector<size_t> moff(k, SIZE_MAX);
+  size_t mtotal = 0;
+  for (size_t i = 0; i < k; ++i) {
+    const size_t nchunk = ((size_t)jobs[i].c->nn1_used + kCoinChunk - 1) / kCoinChunk;
+    const size_t b = round_up(nchunk * (size_t)jobs[i].nshots * 4, 256);
+    if (nchunk && mtotal + b <= kMaskBudget) {
+      moff[i] = mtotal;
+      mtotal += b;
+    }
+  }
+  if (mtotal && (rc = ensure(ctx, ctx->masks, mtotal)) != SDIM_OK) return rc;
   std::vector<TraceDesc> hd(k);
-  long long groups = 0;
+  long long groups = 0, coins = 0;
   for (size_t i = 0; i < k; ++i) {
     const Job& j = jobs[i];
     const int tw = trace_words(j.c->n);
@@ -333,18 +353,24 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
     td.c.nshots = (int)j.nshots;
     groups += (j.nshots + 31) / 32;
     uint8_t* b = static_cast<uint8_t*>(ctx->trace.p) + off[i];
-    size_t o[6];
+    size_t o[4];
     trace_offsets(j.c->nmeas, j.c->nn1, tw, o);
     td.steps = j.c->d_steps;
     td.lops = j.c->d_lops;
     td.wins = j.c->d_wins;
+    td.nthr = j.c->d_nthr;
+    td.nhdr = j.c->d_nhdr;
     td.nsteps = j.c->nsteps;
     td.nwins = j.c->nwins;
     td.mhdr = reinterpret_cast<uint4*>(b + o[0]);
     td.mrow = reinterpret_cast<uint32_t*>(b + o[1]);
-    td.nhdr = reinterpret_cast<uint2*>(b + o[2]);
-    td.nthr = reinterpret_cast<uint32_t*>(b + o[3]);
-    td.nrow = reinterpret_cast<uint32_t*>(b + o[4]);
+    td.nrow = reinterpret_cast<uint32_t*>(b + o[2]);
+    td.coin_begin = coins;
+    if (moff[i] != SIZE_MAX) {
+      td.masks = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(ctx->masks.p) + moff[i]);
+      td.nchunk = (j.c->nn1_used + kCoinChunk - 1) / kCoinChunk;
+      coins += (long long)((td.nchunk + kCoinChunksPerItem - 1) / kCoinChunksPerItem) * j.nshots;
+    }
     td.nm = j.c->nmeas;
     td.nn1 = j.c->nn1;
     td.tw = tw;
@@ -352,6 +378,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
   }
   TraceDesc* dd = static_cast<TraceDesc*>(ctx->tdescs.p);
   CK(cudaMemcpyAsync(dd, hd.data(), sizeof(TraceDesc) * k, cudaMemcpyHostToDevice, s));
+  if (coins) CK(cudaEventRecord(ctx->ev_fork, s));
   // x / z pass: one CTA per program
   {
     const int nmax = jobs[k - 1].c->n;
@@ -368,6 +395,18 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
                       static_cast<uint8_t*>(ctx->gslots.p), xz, hot, in_smem ? 1 : 0, status);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
+  }
+  // coin pass on the second stream, alongside the x / z pass (independent work)
+  if (coins) {
+    CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
+    const int block = 256;
+    const long long grid = (coins + block - 1) / block;
+    if (grid > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one coin pass");
+    launch_coin_pass((int)grid, block, ctx->aux, dd, (int)k, coins);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "coin pass launch");
+    CK(cudaEventRecord(ctx->ev_join, ctx->aux));
+    CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
   }
   if (timed) CK(cudaEventRecord(ctx->ev_xz, s));
   // phase passes, one per row width
@@ -670,6 +709,26 @@ void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int 
   out.wins_off = put(wins);
   out.nsteps = (int)steps.size();
   out.nwins = (int)wins.size();
+  // N1 coin thresholds (dense, 64-ordinal padded, 16-byte aligned) and (threshold, opcode) pairs
+  std::vector<uint32_t> thr;
+  std::vector<uint2> hdr;
+  int used = 0;
+  for (size_t i = op_begin; i < op_begin + nops; ++i) {
+    const uint32_t op = dev[i].x & kOpMask;
+    if (op == OP_M || op == OP_RESET) used = (int)thr.size();
+    if (op == OP_N1D || op == OP_N1F || op == OP_N1P || op == OP_N1OFF) {
+      const uint32_t t = op == OP_N1OFF ? 0xffffffffu : dev[i].y;
+      thr.push_back(t);
+      hdr.push_back(make_uint2(t, op));
+    }
+  }
+  out.nn1_used = used;
+  while (thr.size() % 64) thr.push_back(0xffffffffu);
+  out.nthr_off = (int64_t)dev.size();
+  for (size_t i = 0; i < thr.size(); i += 2) dev.push_back(make_uint2(thr[i], thr[i + 1]));
+  out.nhdr_off = (int64_t)dev.size();
+  dev.insert(dev.end(), hdr.begin(), hdr.end());
+  if (dev.size() & 1) dev.push_back(make_uint2(0u, 0u));
 }
 
 }  // namespace
@@ -712,7 +771,10 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
-      cudaEventCreate(&ctx->ev_xz) != cudaSuccess || cudaEventCreate(&ctx->ev_phase) != cudaSuccess) {
+      cudaEventCreate(&ctx->ev_xz) != cudaSuccess || cudaEventCreate(&ctx->ev_phase) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return SDIM_ECUDA;
@@ -731,8 +793,9 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   if (!ctx) return SDIM_EINVAL;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  cudaStreamSynchronize(ctx->aux);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
-                    &ctx->tdescs, &ctx->trace};
+                    &ctx->tdescs, &ctx->trace, &ctx->masks};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);
@@ -740,6 +803,9 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaEventDestroy(ctx->ev1);
   cudaEventDestroy(ctx->ev_xz);
   cudaEventDestroy(ctx->ev_phase);
+  cudaEventDestroy(ctx->ev_fork);
+  cudaEventDestroy(ctx->ev_join);
+  cudaStreamDestroy(ctx->aux);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SDIM_OK;
@@ -823,8 +889,11 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
     c->d_steps = reinterpret_cast<const uint4*>(c->d_ops + sch.steps_off);
     c->d_lops = reinterpret_cast<const uint4*>(c->d_ops + sch.lops_off);
     c->d_wins = reinterpret_cast<const uint4*>(c->d_ops + sch.wins_off);
+    c->d_nthr = reinterpret_cast<const uint32_t*>(c->d_ops + sch.nthr_off);
+    c->d_nhdr = c->d_ops + sch.nhdr_off;
     c->nsteps = sch.nsteps;
     c->nwins = sch.nwins;
+    c->nn1_used = sch.nn1_used;
   }
   *out = c;
   return SDIM_OK;
@@ -1001,8 +1070,11 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
       circs[i].d_steps = reinterpret_cast<const uint4*>(base + sch[i].steps_off);
       circs[i].d_lops = reinterpret_cast<const uint4*>(base + sch[i].lops_off);
       circs[i].d_wins = reinterpret_cast<const uint4*>(base + sch[i].wins_off);
+      circs[i].d_nthr = reinterpret_cast<const uint32_t*>(base + sch[i].nthr_off);
+      circs[i].d_nhdr = base + sch[i].nhdr_off;
       circs[i].nsteps = sch[i].nsteps;
       circs[i].nwins = sch[i].nwins;
+      circs[i].nn1_used = sch[i].nn1_used;
     }
   }
   const bool on_dev = flags & SDIM_FLAG_OUT_DEVICE;

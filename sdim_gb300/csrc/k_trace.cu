@@ -41,7 +41,20 @@ __global__ void __launch_bounds__(32) k_phase_pass(const TraceDesc* __restrict__
   phase_program<TW>(descs + i, g - descs[i].c.item_begin, threadIdx.x, rec);
 }
 
+// One thread per (chunk group, shot) item of the coin pass; descs with
+// masks only, numbered through coin_begin.
+__global__ void __launch_bounds__(256) k_coin_pass(const TraceDesc* __restrict__ descs, int ndesc, long long total) {
+  const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= total) return;
+  const int i = find_coin_desc(descs, ndesc, it);
+  coin_item(descs + i, it - descs[i].coin_begin);
+}
+
 }  // namespace
+
+void launch_coin_pass(int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc, long long total) {
+  k_coin_pass<<<grid, block, 0, s>>>(descs, ndesc, total);
+}
 
 size_t trace_pass_hot_bytes(int n) { return round16(TraceTab::hot_bytes(n)); }
 size_t trace_pass_xz_bytes(int n) { return round16(TraceTab::xz_bytes(n)); }

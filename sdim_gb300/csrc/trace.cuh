@@ -20,49 +20,56 @@ namespace sdim {
 //   mrow[k][0][tw]: factor words -- random: x_q over the 2n generators with
 //     bit p cleared; deterministic: the destabilizer half of x_q (Wn words)
 //   mrow[k][1][tw]: z_q after the measurement (RESET only)
-//   nhdr[j] (N1 ordinal j): x = coin threshold, y = opcode
-//   nthr[j]: the coin threshold again, padded to a multiple of 64 ordinals
-//     with 0xffffffff, for the phase pass's 64-coin masks
-//   nrow[j][0][tw], nrow[j][1][tw]: x_q and z_q at the N1
-// Rows are tw words (a power of two >= 2 Wn), zero past 2 Wn.  The x / z
-// pass reads the program's layered schedule (steps, lops, windows; built by
-// the host encoder, see append_schedule in abi.cu).
+//   nrow[j][0][tw], nrow[j][1][tw]: x_q and z_q at N1 ordinal j
+// Rows are tw words (a power of two >= 2 Wn), zero past 2 Wn.  From the
+// program's blob (built by the host encoder, see append_schedule in abi.cu):
+// the layered schedule the x / z pass walks (steps, lops, wins), the N1
+// coin thresholds nthr[j] (padded to a multiple of 64 ordinals with
+// 0xffffffff) and nhdr[j] = (threshold, opcode).  masks, when not null,
+// holds the fire bits of every shot, masks[c * nshots + s] bit i = N1
+// ordinal 32 c + i of shot s fired, written by the coin pass.
 struct TraceDesc {
   CircuitDesc c;  // item_begin counts 32-shot groups of the phase pass
   const uint4* steps;
   const uint4* lops;
   const uint4* wins;
+  const uint32_t* nthr;
+  const uint2* nhdr;
   uint4* mhdr;
   uint32_t* mrow;
-  uint2* nhdr;
-  uint32_t* nthr;
   uint32_t* nrow;
+  uint32_t* masks;
+  long long coin_begin;  // first coin-pass item of this program
   int nsteps;
   int nwins;
-  int nm;   // measurements (M and RESET)
-  int nn1;  // N1 ordinals
-  int tw;   // words per trace row
-  int wn;   // words per generator half
+  int nm;      // measurements (M and RESET)
+  int nn1;     // N1 ordinals
+  int nchunk;  // 32-ordinal chunks of fire masks (those before the last measurement)
+  int tw;      // words per trace row
+  int wn;      // words per generator half
 };
 
 __host__ __device__ inline size_t round_up(size_t b, size_t a) { return (b + a - 1) / a * a; }
 
 // Byte offsets of the trace arrays inside one program's trace (each array
-// 256-byte aligned); o[5] is the total.
-__host__ __device__ inline void trace_offsets(int nm, int nn1, int tw, size_t o[6]) {
-  o[0] = 0;                                                        // mhdr
-  o[1] = o[0] + round_up((size_t)nm * 16, 256);                    // mrow
-  o[2] = o[1] + round_up((size_t)nm * 8 * tw, 256);                // nhdr
-  o[3] = o[2] + round_up((size_t)nn1 * 8, 256);                    // nthr
-  o[4] = o[3] + round_up(round_up((size_t)nn1, 64) * 4, 256);      // nrow
-  o[5] = o[4] + round_up((size_t)nn1 * 8 * tw, 256);
+// 256-byte aligned); o[3] is the total.
+__host__ __device__ inline void trace_offsets(int nm, int nn1, int tw, size_t o[4]) {
+  o[0] = 0;                                                  // mhdr
+  o[1] = o[0] + round_up((size_t)nm * 16, 256);              // mrow
+  o[2] = o[1] + round_up((size_t)nm * 8 * tw, 256);          // nrow
+  o[3] = o[2] + round_up((size_t)nn1 * 8 * tw, 256);
 }
 
 __host__ __device__ inline size_t trace_bytes(int nm, int nn1, int tw) {
-  size_t o[6];
+  size_t o[4];
   trace_offsets(nm, nn1, tw, o);
-  return o[5];
+  return o[3];
 }
+
+// Chunks of 32 N1 ordinals of one shot's fire mask.
+constexpr int kCoinChunk = 32;
+// Chunks one coin-pass thread fills.
+constexpr int kCoinChunksPerItem = 8;
 
 // Widest trace row the phase pass has an instance for (n <= 512).
 constexpr int kTraceMaxWords = 32;
@@ -95,6 +102,10 @@ cudaError_t trace_set_smem(int optin);
 // shared memory when xz_in_smem, else at gxz + blockIdx.x * xz_bytes.
 void launch_trace_pass(int threads, int grid, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        uint8_t* gxz, size_t xz_bytes, size_t hot_bytes, int xz_in_smem, int* status);
+
+// Coin pass: the fire masks of every program of descs with masks (items:
+// (chunk group, shot) pairs numbered through coin_begin).
+void launch_coin_pass(int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc, long long total);
 
 // Phase pass: one lane per shot, one warp per 32-shot group; every program of
 // descs has trace rows of tw words.  Returns false for an unsupported tw.

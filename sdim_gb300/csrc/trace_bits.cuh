@@ -113,16 +113,10 @@ __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, con
         atomicCAS(status, DEV_OK, DEV_SLOT_TOO_SMALL);
         return;
       }
-      const bool off = op == OP_N1OFF;
-      if (!off) {
+      if (op != OP_N1OFF) {
         uint32_t* dst = td.nrow + (size_t)j * 2 * tw;
         dst[w] = in ? xr[w] : 0u;
         dst[tw + w] = in ? zr[w] : 0u;
-      }
-      if (w == 0) {
-        const uint32_t thr = off ? 0xffffffffu : lo.y;
-        td.nhdr[j] = make_uint2(thr, op);
-        td.nthr[j] = thr;
       }
       break;
     }
@@ -337,8 +331,6 @@ __device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int*
     }
     e.tm.sync();
   }
-  const int pad = (int)round_up((size_t)td.nn1, 64);
-  for (int j = td.nn1 + t; j < pad; j += size) td.nthr[j] = 0xffffffffu;
   e.tm.sync();
 }
 
@@ -457,8 +449,14 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
 #pragma unroll
   for (int w = 0; w < TW; ++w) d0[w] = d1[w] = 0u;
   // N1 ordinals [nord, cend) of the current 32-ordinal chunk are not yet
-  // replayed; bit i of pend is ordinal nord + i.
+  // replayed; bit i of pend is ordinal nord + i.  With coin-pass masks the
+  // next chunk's word is loaded one chunk ahead.
   uint32_t nord = 0, cend = 0, pend = 0u;
+  const uint32_t* __restrict__ masks = tdp->masks;
+  const int nchunk = tdp->nchunk;
+  const int nshots = tdp->c.nshots;
+  uint32_t pnext = 0u;
+  if (masks && active && nchunk > 0) pnext = __ldg(masks + rel);
   uint4 hn = make_uint4(0u, 0u, 0u, 0u);
   uint32_t fn[FH];
   if (nm > 0) {
@@ -481,7 +479,13 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
     const uint32_t nend = h.z < nn1 ? h.z : nn1;
     while (nord < nend) {
       if (nord == cend) {
-        pend = coin_mask(K, tdp->nthr, nord, shot_lo, shot_hi);
+        if (masks) {
+          const int c = (int)(nord >> 5);
+          pend = pnext;
+          pnext = (active && c + 1 < nchunk) ? __ldg(masks + (size_t)(c + 1) * nshots + rel) : 0u;
+        } else {
+          pend = coin_mask(K, tdp->nthr, nord, shot_lo, shot_hi);
+        }
         cend = nord + 32;
       }
       const uint32_t hi = nend < cend ? nend : cend;
@@ -555,6 +559,32 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
       flush_records(rec, gout, nmeas, rows, k0, min(k + 1, nmeas) - k0, lane);
     }
   }
+}
+
+// Coin pass item it of td: shot it % nshots, chunks kCoinChunksPerItem *
+// (it / nshots) onwards.
+__device__ __forceinline__ void coin_item(const TraceDesc* __restrict__ tdp, long long it) {
+  const int nshots = tdp->c.nshots;
+  const long long cg = it / nshots;
+  const int rel = (int)(it - cg * nshots);
+  const unsigned long long shot = (unsigned long long)(tdp->c.shot0 + rel);
+  const PhiloxKeys K(tdp->c.seed);
+  const uint32_t* nthr = tdp->nthr;
+  uint32_t* out = tdp->masks + rel;
+  const int nchunk = tdp->nchunk;
+  const int c0 = (int)cg * kCoinChunksPerItem;
+  const int c1 = min(nchunk, c0 + kCoinChunksPerItem);
+  for (int c = c0; c < c1; ++c)
+    out[(size_t)c * nshots] = coin_mask(K, nthr, (uint32_t)c * kCoinChunk, (uint32_t)shot, (uint32_t)(shot >> 32));
+}
+
+__device__ __forceinline__ int find_coin_desc(const TraceDesc* descs, int ndesc, long long it) {
+  int lo = 0, hi = ndesc - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (descs[mid].coin_begin <= it) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 __device__ __forceinline__ int find_trace_desc(const TraceDesc* descs, int ndesc, long long it) {
