@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-shots", type=int, default=256)
+    ap.add_argument("--quick", action="store_true",
+                    help="single-program workloads: time the selected engine only (for profiling runs)")
     ap.add_argument("--engine", default="auto", choices=["auto", "trace", "group", "per_shot"],
                     help="batched engine of the timed run (auto: the library's choice)")
     return ap.parse_args()
@@ -301,6 +303,26 @@ def run_reference_arm(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
+TRACE_MIN_SHOTS = 64  # the library's default switch to the trace engine (d = 2)
+
+
+def trace_words(n):
+    """Words per trace row of the d = 2 trace engine (0: n too large)."""
+    w2 = 2 * ((n + 31) // 32)
+    tw = 2
+    while tw < w2:
+        tw *= 2
+    return tw if tw <= 32 else 0
+
+
+def philox_peak(ctx):
+    import ctypes
+    from sdim_gb300 import _lib
+    v = ctypes.c_double()
+    _lib.check(ctx.lib.sdim_probe_philox_rate(ctx.ptr, ctypes.byref(v)), ctx.ptr, "philox probe")
+    return v.value
+
+
 def smem_peak(ctx):
     import ctypes
     from sdim_gb300 import _lib
@@ -385,18 +407,13 @@ def run_single(args, torch, dist, ws, rank, local):
     timer = Timer(torch, stream, ctx, ws, dist)
 
     engine_flags = _lib.engine_flags(None if args.engine == "auto" else args.engine)
+    trace_used = (d == 2 and trace_words(n) > 0 and
+                  (args.engine == "trace" or (args.engine == "auto" and shots >= TRACE_MIN_SHOTS)))
 
     def step(extra=None):
         rc = ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 0, shot0, shots, out.data_ptr(), stream.cuda_stream,
                                      _lib.FLAG_ASYNC | _lib.FLAG_TIME | (engine_flags if extra is None else extra))
         _lib.check(rc, ctx.ptr, "run")
-
-    # per-shot engine (one warp, one full tableau per shot) on the same inputs
-    step(_lib.FLAG_PER_SHOT)
-    ctx.sync()
-    ps_steps = 2
-    ps_step_ms, ps_kern_ms, _ = timer.run(ps_steps, lambda: step(_lib.FLAG_PER_SHOT))
-    ps_records = out[:64, :nrec].cpu().numpy()
 
     for _ in range(args.warmup):
         step()
@@ -406,10 +423,29 @@ def run_single(args, torch, dist, ws, rank, local):
     total_ms = timer.max_over_ranks(sum(step_ms))
     units_per_step = len(spec.ops) * shots
     value = units_per_step * ws * args.steps / (total_ms / 1e3)
-
     rec = out[:64, :nrec].cpu().numpy()
+    if args.quick:
+        # the timed engine only (profiling runs): no comparison engines, no CPU leg
+        return None if rank else {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 bit planes (d=2) / u8 residues (odd d)",
+            "data": "synthetic (seeded circuit generator, Philox outcome and noise stream)",
+            "config": {"workload": desc, "shots_per_gpu": shots, "mode": "quick: timed engine only"},
+            "engine": args.engine, "kernel_ms": statistics.mean(kern_ms),
+            "stages_ms": {"xz_pass": stages[0], "phase_pass": stages[1], "other_engines": stages[2]},
+            "gpu_launches": args.steps, "clocks": clk}
+
+    # per-shot engine (one warp, one full tableau per shot) on the same inputs
+    step(_lib.FLAG_PER_SHOT)
+    ctx.sync()
+    ps_steps = 2
+    ps_step_ms, ps_kern_ms, _ = timer.run(ps_steps, lambda: step(_lib.FLAG_PER_SHOT))
+    ps_records = out[:64, :nrec].cpu().numpy()
     if not np.array_equal(rec, ps_records):
         raise AssertionError("batched and per-shot engines disagree")
+    step()
+    ctx.sync()
     full = out[:, :nrec].cpu().numpy()
     engines = {}
     if d == 2:
@@ -477,6 +513,40 @@ def run_single(args, torch, dist, ws, rank, local):
                                                               f"<TGroupU8<{d}>>")
     if d == 2 and n >= 160:
         kernel = "k_group_cta<TGroupBits<CtaTeam>>"
+    group_model = {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                   "kernel": kernel,
+                   "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth",
+                   "algorithmic_bytes_per_launch": gbytes,
+                   "bytes_model": "x/z rows + common phase once per 32-shot group (per-shot tableau figures), "
+                                  "plus each shot's phase-delta rows at measurements and RESET corrections",
+                   "per_shot_equivalent_GBps": per_shot_bytes * shots / (mean_kern / 1e3) / 1e9,
+                   "hbm_peak_gbs": hbm_peak(), "kernel_ms": mean_kern}
+    if trace_used:
+        # the step cannot outrun drawing its random numbers: one Philox4x32-10
+        # block per 4 N1 ordinals before the last measurement and one per
+        # random measurement, per shot
+        gids = enc.ops[:, 0]
+        meas_at = np.nonzero(np.isin(gids, (14, 15, 16)))[0]
+        nn1_used = int((gids[:meas_at[-1]] == 17).sum()) if len(meas_at) else 0
+        n_random = int((~det_row).sum())
+        blocks = shots * (-(-nn1_used // 4) + n_random)
+        prate = philox_peak(ctx)
+        ach = blocks / (mean_kern / 1e3)
+        roofline = {"bound": "int-multiply (Philox4x32-10 blocks)", "achieved": ach / 1e9, "peak": prate / 1e9,
+                    "unit": "Gblock/s", "frac": ach / prate,
+                    "traffic": read_traffic("trace_engine_surface_L7.md") if args.workload == "surface" else None,
+                    "kernel": "trace engine step: k_trace_pass (x/z, 1 CTA) alongside k_coin_pass, then "
+                              f"k_phase_pass<{trace_words(n)}>",
+                    "peak_source": "Philox throughput measured live by sdim_probe_philox_rate",
+                    "algorithmic_blocks_per_launch": blocks,
+                    "blocks_model": f"per shot ceil({nn1_used} N1 ordinals / 4) coin blocks + {n_random} "
+                                    "random-outcome blocks",
+                    "kernel_ms": mean_kern,
+                    "stages_ms": {"xz_pass_and_coin_pass": stages[0], "phase_pass": stages[1]},
+                    "group_engine_model": group_model}
+    else:
+        roofline = dict(group_model)
+        roofline["traffic"] = None
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -498,18 +568,9 @@ def run_single(args, torch, dist, ws, rank, local):
             "form": "persistent kernel, one warp and one full tableau per shot", "kernel_ms": ps_kern,
             "roofline": {"bound": "smem", "achieved": ps_achieved, "peak": peak, "unit": "GB/s",
                          "frac": ps_achieved / peak, "algorithmic_bytes_per_shot": per_shot_bytes}},
-        "roofline": {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": read_traffic("k_group_persistent_bits_surface_L7.md") if args.workload == "surface"
-                     else None,
-                     "kernel": kernel,
-                     "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth",
-                     "algorithmic_bytes_per_launch": gbytes,
-                     "bytes_model": "x/z rows + common phase once per 32-shot group (per-shot tableau figures), "
-                                    "plus each shot's phase-delta rows at measurements and RESET corrections",
-                     "per_shot_equivalent_GBps": per_shot_bytes * shots / (mean_kern / 1e3) / 1e9,
-                     "hbm_peak_gbs": hbm_peak(), "kernel_ms": mean_kern},
+        "roofline": roofline,
         "cpu_baseline": cpu,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (3 if trace_used else 1),
         "clocks": clk,
         "engine": args.engine,
         "stages_ms": {"xz_pass": stages[0], "phase_pass": stages[1], "other_engines": stages[2]},

@@ -49,6 +49,7 @@ extern "C" {
 #define SDIM_FLAG_TRACE 256u     /* d = 2: trace engine (one x / z pass per program, one lane per shot)
                                     whatever the shot count; by default it runs from 64 shots */
 #define SDIM_FLAG_NO_TRACE 512u  /* d = 2: shot-group engine only */
+#define SDIM_FLAG_NO_COIN_PASS 1024u /* trace engine: draw N1 coins inside the phase pass, no coin pass */
 
 /* snapshot modes for sdim_snapshot */
 #define SDIM_SNAP_EVERY_INSTRUCTION 1
@@ -125,6 +126,11 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
  * the roofline denominator for tableaux resident in shared memory.  No
  * counterpart in the reference (which has no device code). */
 int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs);
+/* Philox4x32-10 blocks per second the device draws at most (eight
+ * independent chains per thread, keys per thread, as the trace engine's coin
+ * pass draws them): the compute roofline of sampling N1 coins.  No
+ * counterpart in the reference. */
+int sdim_probe_philox_rate(sdim_ctx* ctx, double* blocks_per_s);
 /* Waits for the context's last launch stream and reports a device-side
  * error, if any.  With SDIM_FLAG_ASYNC, sdim_run_batch with host outputs
  * returns after queueing the kernels and the record copies; the host buffers

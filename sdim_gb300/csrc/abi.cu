@@ -326,8 +326,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
   size_t mtotal = 0;
   for (size_t i = 0; i < k; ++i) {
     const size_t nchunk = ((size_t)jobs[i].c->nn1_used + kCoinChunk - 1) / kCoinChunk;
-    const size_t b = round_up(nchunk * (size_t)jobs[i].nshots * 4, 256);
-    if (nchunk && mtotal + b <= kMaskBudget) {
+    const size_t b = round_up(nchunk * (size_t)jobs[i].nshots * 8, 256);
+    if (nchunk && mtotal + b <= kMaskBudget && !(flags & SDIM_FLAG_NO_COIN_PASS)) {
       moff[i] = mtotal;
       mtotal += b;
     }
@@ -751,6 +751,29 @@ int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   *gbs = (double)blocks * threads * iters * 16.0 / (ms * 1e-3) / 1e9;
+  return SDIM_OK;
+}
+
+int sdim_probe_philox_rate(sdim_ctx* ctx, double* blocks_per_s) {
+  if (!ctx || !blocks_per_s) return fail(ctx, SDIM_EINVAL, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  int rc = ensure(ctx, ctx->snap, 256 * sizeof(unsigned long long) + 256 * sizeof(uint4));
+  if (rc != SDIM_OK) return rc;
+  unsigned long long seeds[256];
+  for (int i = 0; i < 256; ++i) seeds[i] = 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1);
+  unsigned long long* dseeds = static_cast<unsigned long long*>(ctx->snap.p);
+  uint4* sink = reinterpret_cast<uint4*>(dseeds + 256);
+  CK(cudaMemcpyAsync(dseeds, seeds, sizeof(seeds), cudaMemcpyHostToDevice, ctx->stream));
+  const int grid = 8 * ctx->num_sms, iters = 256;
+  launch_philox_probe(grid, ctx->stream, dseeds, 8, sink);  // warm-up
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  launch_philox_probe(grid, ctx->stream, dseeds, iters, sink);
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *blocks_per_s = (double)grid * 256.0 * iters * 8.0 / (ms * 1e-3);
   return SDIM_OK;
 }
 

@@ -50,7 +50,32 @@ __global__ void __launch_bounds__(256) k_coin_pass(const TraceDesc* __restrict__
   coin_item(descs + i, it - descs[i].coin_begin);
 }
 
+// Philox throughput probe: every thread draws iters x 8 blocks (eight
+// independent chains per step, as the coin pass does) under a key loaded per
+// thread, and folds them so the work stays live.
+__global__ void __launch_bounds__(256) k_philox_probe(const unsigned long long* __restrict__ seeds, int iters,
+                                                      uint4* sink) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const PhiloxKeys K(seeds[t & 255]);
+  uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const uint4 c = K.block(make_uint4((uint32_t)(it * 8 + b), (uint32_t)t, 0u, 1u));
+      acc.x ^= c.x;
+      acc.y ^= c.y;
+      acc.z ^= c.z;
+      acc.w ^= c.w;
+    }
+  }
+  if ((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9e3779b9u) sink[t & 255] = acc;
+}
+
 }  // namespace
+
+void launch_philox_probe(int grid, cudaStream_t s, const unsigned long long* seeds, int iters, uint4* sink) {
+  k_philox_probe<<<grid, 256, 0, s>>>(seeds, iters, sink);
+}
 
 void launch_coin_pass(int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc, long long total) {
   k_coin_pass<<<grid, block, 0, s>>>(descs, ndesc, total);

@@ -26,8 +26,9 @@ namespace sdim {
 // the layered schedule the x / z pass walks (steps, lops, wins), the N1
 // coin thresholds nthr[j] (padded to a multiple of 64 ordinals with
 // 0xffffffff) and nhdr[j] = (threshold, opcode).  masks, when not null,
-// holds the fire bits of every shot, masks[c * nshots + s] bit i = N1
-// ordinal 32 c + i of shot s fired, written by the coin pass.
+// holds the fired Paulis of every shot as word pairs, pair c * nshots + s:
+// bit i of the first word = N1 ordinal 32 c + i of shot s applied X^a with
+// a odd, of the second = Z^b with b odd (written by the coin pass).
 struct TraceDesc {
   CircuitDesc c;  // item_begin counts 32-shot groups of the phase pass
   const uint4* steps;
@@ -102,6 +103,10 @@ cudaError_t trace_set_smem(int optin);
 // shared memory when xz_in_smem, else at gxz + blockIdx.x * xz_bytes.
 void launch_trace_pass(int threads, int grid, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        uint8_t* gxz, size_t xz_bytes, size_t hot_bytes, int xz_in_smem, int* status);
+
+// Philox4x32-10 throughput probe: grid blocks of 256 threads, each drawing
+// iters x 8 blocks keyed by seeds[thread % 256]; results folded into sink[256].
+void launch_philox_probe(int grid, cudaStream_t s, const unsigned long long* seeds, int iters, uint4* sink);
 
 // Coin pass: the fire masks of every program of descs with masks (items:
 // (chunk group, shot) pairs numbered through coin_begin).

@@ -451,12 +451,15 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
   // N1 ordinals [nord, cend) of the current 32-ordinal chunk are not yet
   // replayed; bit i of pend is ordinal nord + i.  With coin-pass masks the
   // next chunk's word is loaded one chunk ahead.
-  uint32_t nord = 0, cend = 0, pend = 0u;
-  const uint32_t* __restrict__ masks = tdp->masks;
+  uint32_t nord = 0, cend = 0, pend = 0u, pendz = 0u;
+  const uint2* __restrict__ masks = reinterpret_cast<const uint2*>(tdp->masks);
   const int nchunk = tdp->nchunk;
   const int nshots = tdp->c.nshots;
-  uint32_t pnext = 0u;
-  if (masks && active && nchunk > 0) pnext = __ldg(masks + rel);
+  uint2 q1 = make_uint2(0u, 0u), q2 = make_uint2(0u, 0u);  // masks of the next two chunks
+  if (masks && active) {
+    if (nchunk > 0) q1 = __ldg(masks + rel);
+    if (nchunk > 1) q2 = __ldg(masks + (size_t)nshots + rel);
+  }
   uint4 hn = make_uint4(0u, 0u, 0u, 0u);
   uint32_t fn[FH];
   if (nm > 0) {
@@ -481,25 +484,40 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
       if (nord == cend) {
         if (masks) {
           const int c = (int)(nord >> 5);
-          pend = pnext;
-          pnext = (active && c + 1 < nchunk) ? __ldg(masks + (size_t)(c + 1) * nshots + rel) : 0u;
+          pend = q1.x;
+          pendz = q1.y;
+          q1 = q2;
+          q2 = (active && c + 2 < nchunk) ? __ldg(masks + (size_t)(c + 2) * nshots + rel) : make_uint2(0u, 0u);
         } else {
+          // no masks: draw the coins here, the Paulis on a fire below
           pend = coin_mask(K, tdp->nthr, nord, shot_lo, shot_hi);
+          pendz = 0xffffffffu;
         }
         cend = nord + 32;
       }
       const uint32_t hi = nend < cend ? nend : cend;
       const uint32_t take = hi - nord;  // 1 .. 32
-      uint32_t due = take >= 32 ? pend : (pend & ((1u << take) - 1u));
+      const uint32_t lim = take >= 32 ? 0xffffffffu : ((1u << take) - 1u);
+      uint32_t due = masks ? ((pend | pendz) & lim) : (pend & lim);
+      const uint32_t ax = pend, bz = pendz;
       pend = take >= 32 ? 0u : (pend >> take);
+      pendz = take >= 32 ? 0u : (pendz >> take);
       if (!active) due = 0u;
       while (due) {
-        const uint32_t j = nord + (uint32_t)(__ffs(due) - 1);
+        const int i = __ffs(due) - 1;
         due &= due - 1u;
-        const uint2 nh = __ldg(tdp->nhdr + j);
-        if (nh.y == OP_N1OFF) continue;  // threshold 0xffffffff: a coin of 0xffffffff is not a fire
-        const int2 ab = noise_choice(nh.y, 2, seed, shot, j);
-        const uint32_t mz = ab.x ? 0xffffffffu : 0u, mx = (ab.y & 1) ? 0xffffffffu : 0u;
+        const uint32_t j = nord + (uint32_t)i;
+        uint32_t mz, mx;
+        if (masks) {
+          mz = ((ax >> i) & 1u) ? 0xffffffffu : 0u;
+          mx = ((bz >> i) & 1u) ? 0xffffffffu : 0u;
+        } else {
+          const uint2 nh = __ldg(tdp->nhdr + j);
+          if (nh.y == OP_N1OFF) continue;  // threshold 0xffffffff: a coin of 0xffffffff is not a fire
+          const int2 ab = noise_choice(nh.y, 2, seed, shot, j);
+          mz = ab.x ? 0xffffffffu : 0u;
+          mx = (ab.y & 1) ? 0xffffffffu : 0u;
+        }
         const uint32_t* nr = tdp->nrow + (size_t)j * 2 * TW;
 #pragma unroll
         for (int w = 0; w < TW; ++w) d1[w] ^= (__ldg(nr + TW + w) & mz) ^ (__ldg(nr + w) & mx);
@@ -562,20 +580,37 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
 }
 
 // Coin pass item it of td: shot it % nshots, chunks kCoinChunksPerItem *
-// (it / nshots) onwards.
+// (it / nshots) onwards.  For every fired N1 (rare) the Pauli is drawn here,
+// so masks[c * nshots + s] = (x mask, z mask): bit i of .x set when ordinal
+// 32 c + i applies X^a with a odd (the phase update reads z_q), of .y when it
+// applies Z^b with b odd (reads x_q); an N1 with probability 0 never fires.
 __device__ __forceinline__ void coin_item(const TraceDesc* __restrict__ tdp, long long it) {
   const int nshots = tdp->c.nshots;
   const long long cg = it / nshots;
   const int rel = (int)(it - cg * nshots);
-  const unsigned long long shot = (unsigned long long)(tdp->c.shot0 + rel);
-  const PhiloxKeys K(tdp->c.seed);
+  const long long shot = tdp->c.shot0 + rel;
+  const unsigned long long seed = tdp->c.seed;
+  const PhiloxKeys K(seed);
   const uint32_t* nthr = tdp->nthr;
-  uint32_t* out = tdp->masks + rel;
+  uint2* out = reinterpret_cast<uint2*>(tdp->masks) + rel;
   const int nchunk = tdp->nchunk;
   const int c0 = (int)cg * kCoinChunksPerItem;
   const int c1 = min(nchunk, c0 + kCoinChunksPerItem);
-  for (int c = c0; c < c1; ++c)
-    out[(size_t)c * nshots] = coin_mask(K, nthr, (uint32_t)c * kCoinChunk, (uint32_t)shot, (uint32_t)(shot >> 32));
+  for (int c = c0; c < c1; ++c) {
+    const uint32_t cb = (uint32_t)c * kCoinChunk;
+    uint32_t f = coin_mask(K, nthr, cb, (uint32_t)(unsigned long long)shot, (uint32_t)((unsigned long long)shot >> 32));
+    uint32_t ax = 0u, bz = 0u;
+    while (f) {
+      const int i = __ffs(f) - 1;
+      f &= f - 1u;
+      const uint2 nh = __ldg(tdp->nhdr + cb + i);
+      if (nh.y == OP_N1OFF) continue;  // threshold 0xffffffff: a coin of 0xffffffff is not a fire
+      const int2 ab = noise_choice(nh.y, 2, seed, shot, cb + i);
+      ax |= (uint32_t)(ab.x & 1) << i;
+      bz |= (uint32_t)(ab.y & 1) << i;
+    }
+    out[(size_t)c * nshots] = make_uint2(ax, bz);
+  }
 }
 
 __device__ __forceinline__ int find_coin_desc(const TraceDesc* descs, int ndesc, long long it) {

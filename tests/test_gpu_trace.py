@@ -80,6 +80,21 @@ def test_mixed_batch_routes_each_program():
     assert np.array_equal(outs[3], alone)
 
 
+@pytest.mark.parametrize("prob", [1e-3, 0.05, 0.5])
+def test_coins_in_the_phase_pass_match_the_coin_pass(prob):
+    """SDIM_FLAG_NO_COIN_PASS draws the N1 coins inside the phase pass; both
+    paths give the oracle's records."""
+    spec = workloads.surface_memory(5, 3, prob=prob)
+    prog = Program(spec.build())
+    dp = prog.compile(True)
+    ctx = prog.context
+    out = np.empty((130, dp.num_records), dtype=np.uint8)
+    rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 12, 7, 130, out.ctypes.data, _lib.FLAG_TRACE | _lib.FLAG_NO_COIN_PASS)
+    _lib.check(rc, ctx.ptr, "trace without coin pass")
+    assert np.array_equal(out, prog.sample(130, seed=12, shot0=7, engine="trace"))
+    assert np.array_equal(out, oracle_run([spec], 12, 7, 130)["records"])
+
+
 def test_xz_pass_in_global_memory():
     spec = workloads.random_hpc(300, 2, 1200, seed=31, mr_every=150, mr_fraction=0.2)
     prog = Program(spec.build())
