@@ -37,7 +37,7 @@ struct sdim_ctx {
   int64_t gmem_bytes = 0;
   size_t gmem_slot_budget = (size_t)8 << 30;
   std::string err;
-  DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace, masks;
+  DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace, masks, tdescs_u8, trace_u8, xz_u8;
   cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void* staging = nullptr;  // pinned host staging of sdim_run_tables
@@ -289,13 +289,28 @@ bool use_trace(const Job& j, unsigned flags) {
   return (flags & SDIM_FLAG_TRACE) || j.nshots >= kTraceMinShots;
 }
 
-// Trace-engine launches for jobs (all use_trace): the x / z pass of every
-// program (warp teams below kCtaTeamQudits qudits, CTA teams above), then one
-// phase pass per trace-row width.  Programs are ordered by n, which orders
-// both the team split and the row widths.
-int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsigned flags, int* status) {
+// Odd-d programs above this many qudits stay on the shot-group engine (the
+// phase pass keeps 32 shots' deltas in shared memory).
+constexpr int kTraceU8MaxQudits = 2048;
+
+// Jobs for the odd-d trace engine: same rule with d odd.
+bool use_trace_u8(const Job& j, unsigned flags) {
+  if (flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT | SDIM_FLAG_TEAM_WARP | SDIM_FLAG_TEAM_CTA |
+               SDIM_FLAG_NO_TRACE))
+    return false;
+  if (j.c->d == 2 || j.c->n > kTraceU8MaxQudits || j.nshots <= 0) return false;
+  return (flags & SDIM_FLAG_TRACE) || j.nshots >= kTraceMinShots;
+}
+
+// Trace-engine launches: the x / z pass of every program (d = 2 jobs, then
+// odd-d jobs per variant of d), the coin pass of the d = 2 jobs alongside on
+// the second stream, then the phase passes (d = 2 per trace-row width, odd
+// d per variant).  d = 2 programs are ordered by n, which orders the row
+// widths; odd-d programs by (variant, n).
+int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujobs, cudaStream_t s, unsigned flags,
+                      int* status) {
   const bool timed = flags & SDIM_FLAG_TIME;
-  if (jobs.empty()) {
+  if (jobs.empty() && ujobs.empty()) {
     if (timed) {
       CK(cudaEventRecord(ctx->ev_xz, s));
       CK(cudaEventRecord(ctx->ev_phase, s));
@@ -306,81 +321,137 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
   int rc;
   if (!ctx->trace_smem_set) {
-    const cudaError_t e = trace_set_smem(ctx->smem_optin);
+    cudaError_t e = trace_set_smem(ctx->smem_optin);
+    if (e == cudaSuccess) e = trace_u8_set_smem(ctx->smem_optin);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFuncSetAttribute");
     ctx->trace_smem_set = true;
   }
+  // ---- d = 2 descriptors
   std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& b) { return a.c->n < b.c->n; });
   const size_t k = jobs.size();
-  std::vector<size_t> off(k);
-  size_t total = 0;
-  for (size_t i = 0; i < k; ++i) {
-    off[i] = total;
-    total += trace_bytes(jobs[i].c->nmeas, jobs[i].c->nn1, trace_words(jobs[i].c->n));
-  }
-  if ((rc = ensure(ctx, ctx->trace, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
-  if ((rc = ensure(ctx, ctx->tdescs, sizeof(TraceDesc) * k)) != SDIM_OK) return rc;
-  // fire masks: one word per 32 N1 ordinals per shot, within a budget
-  constexpr size_t kMaskBudget = (size_t)1 << 30;
-  std::vector<size_t> moff(k, SIZE_MAX);
-  size_t mtotal = 0;
-  for (size_t i = 0; i < k; ++i) {
-    const size_t nchunk = ((size_t)jobs[i].c->nn1_used + kCoinChunk - 1) / kCoinChunk;
-    const size_t b = round_up(nchunk * (size_t)jobs[i].nshots * 8, 256);
-    if (nchunk && mtotal + b <= kMaskBudget && !(flags & SDIM_FLAG_NO_COIN_PASS)) {
-      moff[i] = mtotal;
-      mtotal += b;
-    }
-  }
-  if (mtotal && (rc = ensure(ctx, ctx->masks, mtotal)) != SDIM_OK) return rc;
   std::vector<TraceDesc> hd(k);
-  long long groups = 0, coins = 0;
-  for (size_t i = 0; i < k; ++i) {
-    const Job& j = jobs[i];
-    const int tw = trace_words(j.c->n);
-    if (i > 0 && tw != trace_words(jobs[i - 1].c->n)) groups = 0;  // item numbers restart per phase launch
-    TraceDesc& td = hd[i];
-    std::memset(&td, 0, sizeof(td));
-    td.c.ops = j.c->d_ops;
-    td.c.out = j.out_dev;
-    td.c.seed = j.seed;
-    td.c.shot0 = j.shot0;
-    td.c.item_begin = groups;
-    td.c.nops = j.c->nops;
-    td.c.n = j.c->n;
-    td.c.d = j.c->d;
-    td.c.nmeas = j.c->nmeas;
-    td.c.nshots = (int)j.nshots;
-    groups += (j.nshots + 31) / 32;
-    uint8_t* b = static_cast<uint8_t*>(ctx->trace.p) + off[i];
-    size_t o[4];
-    trace_offsets(j.c->nmeas, j.c->nn1, tw, o);
-    td.steps = j.c->d_steps;
-    td.lops = j.c->d_lops;
-    td.wins = j.c->d_wins;
-    td.nthr = j.c->d_nthr;
-    td.nhdr = j.c->d_nhdr;
-    td.nsteps = j.c->nsteps;
-    td.nwins = j.c->nwins;
-    td.mhdr = reinterpret_cast<uint4*>(b + o[0]);
-    td.mrow = reinterpret_cast<uint32_t*>(b + o[1]);
-    td.nrow = reinterpret_cast<uint32_t*>(b + o[2]);
-    td.coin_begin = coins;
-    if (moff[i] != SIZE_MAX) {
-      td.masks = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(ctx->masks.p) + moff[i]);
-      td.nchunk = (j.c->nn1_used + kCoinChunk - 1) / kCoinChunk;
-      coins += (long long)((td.nchunk + kCoinChunksPerItem - 1) / kCoinChunksPerItem) * j.nshots;
+  long long coins = 0;
+  TraceDesc* dd = nullptr;
+  if (k) {
+    std::vector<size_t> off(k);
+    size_t total = 0;
+    for (size_t i = 0; i < k; ++i) {
+      off[i] = total;
+      total += trace_bytes(jobs[i].c->nmeas, jobs[i].c->nn1, trace_words(jobs[i].c->n));
     }
-    td.nm = j.c->nmeas;
-    td.nn1 = j.c->nn1;
-    td.tw = tw;
-    td.wn = (j.c->n + 31) >> 5;
+    if ((rc = ensure(ctx, ctx->trace, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
+    if ((rc = ensure(ctx, ctx->tdescs, sizeof(TraceDesc) * k)) != SDIM_OK) return rc;
+    // fire masks: a word pair per 32 N1 ordinals per shot, within a budget
+    constexpr size_t kMaskBudget = (size_t)1 << 30;
+    std::vector<size_t> moff(k, SIZE_MAX);
+    size_t mtotal = 0;
+    for (size_t i = 0; i < k; ++i) {
+      const size_t nchunk = ((size_t)jobs[i].c->nn1_used + kCoinChunk - 1) / kCoinChunk;
+      const size_t b = round_up(nchunk * (size_t)jobs[i].nshots * 8, 256);
+      if (nchunk && mtotal + b <= kMaskBudget && !(flags & SDIM_FLAG_NO_COIN_PASS)) {
+        moff[i] = mtotal;
+        mtotal += b;
+      }
+    }
+    if (mtotal && (rc = ensure(ctx, ctx->masks, mtotal)) != SDIM_OK) return rc;
+    long long groups = 0;
+    for (size_t i = 0; i < k; ++i) {
+      const Job& j = jobs[i];
+      const int tw = trace_words(j.c->n);
+      if (i > 0 && tw != trace_words(jobs[i - 1].c->n)) groups = 0;  // item numbers restart per phase launch
+      TraceDesc& td = hd[i];
+      std::memset(&td, 0, sizeof(td));
+      td.c.ops = j.c->d_ops;
+      td.c.out = j.out_dev;
+      td.c.seed = j.seed;
+      td.c.shot0 = j.shot0;
+      td.c.item_begin = groups;
+      td.c.nops = j.c->nops;
+      td.c.n = j.c->n;
+      td.c.d = j.c->d;
+      td.c.nmeas = j.c->nmeas;
+      td.c.nshots = (int)j.nshots;
+      groups += (j.nshots + 31) / 32;
+      uint8_t* b = static_cast<uint8_t*>(ctx->trace.p) + off[i];
+      size_t o[4];
+      trace_offsets(j.c->nmeas, j.c->nn1, tw, o);
+      td.steps = j.c->d_steps;
+      td.lops = j.c->d_lops;
+      td.wins = j.c->d_wins;
+      td.nthr = j.c->d_nthr;
+      td.nhdr = j.c->d_nhdr;
+      td.nsteps = j.c->nsteps;
+      td.nwins = j.c->nwins;
+      td.mhdr = reinterpret_cast<uint4*>(b + o[0]);
+      td.mrow = reinterpret_cast<uint32_t*>(b + o[1]);
+      td.nrow = reinterpret_cast<uint32_t*>(b + o[2]);
+      td.coin_begin = coins;
+      if (moff[i] != SIZE_MAX) {
+        td.masks = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(ctx->masks.p) + moff[i]);
+        td.nchunk = (j.c->nn1_used + kCoinChunk - 1) / kCoinChunk;
+        coins += (long long)((td.nchunk + kCoinChunksPerItem - 1) / kCoinChunksPerItem) * j.nshots;
+      }
+      td.nm = j.c->nmeas;
+      td.nn1 = j.c->nn1;
+      td.tw = tw;
+      td.wn = (j.c->n + 31) >> 5;
+    }
+    dd = static_cast<TraceDesc*>(ctx->tdescs.p);
+    CK(cudaMemcpyAsync(dd, hd.data(), sizeof(TraceDesc) * k, cudaMemcpyHostToDevice, s));
   }
-  TraceDesc* dd = static_cast<TraceDesc*>(ctx->tdescs.p);
-  CK(cudaMemcpyAsync(dd, hd.data(), sizeof(TraceDesc) * k, cudaMemcpyHostToDevice, s));
+  // ---- odd-d descriptors
+  std::stable_sort(ujobs.begin(), ujobs.end(), [](const Job& a, const Job& b) {
+    const int va = trace_u8_variant(a.c->d), vb = trace_u8_variant(b.c->d);
+    return va != vb ? va < vb : a.c->n < b.c->n;
+  });
+  const size_t ku = ujobs.size();
+  std::vector<TraceDescU8> hu(ku);
+  TraceDescU8* du = nullptr;
+  if (ku) {
+    std::vector<size_t> off(ku);
+    size_t total = 0;
+    for (size_t i = 0; i < ku; ++i) {
+      size_t o[5];
+      trace_offsets_u8(ujobs[i].c->nmeas, ujobs[i].c->nn1, trace_row_bytes_u8(ujobs[i].c->n), o);
+      off[i] = total;
+      total += o[4];
+    }
+    if ((rc = ensure(ctx, ctx->trace_u8, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
+    if ((rc = ensure(ctx, ctx->tdescs_u8, sizeof(TraceDescU8) * ku)) != SDIM_OK) return rc;
+    long long groups = 0;
+    for (size_t i = 0; i < ku; ++i) {
+      const Job& j = ujobs[i];
+      if (i > 0 && trace_u8_variant(j.c->d) != trace_u8_variant(ujobs[i - 1].c->d)) groups = 0;
+      TraceDescU8& td = hu[i];
+      std::memset(&td, 0, sizeof(td));
+      td.c.ops = j.c->d_ops;
+      td.c.out = j.out_dev;
+      td.c.seed = j.seed;
+      td.c.shot0 = j.shot0;
+      td.c.item_begin = groups;
+      td.c.nops = j.c->nops;
+      td.c.n = j.c->n;
+      td.c.d = j.c->d;
+      td.c.nmeas = j.c->nmeas;
+      td.c.nshots = (int)j.nshots;
+      groups += (j.nshots + 31) / 32;
+      td.sw = trace_row_bytes_u8(j.c->n);
+      size_t o[5];
+      trace_offsets_u8(j.c->nmeas, j.c->nn1, td.sw, o);
+      uint8_t* b = static_cast<uint8_t*>(ctx->trace_u8.p) + off[i];
+      td.mhdr = reinterpret_cast<uint4*>(b + o[0]);
+      td.mrow = b + o[1];
+      td.nrow = b + o[2];
+      td.nhdr = reinterpret_cast<uint2*>(b + o[3]);
+      td.nm = j.c->nmeas;
+      td.nn1 = j.c->nn1;
+    }
+    du = static_cast<TraceDescU8*>(ctx->tdescs_u8.p);
+    CK(cudaMemcpyAsync(du, hu.data(), sizeof(TraceDescU8) * ku, cudaMemcpyHostToDevice, s));
+  }
   if (coins) CK(cudaEventRecord(ctx->ev_fork, s));
-  // x / z pass: one CTA per program
-  {
+  // ---- x / z passes: one CTA per program
+  if (k) {
     const int nmax = jobs[k - 1].c->n;
     const size_t hot = trace_pass_hot_bytes(nmax), xz = trace_pass_xz_bytes(nmax);
     // after the tableau: the schedule window; about 3.2 KB of static shared memory besides
@@ -396,7 +467,25 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
   }
-  // coin pass on the second stream, alongside the x / z pass (independent work)
+  for (size_t b = 0; b < ku;) {
+    const int v = trace_u8_variant(hu[b].c.d);
+    size_t e = b;
+    while (e < ku && trace_u8_variant(hu[e].c.d) == v) ++e;
+    const int nmax = hu[e - 1].c.n;
+    const size_t hot = trace_u8_hot_bytes(nmax), xz = trace_u8_xz_bytes(nmax);
+    const bool in_smem = !force_gmem && hot + xz + 4096 <= (size_t)ctx->smem_optin;
+    int grid = (int)std::min<size_t>(e - b, 65535);
+    if (!in_smem) {
+      grid = std::min(grid, 2 * ctx->num_sms);
+      if ((rc = ensure(ctx, ctx->xz_u8, xz * (size_t)grid)) != SDIM_OK) return rc;
+    }
+    launch_trace_u8_xz(v, grid, hot + (in_smem ? xz : 0), s, du + b, (int)(e - b),
+                       static_cast<uint8_t*>(ctx->xz_u8.p), xz, hot, in_smem ? 1 : 0, status);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "odd-d trace pass launch");
+    b = e;
+  }
+  // ---- coin pass on the second stream, alongside the x / z passes (independent work)
   if (coins) {
     CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
     const int block = 256;
@@ -409,7 +498,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
   }
   if (timed) CK(cudaEventRecord(ctx->ev_xz, s));
-  // phase passes, one per row width
+  // ---- phase passes
   for (size_t b = 0; b < k;) {
     const int tw = hd[b].tw;
     size_t e = b;
@@ -425,6 +514,24 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, cudaStream_t s, unsi
       return fail(ctx, SDIM_EINVAL, "no phase pass for trace rows of " + std::to_string(tw) + " words");
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "phase pass launch");
+    b = e;
+  }
+  for (size_t b = 0; b < ku;) {
+    const int v = trace_u8_variant(hu[b].c.d);
+    size_t e = b;
+    long long items = 0;
+    while (e < ku && trace_u8_variant(hu[e].c.d) == v) {
+      items = hu[e].c.item_begin + (hu[e].c.nshots + 31) / 32;
+      ++e;
+    }
+    const int nmax = hu[e - 1].c.n;
+    // (shot, chunk) threads: about 64 generators per thread, 32 to 512 threads
+    const int nch = std::max(1, std::min(16, (2 * nmax + 63) / 64));
+    if (items > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one phase pass");
+    launch_trace_u8_phase(v, (int)items, 32 * nch, trace_u8_phase_smem(nmax), s, du + b, (int)(e - b), items,
+                          status);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "odd-d phase pass launch");
     b = e;
   }
   if (timed) {
@@ -443,8 +550,8 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsig
   const bool plain = flags & SDIM_FLAG_PLAIN;
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
   ctx->last_stream = s;
-  std::vector<Job> jobs, tjobs;
-  for (const Job& j : all_jobs) (use_trace(j, flags) ? tjobs : jobs).push_back(j);
+  std::vector<Job> jobs, tjobs, ujobs;
+  for (const Job& j : all_jobs) (use_trace(j, flags) ? tjobs : use_trace_u8(j, flags) ? ujobs : jobs).push_back(j);
   int rc;
   if ((rc = ensure(ctx, ctx->status, sizeof(int))) != SDIM_OK) return rc;
   if ((rc = ensure(ctx, ctx->counters, sizeof(unsigned long long) * V_COUNT)) != SDIM_OK) return rc;
@@ -493,7 +600,7 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsig
   CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * V_COUNT, s));
   if (flags & SDIM_FLAG_TIME) CK(cudaEventRecord(ctx->ev0, s));
   int* status = static_cast<int*>(ctx->status.p);
-  if ((rc = launch_trace_jobs(ctx, tjobs, s, flags, status)) != SDIM_OK) return rc;
+  if ((rc = launch_trace_jobs(ctx, tjobs, ujobs, s, flags, status)) != SDIM_OK) return rc;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const Group& g = groups[gi];
     if (g.items == 0) continue;
@@ -818,7 +925,7 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   cudaStreamSynchronize(ctx->aux);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
-                    &ctx->tdescs, &ctx->trace, &ctx->masks};
+                    &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);

@@ -1,0 +1,90 @@
+// Trace engine kernels for odd prime d: the x / z pass (one CTA per
+// program, TGroupU8 team with no live shots) and the phase pass (one CTA
+// per 32-shot group, (shot, chunk) threads).  Instantiated for d = 3, 5, 7
+// and a generic d.
+#include "trace_u8.cuh"
+#include "variants.cuh"
+
+namespace sdim {
+namespace {
+
+template <int DD>
+__global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const TraceDescU8* __restrict__ descs, int ndesc,
+                                                                     uint8_t* gxz, size_t xz_bytes, size_t hot_bytes,
+                                                                     int xz_in_smem, int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int red[40];
+  uint8_t* hot = smem;
+  uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
+  for (int i = blockIdx.x; i < ndesc; i += gridDim.x) {
+    const TraceDescU8 td = descs[i];
+    TGroupU8<DD, CtaTeam> e(xz, hot, td.c.n, td.c.d, CtaTeam(red));
+    trace_program_u8(td, e, status);
+    __syncthreads();
+  }
+}
+
+template <int DD>
+__global__ void __launch_bounds__(512) k_phase_pass_u8(const TraceDescU8* __restrict__ descs, int ndesc,
+                                                       long long total_groups, const int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
+  const long long g = blockIdx.x;
+  if (g >= total_groups) return;
+  const int i = find_trace_desc_u8(descs, ndesc, g);
+  phase_program_u8<DD>(descs + i, g - descs[i].c.item_begin, smem);
+}
+
+template <int DD>
+struct TraceU8 {
+  static cudaError_t set_smem(int optin) {
+    const cudaError_t e = set_dynamic_smem(k_trace_pass_u8<DD>, optin);
+    return e != cudaSuccess ? e : set_dynamic_smem(k_phase_pass_u8<DD>, optin);
+  }
+  static void xz(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
+                 size_t hot, int in_smem, int* status) {
+    k_trace_pass_u8<DD><<<grid, kTracePassThreads, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, status);
+  }
+  static void phase(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, long long total,
+                    int* status) {
+    k_phase_pass_u8<DD><<<grid, block, smem, s>>>(d, nd, total, status);
+  }
+};
+
+}  // namespace
+
+int trace_u8_variant(int d) { return d == 3 ? 0 : d == 5 ? 1 : d == 7 ? 2 : 3; }
+
+cudaError_t trace_u8_set_smem(int optin) {
+  cudaError_t e;
+  if ((e = TraceU8<3>::set_smem(optin)) != cudaSuccess) return e;
+  if ((e = TraceU8<5>::set_smem(optin)) != cudaSuccess) return e;
+  if ((e = TraceU8<7>::set_smem(optin)) != cudaSuccess) return e;
+  return TraceU8<0>::set_smem(optin);
+}
+
+size_t trace_u8_hot_bytes(int n) { return round16(SlotGroupU8::hot_bytes(n)); }
+size_t trace_u8_xz_bytes(int n) { return round16(SlotGroupU8::xz_bytes(n)); }
+size_t trace_u8_phase_smem(int n) { return round16(phase_u8_smem(n)); }
+
+void launch_trace_u8_xz(int variant, int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+                        uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status) {
+  switch (variant) {
+    case 0: TraceU8<3>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 1: TraceU8<5>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 2: TraceU8<7>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    default: TraceU8<0>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+  }
+}
+
+void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
+                           int nd, long long total, int* status) {
+  switch (variant) {
+    case 0: TraceU8<3>::phase(grid, block, smem, s, d, nd, total, status); break;
+    case 1: TraceU8<5>::phase(grid, block, smem, s, d, nd, total, status); break;
+    case 2: TraceU8<7>::phase(grid, block, smem, s, d, nd, total, status); break;
+    default: TraceU8<0>::phase(grid, block, smem, s, d, nd, total, status); break;
+  }
+}
+
+}  // namespace sdim

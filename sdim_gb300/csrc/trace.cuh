@@ -72,6 +72,28 @@ constexpr int kCoinChunk = 32;
 // Chunks one coin-pass thread fills.
 constexpr int kCoinChunksPerItem = 8;
 
+// Trace of one odd-d program (layout in trace_u8.cuh); N1 coins are drawn in
+// its phase pass.
+struct TraceDescU8 {
+  CircuitDesc c;  // item_begin counts 32-shot groups of the phase pass
+  uint4* mhdr;
+  uint8_t* mrow;
+  uint8_t* nrow;
+  uint2* nhdr;  // N1 ordinal j: (coin threshold, opcode), 0xffffffff for probability 0
+  int nm, nn1;
+  int sw;  // bytes per trace row
+};
+
+__host__ __device__ inline int trace_row_bytes_u8(int n) { return (int)round_up((size_t)2 * n, 16); }
+
+__host__ __device__ inline void trace_offsets_u8(int nm, int nn1, int sw, size_t o[5]) {
+  o[0] = 0;                                                // mhdr
+  o[1] = o[0] + round_up((size_t)nm * 16, 256);            // mrow
+  o[2] = o[1] + round_up((size_t)nm * 2 * sw, 256);        // nrow
+  o[3] = o[2] + round_up((size_t)nn1 * 2 * sw, 256);       // nhdr
+  o[4] = o[3] + round_up((size_t)nn1 * 8, 256);
+}
+
 // Widest trace row the phase pass has an instance for (n <= 512).
 constexpr int kTraceMaxWords = 32;
 
@@ -116,5 +138,17 @@ void launch_coin_pass(int grid, int block, cudaStream_t s, const TraceDesc* desc
 // descs has trace rows of tw words.  Returns false for an unsupported tw.
 bool launch_phase_pass(int tw, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        long long total_groups, int* status);
+
+// Odd-d trace engine (k_trace_u8.cu).  variant: 0, 1, 2 for d = 3, 5, 7, 3
+// for any other odd prime.
+int trace_u8_variant(int d);
+cudaError_t trace_u8_set_smem(int optin);
+size_t trace_u8_hot_bytes(int n);
+size_t trace_u8_xz_bytes(int n);
+size_t trace_u8_phase_smem(int n);
+void launch_trace_u8_xz(int variant, int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+                        uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status);
+void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
+                           int nd, long long total, int* status);
 
 }  // namespace sdim

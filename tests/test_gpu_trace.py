@@ -116,3 +116,58 @@ def test_full_size_noisy_surface_against_group_engine_and_oracle():
     assert np.array_equal(rec, prog.sample(100_000, seed=2, engine="group"))
     assert np.array_equal(rec[:64], oracle_run([spec], 2, 0, 64)["records"])
     assert np.array_equal(rec[-64:], oracle_run([spec], 2, 100_000 - 64, 64)["records"])
+
+
+# ---------------------------------------------------------------- odd d
+
+
+def test_pr1_fixture_on_the_odd_d_trace_engine(golden):
+    """PR1 (d = 3, n = 32, 1,024 shots): every record equals the reference's."""
+    from tests.conftest import program_of
+    cases, arrays = golden
+    name = next(k for k in cases if k.startswith("pr1"))
+    prog = program_of(cases[name])
+    rec = prog.sample(cases[name]["nshots"], seed=cases[name]["seed"], engine="trace")
+    assert np.array_equal(rec, arrays[f"{name}__records"])
+
+
+@pytest.mark.parametrize("d", [3, 5, 7, 11])
+@pytest.mark.parametrize("n", [1, 5, 33, 100])
+def test_odd_d_small_n_against_oracle(d, n):
+    spec = workloads.random_hpc(n, d, 5 * n + 20, seed=31 * d + n, mr_every=max(1, n // 2), mr_fraction=0.3)
+    prog = Program(spec.build())
+    rec = prog.sample(70, seed=d + n, shot0=3, engine="trace")
+    assert np.array_equal(rec, oracle_run([spec], d + n, 3, 70)["records"]), (d, n)
+
+
+@pytest.mark.parametrize("d", [3, 5, 7, 13])
+@pytest.mark.parametrize("n", [170, 256, 700])
+def test_odd_d_large_n_against_group_engine(d, n):
+    # n >= 230 puts the x / z pass's tableau in global memory
+    spec = workloads.random_hpc(n, d, 3 * n, seed=17 * d + n, mr_every=n, mr_fraction=0.1)
+    prog = Program(spec.build())
+    rec = prog.sample(66, seed=n, engine="trace")
+    assert np.array_equal(rec, prog.sample(66, seed=n, engine="group")), (d, n)
+
+
+@pytest.mark.parametrize("d", [3, 5])
+def test_odd_d_all_gates_and_noise_channels(d):
+    spec = workloads.all_gates_random(6, d, 250, seed=7 * d, noise_probs=(0.0, 0.35, 1.0))
+    prog = Program(spec.build())
+    rec = prog.sample(100, seed=d, shot0=5, engine="trace")
+    assert np.array_equal(rec, oracle_run([spec], d, 5, 100)["records"])
+
+
+def test_mixed_dimensions_in_one_batch():
+    specs = [workloads.random_hpc(30, 3, 150, seed=1, mr_every=15), workloads.random_hpc(40, 2, 200, seed=2,
+                                                                                          mr_every=20),
+             workloads.random_hpc(64, 5, 300, seed=3, mr_every=32), workloads.random_hpc(20, 7, 90, seed=4,
+                                                                                        mr_every=10),
+             workloads.random_hpc(12, 3, 60, seed=5, mr_every=6)]
+    shots = [100, 90, 70, 64, 10]
+    runner = BatchRunner()
+    for i, (s, k) in enumerate(zip(specs, shots)):
+        runner.add_spec(s, k, seed=100 + i, shot0=2 * i)
+    outs = runner.run()
+    for e, s, out in zip(runner.entries, specs, outs):
+        assert np.array_equal(out, oracle_run([s], e.seed, e.shot0, e.shots)["records"]), s.name
