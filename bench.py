@@ -303,7 +303,7 @@ def run_reference_arm(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
-TRACE_MIN_SHOTS = 64  # the library's default switch to the trace engine (d = 2)
+TRACE_MIN_SHOTS = 128  # the library's default switch to the trace engine
 
 
 def trace_words(n):

@@ -29,6 +29,7 @@ FLAG_TEAM_CTA = 128
 FLAG_TRACE = 256
 FLAG_NO_TRACE = 512
 FLAG_NO_COIN_PASS = 1024
+FLAG_SPLIT_XZ = 2048
 
 
 def engine_flags(engine) -> int:

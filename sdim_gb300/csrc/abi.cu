@@ -273,10 +273,11 @@ int job_variant(const sdim_circuit* c, unsigned flags) {
   return c->gvariant;
 }
 
-// Below this many shots a d = 2 program runs on the shot-group engine: one
-// x / z pass per program plus a phase pass only pays once there are several
-// 32-shot groups to share it.
-constexpr int64_t kTraceMinShots = 64;
+// Below this many shots a program runs on the shot-group engine: one x / z
+// pass per program plus a phase pass only pays once there are several 32-shot
+// groups to share it, and in a batch of small programs the group engine's
+// single persistent launch keeps every SM busy.
+constexpr int64_t kTraceMinShots = 128;
 
 // Jobs for the trace engine: d = 2, batched form, trace rows of at most
 // kTraceMaxWords words (n <= 512) and kTraceMinShots shots, unless
@@ -467,20 +468,37 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
   }
+  // odd d: one CTA with the tableau in shared memory when it fits, else a
+  // CTA pair splitting the generator columns (trace_split_u8.cuh) when that
+  // fits, else one CTA with the tableau in global memory
+  const size_t optin = (size_t)ctx->smem_optin;
+  auto xz_mode = [&](int n) {
+    const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + 4096 <= optin;
+    const bool pair = trace_u8_split_smem(n) + 4096 <= optin;
+    if (force_gmem) return 2;
+    if (pair && (flags & SDIM_FLAG_SPLIT_XZ)) return 1;
+    return single ? 0 : pair ? 1 : 2;
+  };
   for (size_t b = 0; b < ku;) {
     const int v = trace_u8_variant(hu[b].c.d);
+    const int mode = xz_mode(hu[b].c.n);
     size_t e = b;
-    while (e < ku && trace_u8_variant(hu[e].c.d) == v) ++e;
+    while (e < ku && trace_u8_variant(hu[e].c.d) == v && xz_mode(hu[e].c.n) == mode) ++e;
     const int nmax = hu[e - 1].c.n;
-    const size_t hot = trace_u8_hot_bytes(nmax), xz = trace_u8_xz_bytes(nmax);
-    const bool in_smem = !force_gmem && hot + xz + 4096 <= (size_t)ctx->smem_optin;
-    int grid = (int)std::min<size_t>(e - b, 65535);
-    if (!in_smem) {
-      grid = std::min(grid, 2 * ctx->num_sms);
-      if ((rc = ensure(ctx, ctx->xz_u8, xz * (size_t)grid)) != SDIM_OK) return rc;
+    if (mode == 1) {
+      launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax), s, du + b,
+                            (int)(e - b), status);
+    } else {
+      const size_t hot = trace_u8_hot_bytes(nmax), xz = trace_u8_xz_bytes(nmax);
+      const bool in_smem = mode == 0;
+      int grid = (int)std::min<size_t>(e - b, 65535);
+      if (!in_smem) {
+        grid = std::min(grid, 2 * ctx->num_sms);
+        if ((rc = ensure(ctx, ctx->xz_u8, xz * (size_t)grid)) != SDIM_OK) return rc;
+      }
+      launch_trace_u8_xz(v, grid, hot + (in_smem ? xz : 0), s, du + b, (int)(e - b),
+                         static_cast<uint8_t*>(ctx->xz_u8.p), xz, hot, in_smem ? 1 : 0, status);
     }
-    launch_trace_u8_xz(v, grid, hot + (in_smem ? xz : 0), s, du + b, (int)(e - b),
-                       static_cast<uint8_t*>(ctx->xz_u8.p), xz, hot, in_smem ? 1 : 0, status);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "odd-d trace pass launch");
     b = e;

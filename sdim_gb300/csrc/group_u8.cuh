@@ -31,6 +31,17 @@
 
 namespace sdim {
 
+// Four residues of a 32-bit word, each in [0, d^2 - d], reduced mod d at
+// once for d in {3, 5, 7}: even and odd bytes go through 16-bit lanes, where
+// floor(v / d) = (v m) >> 8 with m = 86, 52, 37 is exact over that range.
+template <int DD>
+__device__ __forceinline__ uint32_t packed_mod(uint32_t v) {
+  constexpr uint32_t m = DD == 3 ? 86u : DD == 5 ? 52u : 37u;
+  const uint32_t lo = v & 0x00FF00FFu, hi = (v >> 8) & 0x00FF00FFu;
+  const uint32_t qlo = ((lo * m) >> 8) & 0x00FF00FFu, qhi = ((hi * m) >> 8) & 0x00FF00FFu;
+  return (lo - qlo * (uint32_t)DD) | ((hi - qhi * (uint32_t)DD) << 8);
+}
+
 struct SlotGroupU8 {
   static constexpr int kShots = 32;
   __host__ __device__ static size_t xz_bytes(int n) { return 2 * (size_t)n * SlotU8::stride(n); }
@@ -207,6 +218,49 @@ struct TGroupU8 {
         uint32_t* zcol = reinterpret_cast<uint32_t*>(Z) + w;
         const int S4 = S >> 2;
         int k = r;
+        if constexpr (DD == 3 || DD == 5 || DD == 7) {
+          // four residues per operation (packed_mod): f a <= (d-1)^2 and
+          // x + f a <= d^2 - d stay inside a byte; dots add up in 16-bit lanes
+          uint32_t dlo = 0u, dhi = 0u;
+          int rows = 0;
+          // four rows in flight: their loads are issued before any store
+          for (; k + 3 * R < n; k += 4 * R) {
+            uint32_t xw[4], zw[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              xw[i] = xcol[(size_t)(k + i * R) * S4];
+              zw[i] = zcol[(size_t)(k + i * R) * S4];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const uint32_t a = CX[k + i * R], b = CZ[k + i * R];
+              dlo += (zw[i] & 0x00FF00FFu) * a;
+              dhi += ((zw[i] >> 8) & 0x00FF00FFu) * a;
+              xcol[(size_t)(k + i * R) * S4] = packed_mod<DD>(xw[i] + fw * a);
+              zcol[(size_t)(k + i * R) * S4] = packed_mod<DD>(zw[i] + fw * b);
+            }
+            if ((rows += 4) >= 1024) {  // 1024 (d-1)^2 < 2^16
+              dots[0] += (int)(dlo & 0xffffu);
+              dots[2] += (int)(dlo >> 16);
+              dots[1] += (int)(dhi & 0xffffu);
+              dots[3] += (int)(dhi >> 16);
+              dlo = dhi = 0u;
+              rows = 0;
+            }
+          }
+          for (; k < n; k += R) {
+            const uint32_t xw = xcol[(size_t)k * S4], zw = zcol[(size_t)k * S4];
+            const uint32_t a = CX[k], b = CZ[k];
+            dlo += (zw & 0x00FF00FFu) * a;
+            dhi += ((zw >> 8) & 0x00FF00FFu) * a;
+            xcol[(size_t)k * S4] = packed_mod<DD>(xw + fw * a);
+            zcol[(size_t)k * S4] = packed_mod<DD>(zw + fw * b);
+          }
+          dots[0] += (int)(dlo & 0xffffu);
+          dots[2] += (int)(dlo >> 16);
+          dots[1] += (int)(dhi & 0xffffu);
+          dots[3] += (int)(dhi >> 16);
+        }
         for (; k + 3 * R < n; k += 4 * R) {
           uint32_t x0 = xcol[(size_t)k * S4], x1 = xcol[(size_t)(k + R) * S4];
           uint32_t x2 = xcol[(size_t)(k + 2 * R) * S4], x3 = xcol[(size_t)(k + 3 * R) * S4];

@@ -2,7 +2,7 @@
 // program, TGroupU8 team with no live shots) and the phase pass (one CTA
 // per 32-shot group, (shot, chunk) threads).  Instantiated for d = 3, 5, 7
 // and a generic d.
-#include "trace_u8.cuh"
+#include "trace_split_u8.cuh"
 #include "variants.cuh"
 
 namespace sdim {
@@ -24,6 +24,19 @@ __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const Trace
   }
 }
 
+// One program per CTA pair (cluster of two, grid-stride over programs).
+template <int DD>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTracePassThreads)
+    k_trace_pass_split(const TraceDescU8* __restrict__ descs, int ndesc, int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int red[40];
+  for (int i = (int)(blockIdx.x >> 1); i < ndesc; i += (int)(gridDim.x >> 1)) {
+    const TraceDescU8 td = descs[i];
+    SplitU8<DD> e(smem, td.c.n, td.c.d, red);
+    split_program(td, e, status);
+  }
+}
+
 template <int DD>
 __global__ void __launch_bounds__(512) k_phase_pass_u8(const TraceDescU8* __restrict__ descs, int ndesc,
                                                        long long total_groups, const int* status) {
@@ -38,8 +51,12 @@ __global__ void __launch_bounds__(512) k_phase_pass_u8(const TraceDescU8* __rest
 template <int DD>
 struct TraceU8 {
   static cudaError_t set_smem(int optin) {
-    const cudaError_t e = set_dynamic_smem(k_trace_pass_u8<DD>, optin);
+    cudaError_t e = set_dynamic_smem(k_trace_pass_u8<DD>, optin);
+    if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_split<DD>, optin);
     return e != cudaSuccess ? e : set_dynamic_smem(k_phase_pass_u8<DD>, optin);
+  }
+  static void split(int pairs, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, int* status) {
+    k_trace_pass_split<DD><<<2 * pairs, kTracePassThreads, smem, s>>>(d, nd, status);
   }
   static void xz(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
                  size_t hot, int in_smem, int* status) {
@@ -66,6 +83,17 @@ cudaError_t trace_u8_set_smem(int optin) {
 size_t trace_u8_hot_bytes(int n) { return round16(SlotGroupU8::hot_bytes(n)); }
 size_t trace_u8_xz_bytes(int n) { return round16(SlotGroupU8::xz_bytes(n)); }
 size_t trace_u8_phase_smem(int n) { return round16(phase_u8_smem(n)); }
+size_t trace_u8_split_smem(int n) { return round16(split_smem_bytes(n)); }
+
+void launch_trace_u8_split(int variant, int pairs, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+                           int* status) {
+  switch (variant) {
+    case 0: TraceU8<3>::split(pairs, smem, s, d, nd, status); break;
+    case 1: TraceU8<5>::split(pairs, smem, s, d, nd, status); break;
+    case 2: TraceU8<7>::split(pairs, smem, s, d, nd, status); break;
+    default: TraceU8<0>::split(pairs, smem, s, d, nd, status); break;
+  }
+}
 
 void launch_trace_u8_xz(int variant, int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
                         uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status) {

@@ -148,6 +148,10 @@ size_t trace_u8_xz_bytes(int n);
 size_t trace_u8_phase_smem(int n);
 void launch_trace_u8_xz(int variant, int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
                         uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status);
+// x / z pass on CTA pairs (trace_split_u8.cuh): `pairs` clusters of two.
+size_t trace_u8_split_smem(int n);
+void launch_trace_u8_split(int variant, int pairs, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+                           int* status);
 void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
                            int nd, long long total, int* status);
 

@@ -56,7 +56,7 @@ def test_records_do_not_depend_on_the_split():
     parts = np.concatenate([prog.sample(37, seed=8, engine="trace"),
                             prog.sample(113, seed=8, shot0=37, engine="trace")])
     assert np.array_equal(whole, parts)
-    assert np.array_equal(whole[:20], prog.sample(20, seed=8))        # group engine below 64 shots
+    assert np.array_equal(whole[:20], prog.sample(20, seed=8))        # group engine below 128 shots
     assert np.array_equal(whole[:3], prog.sample(3, seed=8, per_shot=True))
 
 
@@ -68,7 +68,7 @@ def test_mixed_batch_routes_each_program():
              workloads.random_hpc(12, 3, 120, seed=6, mr_every=6), workloads.random_hpc(300, 2, 900, seed=7,
                                                                                         mr_every=300),
              workloads.random_hpc(70, 2, 300, seed=8, mr_every=35)]
-    shots = [300, 10, 80, 64, 129]
+    shots = [300, 10, 80, 128, 129]
     runner = BatchRunner()
     for i, (s, k) in enumerate(zip(specs, shots)):
         runner.add_spec(s, k, seed=int(rng.integers(1 << 30)), shot0=i)
@@ -76,7 +76,7 @@ def test_mixed_batch_routes_each_program():
     for e, s, out in zip(runner.entries, specs, outs):
         if s.num_qudits <= 70:
             assert np.array_equal(out, oracle_run([s], e.seed, e.shot0, e.shots)["records"]), s.name
-    alone = Program(specs[3].build()).sample(64, seed=runner.entries[3].seed, shot0=3, engine="group")
+    alone = Program(specs[3].build()).sample(128, seed=runner.entries[3].seed, shot0=3, engine="group")
     assert np.array_equal(outs[3], alone)
 
 
@@ -164,10 +164,27 @@ def test_mixed_dimensions_in_one_batch():
              workloads.random_hpc(64, 5, 300, seed=3, mr_every=32), workloads.random_hpc(20, 7, 90, seed=4,
                                                                                         mr_every=10),
              workloads.random_hpc(12, 3, 60, seed=5, mr_every=6)]
-    shots = [100, 90, 70, 64, 10]
+    shots = [200, 130, 150, 128, 10]
     runner = BatchRunner()
     for i, (s, k) in enumerate(zip(specs, shots)):
         runner.add_spec(s, k, seed=100 + i, shot0=2 * i)
     outs = runner.run()
     for e, s, out in zip(runner.entries, specs, outs):
         assert np.array_equal(out, oracle_run([s], e.seed, e.shot0, e.shots)["records"]), s.name
+
+
+@pytest.mark.parametrize("d", [3, 5, 7, 11])
+@pytest.mark.parametrize("n", [1, 6, 33, 100])
+def test_odd_d_cta_pair_against_oracle(d, n):
+    """SDIM_FLAG_SPLIT_XZ runs the odd-d x / z pass on a CTA pair (stabilizer
+    and destabilizer columns in the two blocks' shared memory) even where one
+    CTA would do; records equal the oracle's, noise included."""
+    spec = (workloads.all_gates_random(n, d, 200, seed=3 * d + n, noise_probs=(0.0, 0.3, 1.0)) if n <= 6 else
+            workloads.random_hpc(n, d, 5 * n + 20, seed=13 * d + n, mr_every=max(1, n // 2), mr_fraction=0.3))
+    prog = Program(spec.build())
+    dp = prog.compile(True)
+    ctx = prog.context
+    out = np.empty((70, dp.num_records), dtype=np.uint8)
+    rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, d, 2, 70, out.ctypes.data, _lib.FLAG_TRACE | _lib.FLAG_SPLIT_XZ)
+    _lib.check(rc, ctx.ptr, "odd-d trace on a CTA pair")
+    assert np.array_equal(out, oracle_run([spec], d, 2, 70)["records"]), (d, n)
