@@ -472,9 +472,10 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   // CTA pair splitting the generator columns (trace_split_u8.cuh) when that
   // fits, else one CTA with the tableau in global memory
   const size_t optin = (size_t)ctx->smem_optin;
+  const size_t win = trace_u8_window_bytes();
   auto xz_mode = [&](int n) {
-    const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + 4096 <= optin;
-    const bool pair = trace_u8_split_smem(n) + 4096 <= optin;
+    const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
+    const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
     if (force_gmem) return 2;
     if (pair && (flags & SDIM_FLAG_SPLIT_XZ)) return 1;
     return single ? 0 : pair ? 1 : 2;
@@ -486,8 +487,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     while (e < ku && trace_u8_variant(hu[e].c.d) == v && xz_mode(hu[e].c.n) == mode) ++e;
     const int nmax = hu[e - 1].c.n;
     if (mode == 1) {
-      launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax), s, du + b,
-                            (int)(e - b), status);
+      launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax) + win,
+                            trace_u8_split_smem(nmax), s, du + b, (int)(e - b), status);
     } else {
       const size_t hot = trace_u8_hot_bytes(nmax), xz = trace_u8_xz_bytes(nmax);
       const bool in_smem = mode == 0;
@@ -496,7 +497,9 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
         grid = std::min(grid, 2 * ctx->num_sms);
         if ((rc = ensure(ctx, ctx->xz_u8, xz * (size_t)grid)) != SDIM_OK) return rc;
       }
-      launch_trace_u8_xz(v, grid, hot + (in_smem ? xz : 0), s, du + b, (int)(e - b),
+      // about two generator columns per thread: 64 to kTracePassThreads threads
+      const int block = std::max(64, std::min(kTracePassThreads, (nmax + 31) & ~31));
+      launch_trace_u8_xz(v, grid, block, hot + (in_smem ? xz : 0) + win, s, du + b, (int)(e - b),
                          static_cast<uint8_t*>(ctx->xz_u8.p), xz, hot, in_smem ? 1 : 0, status);
     }
     const cudaError_t le = cudaGetLastError();
@@ -744,11 +747,12 @@ int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* n
 //   lops[i] = {instruction word, y, ordinal (measurement index of M /
 //     RESET, noise ordinal of N1), N1 ordinals before it (M / RESET)};
 //   wins[i] = {first step, steps, first op, ops}: windows of at most
-//     kTraceWinSteps steps and kTraceWinOps ops that the pass stages in
-//     shared memory (a longer step is a window of its own, read in place).
+//     win_steps steps and win_ops ops that the pass stages in shared memory
+//     (a longer step is a window of its own, read in place).
 // Between two measurements only ops that share a qudit (or two P's) are
 // ordered, so each op goes one level after the last op it follows.
-void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int n, TraceSchedule& out) {
+void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int n, int win_steps, int win_ops,
+                     TraceSchedule& out) {
   std::vector<uint4> steps, lops, wins;
   std::vector<std::vector<uint4>> layers;
   std::vector<int> last(n, -1), gen(n, -1);
@@ -808,14 +812,14 @@ void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int 
   }
   if (!layers.empty()) flush();
   for (size_t s = 0; s < steps.size();) {
-    if (steps[s].z > (uint32_t)kTraceWinOps) {
+    if (steps[s].z > (uint32_t)win_ops) {
       wins.push_back(make_uint4((uint32_t)s, 1u, steps[s].y, steps[s].z));
       ++s;
       continue;
     }
     size_t e = s;
     uint32_t cnt = 0;
-    while (e < steps.size() && e - s < (size_t)kTraceWinSteps && cnt + steps[e].z <= (uint32_t)kTraceWinOps)
+    while (e < steps.size() && e - s < (size_t)win_steps && cnt + steps[e].z <= (uint32_t)win_ops)
       cnt += steps[e++].z;
     wins.push_back(make_uint4((uint32_t)s, (uint32_t)(e - s), steps[s].y, cnt));
     s = e;
@@ -1002,7 +1006,7 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
   if (rc != SDIM_OK) return rc;
   const size_t ndev = dev.size();
   TraceSchedule sch;
-  if (d == 2 && trace_words(n)) append_schedule(dev, 0, ndev, n, sch);
+  if (d == 2 && trace_words(n)) append_schedule(dev, 0, ndev, n, kTraceWinSteps, kTraceWinOps, sch);
   cudaSetDevice(ctx->device);
   sdim_circuit* c = new sdim_circuit();
   c->device = ctx->device;
@@ -1190,7 +1194,8 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
     c.nn1 = nn1;
     c.nops_user = r1 - r0;
     c.nops = (int)(dev.size() - op_off[i]);
-    if (d[i] == 2 && trace_words(n[i])) append_schedule(dev, op_off[i], (size_t)c.nops, n[i], sch[i]);
+    if (d[i] == 2 && trace_words(n[i]))
+      append_schedule(dev, op_off[i], (size_t)c.nops, n[i], kTraceWinSteps, kTraceWinOps, sch[i]);
     c.variant = variant_for(d[i]);
     c.gvariant = group_variant_for(d[i], n[i], 0);
     c.gblock = variant_ops(c.gvariant).cta ? cta_block_for(n[i]) : 32;

@@ -16,10 +16,11 @@ __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const Trace
   __shared__ int red[40];
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
+  uint2* win = reinterpret_cast<uint2*>(smem + hot_bytes + (xz_in_smem ? xz_bytes : 0));
   for (int i = blockIdx.x; i < ndesc; i += gridDim.x) {
     const TraceDescU8 td = descs[i];
     TGroupU8<DD, CtaTeam> e(xz, hot, td.c.n, td.c.d, CtaTeam(red));
-    trace_program_u8(td, e, status);
+    trace_program_u8(td, e, win, status);
     __syncthreads();
   }
 }
@@ -27,13 +28,14 @@ __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const Trace
 // One program per CTA pair (cluster of two, grid-stride over programs).
 template <int DD>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTracePassThreads)
-    k_trace_pass_split(const TraceDescU8* __restrict__ descs, int ndesc, int* status) {
+    k_trace_pass_split(const TraceDescU8* __restrict__ descs, int ndesc, size_t win_off, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int red[40];
+  uint2* win = reinterpret_cast<uint2*>(smem + win_off);
   for (int i = (int)(blockIdx.x >> 1); i < ndesc; i += (int)(gridDim.x >> 1)) {
     const TraceDescU8 td = descs[i];
     SplitU8<DD> e(smem, td.c.n, td.c.d, red);
-    split_program(td, e, status);
+    split_program(td, e, win, status);
   }
 }
 
@@ -55,12 +57,13 @@ struct TraceU8 {
     if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_split<DD>, optin);
     return e != cudaSuccess ? e : set_dynamic_smem(k_phase_pass_u8<DD>, optin);
   }
-  static void split(int pairs, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, int* status) {
-    k_trace_pass_split<DD><<<2 * pairs, kTracePassThreads, smem, s>>>(d, nd, status);
+  static void split(int pairs, size_t smem, size_t scratch_off, cudaStream_t s, const TraceDescU8* d, int nd,
+                    int* status) {
+    k_trace_pass_split<DD><<<2 * pairs, kTracePassThreads, smem, s>>>(d, nd, scratch_off, status);
   }
-  static void xz(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
-                 size_t hot, int in_smem, int* status) {
-    k_trace_pass_u8<DD><<<grid, kTracePassThreads, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, status);
+  static void xz(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
+                 size_t xzb, size_t hot, int in_smem, int* status) {
+    k_trace_pass_u8<DD><<<grid, block, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, status);
   }
   static void phase(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, long long total,
                     int* status) {
@@ -84,24 +87,25 @@ size_t trace_u8_hot_bytes(int n) { return round16(SlotGroupU8::hot_bytes(n)); }
 size_t trace_u8_xz_bytes(int n) { return round16(SlotGroupU8::xz_bytes(n)); }
 size_t trace_u8_phase_smem(int n) { return round16(phase_u8_smem(n)); }
 size_t trace_u8_split_smem(int n) { return round16(split_smem_bytes(n)); }
+size_t trace_u8_window_bytes() { return sizeof(uint2) * kOpWindow; }
 
-void launch_trace_u8_split(int variant, int pairs, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
-                           int* status) {
+void launch_trace_u8_split(int variant, int pairs, size_t smem, size_t scratch_off, cudaStream_t s,
+                           const TraceDescU8* d, int nd, int* status) {
   switch (variant) {
-    case 0: TraceU8<3>::split(pairs, smem, s, d, nd, status); break;
-    case 1: TraceU8<5>::split(pairs, smem, s, d, nd, status); break;
-    case 2: TraceU8<7>::split(pairs, smem, s, d, nd, status); break;
-    default: TraceU8<0>::split(pairs, smem, s, d, nd, status); break;
+    case 0: TraceU8<3>::split(pairs, smem, scratch_off, s, d, nd, status); break;
+    case 1: TraceU8<5>::split(pairs, smem, scratch_off, s, d, nd, status); break;
+    case 2: TraceU8<7>::split(pairs, smem, scratch_off, s, d, nd, status); break;
+    default: TraceU8<0>::split(pairs, smem, scratch_off, s, d, nd, status); break;
   }
 }
 
-void launch_trace_u8_xz(int variant, int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+void launch_trace_u8_xz(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
                         uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status) {
   switch (variant) {
-    case 0: TraceU8<3>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
-    case 1: TraceU8<5>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
-    case 2: TraceU8<7>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
-    default: TraceU8<0>::xz(grid, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 0: TraceU8<3>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 1: TraceU8<5>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 2: TraceU8<7>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    default: TraceU8<0>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
   }
 }
 

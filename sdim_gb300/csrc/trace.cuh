@@ -116,6 +116,7 @@ constexpr int kTraceWinSteps = 512;
 constexpr int kTraceWinOps = 2048;
 inline size_t trace_pass_window_bytes() { return (size_t)16 * (kTraceWinSteps + kTraceWinOps); }
 
+
 // Shared-memory bytes of one x / z pass CTA (hot part, x / z part).
 size_t trace_pass_hot_bytes(int n);
 size_t trace_pass_xz_bytes(int n);
@@ -146,12 +147,17 @@ cudaError_t trace_u8_set_smem(int optin);
 size_t trace_u8_hot_bytes(int n);
 size_t trace_u8_xz_bytes(int n);
 size_t trace_u8_phase_smem(int n);
-void launch_trace_u8_xz(int variant, int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+void launch_trace_u8_xz(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
                         uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status);
-// x / z pass on CTA pairs (trace_split_u8.cuh): `pairs` clusters of two.
+// x / z pass on CTA pairs (trace_split_u8.cuh): `pairs` clusters of two,
+// the instruction window at trace_u8_split_smem(nmax),
+// smem = that + trace_u8_window_bytes().
 size_t trace_u8_split_smem(int n);
-void launch_trace_u8_split(int variant, int pairs, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
-                           int* status);
+// Shared memory of the instruction window both odd-d x / z passes keep after
+// their tableau.
+size_t trace_u8_window_bytes();
+void launch_trace_u8_split(int variant, int pairs, size_t smem, size_t scratch_off, cudaStream_t s,
+                           const TraceDescU8* d, int nd, int* status);
 void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
                            int nd, long long total, int* status);
 

@@ -43,8 +43,12 @@ __device__ __forceinline__ void st_peer_u32(uint32_t addr, uint32_t v) {
   asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 
-// Local column stride: a multiple of 4 bytes.
-__host__ __device__ inline int split_stride(int n) { return (n + 3) & ~3; }
+// Local column stride: a multiple of 4 bytes with an odd word count, so the
+// 32 rows a warp walks down one column sit in 32 different banks.
+__host__ __device__ inline int split_stride(int n) {
+  const int s = (n + 3) & ~3;
+  return ((s >> 2) & 1) ? s : s + 4;
+}
 
 // Bytes of an exchange buffer: ints p, s1, phc, ex, then cx[np], cz[np], f[np].
 __host__ __device__ inline int split_xchg_bytes(int n) { return 16 + 3 * SlotU8::npad(n); }
@@ -420,16 +424,20 @@ __device__ void split_measure(SplitU8<DD>& e, const TraceDescU8& td, int q, uint
 
 // Runs the shared part of td's program on the CTA pair and writes its trace.
 template <int DD>
-__device__ void split_program(const TraceDescU8& td, SplitU8<DD>& e, int* status) {
+__device__ void split_program(const TraceDescU8& td, SplitU8<DD>& e, uint2* win, int* status) {
   const CircuitDesc& c = td.c;
   e.init();
   const int t = e.tm.t, size = e.tm.size();
   const int n = c.n, d = c.d, SL = e.SL, sw = td.sw, r = e.r;
   uint32_t mord = 0, nord = 0;
-  uint2 nxt = (c.nops > 0) ? __ldg(c.ops) : make_uint2(0u, 0u);
   for (int i = 0; i < c.nops; ++i) {
-    const uint2 cur = nxt;
-    if (i + 1 < c.nops) nxt = __ldg(c.ops + i + 1);
+    if ((i & (kOpWindow - 1)) == 0) {  // stage the next window of instructions
+      e.tm.sync();
+      const int cnt = min(kOpWindow, c.nops - i);
+      for (int j = t; j < cnt; j += size) win[j] = __ldg(c.ops + i + j);
+      e.tm.sync();
+    }
+    const uint2 cur = win[i & (kOpWindow - 1)];
     const uint32_t op = cur.x & kOpMask;
     const int q = (int)(cur.x >> 8);
     // both CTAs read the same stream and leave at the same instruction
@@ -505,5 +513,6 @@ __device__ void split_program(const TraceDescU8& td, SplitU8<DD>& e, int* status
   e.tm.sync();
   cluster_sync_all();  // neither CTA leaves while its partner may still write into it
 }
+
 
 }  // namespace sdim

@@ -149,18 +149,26 @@ __device__ void trace_measure_u8(TGroupU8<DD, Team>& e, const TraceDescU8& td, i
   }
 }
 
-// Runs the shared part of td's program and writes its trace.
+// Instructions the odd-d x / z passes stage in shared memory at a time.
+constexpr int kOpWindow = 512;
+
+// Runs the shared part of td's program and writes its trace; win: room for
+// kOpWindow instructions in shared memory.
 template <int DD, class Team>
-__device__ void trace_program_u8(const TraceDescU8& td, TGroupU8<DD, Team>& e, int* status) {
+__device__ void trace_program_u8(const TraceDescU8& td, TGroupU8<DD, Team>& e, uint2* win, int* status) {
   const CircuitDesc& c = td.c;
   e.init(0);
   const int t = e.tm.t, size = e.tm.size();
   const int n = c.n, d = c.d, S = e.S, sw = td.sw;
   uint32_t mord = 0, nord = 0;
-  uint2 nxt = (c.nops > 0) ? __ldg(c.ops) : make_uint2(0u, 0u);
   for (int i = 0; i < c.nops; ++i) {
-    const uint2 cur = nxt;
-    if (i + 1 < c.nops) nxt = __ldg(c.ops + i + 1);
+    if ((i & (kOpWindow - 1)) == 0) {  // stage the next window of instructions
+      e.tm.sync();
+      const int cnt = min(kOpWindow, c.nops - i);
+      for (int j = t; j < cnt; j += size) win[j] = __ldg(c.ops + i + j);
+      e.tm.sync();
+    }
+    const uint2 cur = win[i & (kOpWindow - 1)];
     const uint32_t op = cur.x & kOpMask;
     const int q = (int)(cur.x >> 8);
     if (q >= n) {
@@ -306,6 +314,11 @@ __device__ void phase_program_u8(const TraceDescU8* __restrict__ tdp, long long 
     }
     const uint8_t* row = rows + (size_t)(k & 1) * 2 * sw;
     const bool det = h.x & 1u;
+    // d in {3, 5, 7}: four residues per 32-bit word (packed_mod, __dp4a)
+    constexpr bool kPacked = DD == 3 || DD == 5 || DD == 7;
+    uint32_t* dw = reinterpret_cast<uint32_t*>(ds);
+    const uint32_t* rw = reinterpret_cast<const uint32_t*>(row);
+    const int nw2 = (2 * n + 3) >> 2, nw1 = (n + 3) >> 2;
     if (!det) {
       const int p = (int)h.y, ex = (int)(h.x >> 8);
       if (ex != 1) {
@@ -313,11 +326,19 @@ __device__ void phase_program_u8(const TraceDescU8* __restrict__ tdp, long long 
         __syncthreads();
       }
       const int dp = ds[p];  // the rowsum below never writes generator p (FW_p = 0)
-      if (dp)
-        for (int g = ch; g < 2 * n; g += nch) {
-          const int f = row[g];
-          if (f) ds[g] = (uint8_t)M.mo(ds[g] + f * dp);
+      if (dp) {
+        if constexpr (kPacked) {
+          for (int w = ch; w < nw2; w += nch) {
+            const uint32_t fw = rw[w];
+            if (fw) dw[w] = packed_mod<DD>(dw[w] + fw * (uint32_t)dp);
+          }
+        } else {
+          for (int g = ch; g < 2 * n; g += nch) {
+            const int f = row[g];
+            if (f) ds[g] = (uint8_t)M.mo(ds[g] + f * dp);
+          }
         }
+      }
       __syncthreads();
       if (ch == 0) {
         const int m = live ? mulshift(stream_block(c.seed, shot, (uint32_t)k, 0u).x, (uint32_t)d) : 0;
@@ -329,9 +350,14 @@ __device__ void phase_program_u8(const TraceDescU8* __restrict__ tdp, long long 
       if (ch == 0) shot_acc[s] = 0;
       __syncthreads();
       int acc = 0;
-      for (int i = ch; i < n; i += nch) {
-        const int f = row[i];
-        if (f) acc += f * ds[i];
+      if constexpr (kPacked) {
+        // factor bytes past n are zero, so whole words of the first n generators add up
+        for (int w = ch; w < nw1; w += nch) acc = (int)__dp4a(rw[w], dw[w], (unsigned)acc);
+      } else {
+        for (int i = ch; i < n; i += nch) {
+          const int f = row[i];
+          if (f) acc += f * ds[i];
+        }
       }
       if (acc) atomicAdd(&shot_acc[s], acc);
       __syncthreads();
@@ -341,7 +367,15 @@ __device__ void phase_program_u8(const TraceDescU8* __restrict__ tdp, long long 
     const int m = shot_m[s];
     if ((h.x & 2u) && m) {
       const uint8_t* zq = row + sw;
-      for (int g = ch; g < 2 * n; g += nch) ds[g] = (uint8_t)M.mo(ds[g] + M.phi * m * zq[g]);
+      if constexpr (kPacked) {
+        const uint32_t* zw = reinterpret_cast<const uint32_t*>(zq);
+        for (int w = ch; w < nw2; w += nch) {
+          const uint32_t z = zw[w];
+          if (z) dw[w] = packed_mod<DD>(dw[w] + z * (uint32_t)m);
+        }
+      } else {
+        for (int g = ch; g < 2 * n; g += nch) ds[g] = (uint8_t)M.mo(ds[g] + M.phi * m * zq[g]);
+      }
     }
     if (ch == 0 && live && k < c.nmeas) out[k] = (uint8_t)(m | ((int)det << 7));
     __syncthreads();  // the deltas are final, and buffer k & 1 is free for measurement k + 2
