@@ -342,13 +342,14 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     }
     if ((rc = ensure(ctx, ctx->trace, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
     if ((rc = ensure(ctx, ctx->tdescs, sizeof(TraceDesc) * k)) != SDIM_OK) return rc;
-    // fire masks: a word pair per 32 N1 ordinals per shot, within a budget
+    // fire masks: a word pair per 32 N1 ordinals per shot and the chunk map,
+    // within a budget
     constexpr size_t kMaskBudget = (size_t)1 << 30;
     std::vector<size_t> moff(k, SIZE_MAX);
     size_t mtotal = 0;
     for (size_t i = 0; i < k; ++i) {
-      const size_t nchunk = ((size_t)jobs[i].c->nn1_used + kCoinChunk - 1) / kCoinChunk;
-      const size_t b = round_up(nchunk * (size_t)jobs[i].nshots * 8, 256);
+      const long long nchunk = ((long long)jobs[i].c->nn1_used + kCoinChunk - 1) / kCoinChunk;
+      const size_t b = coin_mask_bytes(nchunk, jobs[i].nshots) + coin_map_bytes(nchunk, jobs[i].nshots);
       if (nchunk && mtotal + b <= kMaskBudget && !(flags & SDIM_FLAG_NO_COIN_PASS)) {
         moff[i] = mtotal;
         mtotal += b;
@@ -390,6 +391,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       if (moff[i] != SIZE_MAX) {
         td.masks = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(ctx->masks.p) + moff[i]);
         td.nchunk = (j.c->nn1_used + kCoinChunk - 1) / kCoinChunk;
+        td.cmap = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(td.masks) +
+                                              coin_mask_bytes(td.nchunk, j.nshots));
         coins += (long long)((td.nchunk + kCoinChunksPerItem - 1) / kCoinChunksPerItem) * j.nshots;
       }
       td.nm = j.c->nmeas;

@@ -31,14 +31,17 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
 // control are provably warp-uniform, so they stay out of the per-lane
 // registers.
 template <int TW>
-__global__ void __launch_bounds__(32) k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc,
+__global__ void __launch_bounds__(32, 32) k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc,
                                                    long long total_groups, const int* status) {
   __shared__ uint8_t rec[32 * kRecStride];
   if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
   const long long g = blockIdx.x;
   if (g >= total_groups) return;
   const int i = find_trace_desc(descs, ndesc, g);
-  phase_program<TW>(descs + i, g - descs[i].c.item_begin, threadIdx.x, rec);
+  if (descs[i].masks)
+    phase_program<TW, true>(descs + i, g - descs[i].c.item_begin, threadIdx.x, rec);
+  else
+    phase_program<TW, false>(descs + i, g - descs[i].c.item_begin, threadIdx.x, rec);
 }
 
 // One thread per (chunk group, shot) item of the coin pass; descs with

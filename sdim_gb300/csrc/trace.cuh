@@ -28,7 +28,9 @@ namespace sdim {
 // 0xffffffff) and nhdr[j] = (threshold, opcode).  masks, when not null,
 // holds the fired Paulis of every shot as word pairs, pair c * nshots + s:
 // bit i of the first word = N1 ordinal 32 c + i of shot s applied X^a with
-// a odd, of the second = Z^b with b odd (written by the coin pass).
+// a odd, of the second = Z^b with b odd (written by the coin pass), and
+// cmap its chunk map: bit i of word w * nshots + s set when pair (32 w + i)
+// of shot s is not zero (bits at or past nchunk are undefined).
 struct TraceDesc {
   CircuitDesc c;  // item_begin counts 32-shot groups of the phase pass
   const uint4* steps;
@@ -40,6 +42,7 @@ struct TraceDesc {
   uint32_t* mrow;
   uint32_t* nrow;
   uint32_t* masks;
+  uint32_t* cmap;
   long long coin_begin;  // first coin-pass item of this program
   int nsteps;
   int nwins;
@@ -69,8 +72,17 @@ __host__ __device__ inline size_t trace_bytes(int nm, int nn1, int tw) {
 
 // Chunks of 32 N1 ordinals of one shot's fire mask.
 constexpr int kCoinChunk = 32;
-// Chunks one coin-pass thread fills.
+// Chunks one coin-pass thread fills (one byte of the chunk map).
 constexpr int kCoinChunksPerItem = 8;
+
+// Bytes of the fire masks and of the chunk map of one program (each
+// 256-byte aligned).
+__host__ __device__ inline size_t coin_mask_bytes(long long nchunk, long long nshots) {
+  return round_up((size_t)nchunk * (size_t)nshots * 8, 256);
+}
+__host__ __device__ inline size_t coin_map_bytes(long long nchunk, long long nshots) {
+  return round_up((size_t)((nchunk + 31) / 32) * (size_t)nshots * 4, 256);
+}
 
 // Trace of one odd-d program (layout in trace_u8.cuh); N1 coins are drawn in
 // its phase pass.

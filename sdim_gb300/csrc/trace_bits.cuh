@@ -401,10 +401,15 @@ __device__ __forceinline__ void load_row(const uint32_t* p, uint32_t (&r)[N]) {
   }
 }
 
+// Delta of a d = 2 shot is a multiple of 2 mod 4 at every point: it starts
+// at 0, and every update adds 2 (a z_q + b x_q) (N1), 2 m z_q (RESET), 2 m
+// (the new delta_p) or f_g delta_p with delta_p already even.  So only its
+// high bit plane is kept: d1, one bit per generator.
+//
 // Registers hold what every measurement uses (header and row pointers, the
-// shot, delta); the arrays of the N1 paths are read from the descriptor when
-// a coin chunk or a fire needs them.  The next measurement's header and
-// factor half-row are loaded one iteration ahead.
+// shot, d1); the arrays of the N1 paths are read from the descriptor when a
+// fire needs them.  The next measurement's header and factor half-row are
+// loaded one iteration ahead.
 // Records are staged per warp in shared memory, rec[32][kRecStride] bytes
 // (row = lane, column = measurement mod 64; 17 words per row keep the lanes
 // on distinct banks), and every 64 measurements the warp writes each shot's
@@ -426,7 +431,74 @@ __device__ __forceinline__ void flush_records(const uint8_t* rec, uint8_t* __res
   __syncwarp();
 }
 
-template <int TW>
+// Word w of d, w warp-uniform: a tree of uniform branches rather than a
+// compare and select per word.
+template <int LO, int HI, int TW>
+__device__ __forceinline__ uint32_t word_at(const uint32_t (&d)[TW], int w) {
+  if constexpr (HI - LO == 1) {
+    return d[LO];
+  } else {
+    constexpr int MID = (LO + HI) / 2;
+    if (w < MID) return word_at<LO, MID>(d, w);
+    return word_at<MID, HI>(d, w);
+  }
+}
+
+// Sets bit b of word w of d to v (w warp-uniform, v in {0, 1}).
+template <int LO, int HI, int TW>
+__device__ __forceinline__ void put_bit(uint32_t (&d)[TW], int w, int b, uint32_t v) {
+  if constexpr (HI - LO == 1) {
+    d[LO] = (d[LO] & ~(1u << b)) | (v << b);
+  } else {
+    constexpr int MID = (LO + HI) / 2;
+    if (w < MID)
+      put_bit<LO, MID>(d, w, b, v);
+    else
+      put_bit<MID, HI>(d, w, b, v);
+  }
+}
+
+// The next N1 fire of one shot, read from the coin pass's chunk map and
+// fire masks: a shot with F fires loads F mask pairs and its chunk-map
+// words, and a measurement with no fire before it costs one compare.
+struct FireCursor {
+  const uint2* masks;
+  const uint32_t* cmap;
+  int nshots, rel, nchunk, ncw;
+  int cw;           // chunk-map word in use
+  uint32_t cbits;   // its chunks not yet loaded
+  uint32_t ax, bz;  // masks of the loaded chunk, applied fires cleared
+  uint32_t base;    // first ordinal of the loaded chunk
+  uint32_t next;    // ordinal of the next fire, 0xffffffff when there is none
+
+  __device__ __forceinline__ void advance() {
+    uint32_t pend = ax | bz;
+    while (!pend) {
+      while (!cbits) {
+        if (++cw >= ncw) {
+          next = 0xffffffffu;
+          return;
+        }
+        cbits = __ldg(cmap + (size_t)cw * nshots + rel);
+        if (cw == ncw - 1 && (nchunk & 31)) cbits &= (1u << (nchunk & 31)) - 1u;
+      }
+      const int b = __ffs(cbits) - 1;
+      cbits &= cbits - 1u;
+      const int c = 32 * cw + b;
+      const uint2 m = __ldg(masks + (size_t)c * nshots + rel);
+      ax = m.x;
+      bz = m.y;
+      base = 32u * (uint32_t)c;
+      pend = ax | bz;
+    }
+    next = base + (uint32_t)(__ffs(pend) - 1);
+  }
+};
+
+// One 32-shot group of a program (lane = shot).  With coin-pass masks
+// (kMasks) the N1 fires come from a FireCursor; without, the coins of each
+// 32-ordinal chunk are drawn here when the replay reaches it.
+template <int TW, bool kMasks>
 __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp, long long group, int lane,
                                               uint8_t* rec) {
   constexpr int FH = TW / 2;  // factor words of a deterministic measurement
@@ -445,20 +517,24 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
   uint8_t* __restrict__ gout = tdp->c.out + first * (long long)nmeas;
   uint8_t* myrec = rec + lane * kRecStride;
   const PhiloxKeys K(seed);
-  uint32_t d0[TW], d1[TW];
+  uint32_t d1[TW];
 #pragma unroll
-  for (int w = 0; w < TW; ++w) d0[w] = d1[w] = 0u;
-  // N1 ordinals [nord, cend) of the current 32-ordinal chunk are not yet
-  // replayed; bit i of pend is ordinal nord + i.  With coin-pass masks the
-  // next chunk's word is loaded one chunk ahead.
-  uint32_t nord = 0, cend = 0, pend = 0u, pendz = 0u;
-  const uint2* __restrict__ masks = reinterpret_cast<const uint2*>(tdp->masks);
-  const int nchunk = tdp->nchunk;
-  const int nshots = tdp->c.nshots;
-  uint2 q1 = make_uint2(0u, 0u), q2 = make_uint2(0u, 0u);  // masks of the next two chunks
-  if (masks && active) {
-    if (nchunk > 0) q1 = __ldg(masks + rel);
-    if (nchunk > 1) q2 = __ldg(masks + (size_t)nshots + rel);
+  for (int w = 0; w < TW; ++w) d1[w] = 0u;
+  FireCursor fc;
+  // without masks: N1 ordinals [nord, cend) of the current 32-ordinal chunk
+  // are not yet replayed; bit i of pend is ordinal nord + i
+  uint32_t nord = 0, cend = 0, pend = 0u;
+  if constexpr (kMasks) {
+    fc.masks = reinterpret_cast<const uint2*>(tdp->masks);
+    fc.cmap = tdp->cmap;
+    fc.nshots = tdp->c.nshots;
+    fc.rel = (int)rel;
+    fc.nchunk = tdp->nchunk;
+    fc.ncw = (tdp->nchunk + 31) >> 5;
+    fc.cw = -1;
+    fc.cbits = fc.ax = fc.bz = fc.base = 0u;
+    fc.next = 0xffffffffu;
+    if (active) fc.advance();
   }
   uint4 hn = make_uint4(0u, 0u, 0u, 0u);
   uint32_t fn[FH];
@@ -480,92 +556,65 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
       if (k + 1 < nm) hn = __ldg(mhdr + k + 1);
     }
     const uint32_t nend = h.z < nn1 ? h.z : nn1;
-    while (nord < nend) {
-      if (nord == cend) {
-        if (masks) {
-          const int c = (int)(nord >> 5);
-          pend = q1.x;
-          pendz = q1.y;
-          q1 = q2;
-          q2 = (active && c + 2 < nchunk) ? __ldg(masks + (size_t)(c + 2) * nshots + rel) : make_uint2(0u, 0u);
-        } else {
-          // no masks: draw the coins here, the Paulis on a fire below
-          pend = coin_mask(K, tdp->nthr, nord, shot_lo, shot_hi);
-          pendz = 0xffffffffu;
-        }
-        cend = nord + 32;
-      }
-      const uint32_t hi = nend < cend ? nend : cend;
-      const uint32_t take = hi - nord;  // 1 .. 32
-      const uint32_t lim = take >= 32 ? 0xffffffffu : ((1u << take) - 1u);
-      uint32_t due = masks ? ((pend | pendz) & lim) : (pend & lim);
-      const uint32_t ax = pend, bz = pendz;
-      pend = take >= 32 ? 0u : (pend >> take);
-      pendz = take >= 32 ? 0u : (pendz >> take);
-      if (!active) due = 0u;
-      while (due) {
-        const int i = __ffs(due) - 1;
-        due &= due - 1u;
-        const uint32_t j = nord + (uint32_t)i;
-        uint32_t mz, mx;
-        if (masks) {
-          mz = ((ax >> i) & 1u) ? 0xffffffffu : 0u;
-          mx = ((bz >> i) & 1u) ? 0xffffffffu : 0u;
-        } else {
-          const uint2 nh = __ldg(tdp->nhdr + j);
-          if (nh.y == OP_N1OFF) continue;  // threshold 0xffffffff: a coin of 0xffffffff is not a fire
-          const int2 ab = noise_choice(nh.y, 2, seed, shot, j);
-          mz = ab.x ? 0xffffffffu : 0u;
-          mx = (ab.y & 1) ? 0xffffffffu : 0u;
-        }
+    if constexpr (kMasks) {
+      while (fc.next < nend) {
+        const uint32_t j = fc.next, bit = 1u << (j & 31u);
+        const uint32_t mz = (fc.ax & bit) ? 0xffffffffu : 0u, mx = (fc.bz & bit) ? 0xffffffffu : 0u;
+        fc.ax &= ~bit;
+        fc.bz &= ~bit;
         const uint32_t* nr = tdp->nrow + (size_t)j * 2 * TW;
 #pragma unroll
         for (int w = 0; w < TW; ++w) d1[w] ^= (__ldg(nr + TW + w) & mz) ^ (__ldg(nr + w) & mx);
+        fc.advance();
       }
-      nord = hi;
+    } else {
+      while (nord < nend) {
+        if (nord == cend) {
+          // the Paulis are drawn on a fire below
+          pend = coin_mask(K, tdp->nthr, nord, shot_lo, shot_hi);
+          cend = nord + 32;
+        }
+        const uint32_t hi = nend < cend ? nend : cend;
+        const uint32_t take = hi - nord;  // 1 .. 32
+        const uint32_t lim = take >= 32 ? 0xffffffffu : ((1u << take) - 1u);
+        uint32_t due = active ? (pend & lim) : 0u;
+        pend = take >= 32 ? 0u : (pend >> take);
+        while (due) {
+          const int i = __ffs(due) - 1;
+          due &= due - 1u;
+          const uint32_t j = nord + (uint32_t)i;
+          const uint2 nh = __ldg(tdp->nhdr + j);
+          if (nh.y == OP_N1OFF) continue;  // threshold 0xffffffff: a coin of 0xffffffff is not a fire
+          const int2 ab = noise_choice(nh.y, 2, seed, shot, j);
+          const uint32_t mz = ab.x ? 0xffffffffu : 0u, mx = (ab.y & 1) ? 0xffffffffu : 0u;
+          const uint32_t* nr = tdp->nrow + (size_t)j * 2 * TW;
+#pragma unroll
+          for (int w = 0; w < TW; ++w) d1[w] ^= (__ldg(nr + TW + w) & mz) ^ (__ldg(nr + w) & mx);
+        }
+        nord = hi;
+      }
     }
     const uint32_t* row = mrow + (size_t)k * 2 * TW;
     const uint32_t det = h.x & 1u;
     int m;
     if (!det) {
-      const int p = (int)h.y, wp = p >> 5, bp = p & 31, wd = wn + wp;
-      const uint32_t pbit = 1u << bp;
-      uint32_t a0 = 0u, a1 = 0u;
+      // delta_g += delta_p (g in the factor row), delta_{n+p} = delta_p,
+      // delta_p = 2 m
+      const int p = (int)h.y, wp = p >> 5, bp = p & 31;
+      const uint32_t dp = (word_at<0, TW>(d1, wp) >> bp) & 1u;
+      if (dp) {
 #pragma unroll
-      for (int w = 0; w < TW; ++w)
-        if (w == wp) {
-          a0 = d0[w];
-          a1 = d1[w];
-        }
-      const uint32_t dp0 = (a0 >> bp) & 1u, dp1 = (a1 >> bp) & 1u;
-      if (dp0 | dp1) {
-        const uint32_t m0 = 0u - dp0, m1 = 0u - dp1;
-#pragma unroll
-        for (int w = 0; w < TW; ++w) {
-          const uint32_t F = __ldg(row + w);
-          const uint32_t lo = d0[w], a = F & m0;
-          d0[w] = lo ^ a;
-          d1[w] ^= (F & m1) ^ (lo & a);
-        }
+        for (int w = 0; w < TW; ++w) d1[w] ^= __ldg(row + w);
       }
       m = active ? mulshift(K.block(make_uint4((uint32_t)k, shot_lo, shot_hi, 0u)).x, 2u) : 0;
-#pragma unroll
-      for (int w = 0; w < TW; ++w) {
-        if (w == wd) {
-          d0[w] = (d0[w] & ~pbit) | (dp0 << bp);
-          d1[w] = (d1[w] & ~pbit) | (dp1 << bp);
-        }
-        if (w == wp) {
-          d0[w] &= ~pbit;
-          d1[w] = (d1[w] & ~pbit) | ((uint32_t)m << bp);
-        }
-      }
+      put_bit<0, TW>(d1, wn + wp, bp, dp);
+      put_bit<0, TW>(d1, wp, bp, (uint32_t)m);
     } else {
       if constexpr (!kAhead) load_row<FH>(row, f);
-      int sacc = 0;
+      int s = 0;
 #pragma unroll
-      for (int w = 0; w < FH; ++w) sacc += __popc(f[w] & d0[w]) + 2 * __popc(f[w] & d1[w]);
-      m = (((((int)h.w + sacc) & 3) + 1) >> 1) & 1;
+      for (int w = 0; w < FH; ++w) s += __popc(f[w] & d1[w]);
+      m = (((((int)h.w + 2 * s) & 3) + 1) >> 1) & 1;
     }
     if ((h.x & 2u) && (m & 1)) {
 #pragma unroll
@@ -584,6 +633,8 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
 // so masks[c * nshots + s] = (x mask, z mask): bit i of .x set when ordinal
 // 32 c + i applies X^a with a odd (the phase update reads z_q), of .y when it
 // applies Z^b with b odd (reads x_q); an N1 with probability 0 never fires.
+// The item's byte of the chunk map (byte cg % 4 of word cg / 4) marks which
+// of its chunks have a non-zero pair.
 __device__ __forceinline__ void coin_item(const TraceDesc* __restrict__ tdp, long long it) {
   const int nshots = tdp->c.nshots;
   const long long cg = it / nshots;
@@ -596,6 +647,7 @@ __device__ __forceinline__ void coin_item(const TraceDesc* __restrict__ tdp, lon
   const int nchunk = tdp->nchunk;
   const int c0 = (int)cg * kCoinChunksPerItem;
   const int c1 = min(nchunk, c0 + kCoinChunksPerItem);
+  uint32_t any = 0u;
   for (int c = c0; c < c1; ++c) {
     const uint32_t cb = (uint32_t)c * kCoinChunk;
     uint32_t f = coin_mask(K, nthr, cb, (uint32_t)(unsigned long long)shot, (uint32_t)((unsigned long long)shot >> 32));
@@ -610,7 +662,9 @@ __device__ __forceinline__ void coin_item(const TraceDesc* __restrict__ tdp, lon
       bz |= (uint32_t)(ab.y & 1) << i;
     }
     out[(size_t)c * nshots] = make_uint2(ax, bz);
+    any |= (uint32_t)((ax | bz) != 0u) << (c - c0);
   }
+  reinterpret_cast<uint8_t*>(tdp->cmap + (size_t)(cg >> 2) * nshots + rel)[cg & 3] = (uint8_t)any;
 }
 
 __device__ __forceinline__ int find_coin_desc(const TraceDesc* descs, int ndesc, long long it) {
