@@ -104,6 +104,17 @@ int sdim_run(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t sho
  * NULL for the context's stream) and out on the device. */
 int sdim_run_device(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot0,
                     int64_t nshots, uint8_t* out_dev, void* stream, unsigned flags);
+/* The reference's multi-shot route, Program.simulate(shots) without
+ * record_tableau / force_tableau (sdim/program.py:244-265): row 0 of out is
+ * shot 0 of ref (the same program encoded with every N1 as the identity, as
+ * the reference's tableau shot treats it, sdim/program.py:31) run on the
+ * tableau engines; rows 1 .. nshots-1 propagate Pauli frames of circ against
+ * it (simulate_frame, sdim/program.py:45-165) with the noise of circ.  out
+ * holds nshots x records bytes (host memory unless SDIM_FLAG_OUT_DEVICE).
+ * SDIM_EINVAL when circ and ref differ in n, d or records; SDIM_EUNSUPPORTED
+ * when 64 n bytes of frames do not fit in a block's shared memory. */
+int sdim_frame_run(sdim_ctx* ctx, const sdim_circuit* circ, const sdim_circuit* ref, uint64_t seed,
+                   int64_t nshots, uint8_t* out, unsigned flags);
 /* Many programs (uneven n, d, depth, shots) in persistent launches fed by a
  * device work queue.  outs[i] holds nshots[i] x records(circs[i]) bytes.
  * The reference has no batch API; it is Program.simulate called once per program. */

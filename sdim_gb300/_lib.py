@@ -59,6 +59,7 @@ SIGNATURES = {
     "sdim_circuit_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "sdim_run": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, C.c_uint]),
     "sdim_run_device": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, _P, C.c_uint]),
+    "sdim_frame_run": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_int64, _P, C.c_uint]),
     "sdim_run_batch": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.c_uint]),
     "sdim_sync": (C.c_int, [_P]),
     "sdim_query": (C.c_int, [_P]),

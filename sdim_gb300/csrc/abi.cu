@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/sdim_gb300.h"
+#include "frame.cuh"
 #include "kernels.cuh"
 #include "trace.cuh"
 #include "variants.cuh"
@@ -50,6 +51,7 @@ struct sdim_ctx {
   double stage_ms[3] = {0.0, 0.0, 0.0};  // x / z passes, phase passes, other engines
   int smem_attr_set[V_COUNT] = {};
   bool trace_smem_set = false;
+  bool frame_smem_set = false;
   int trace_threads = kTracePassThreads;  // x / z pass CTA size (SDIM_TRACE_PASS_THREADS: 256 or 512)
 };
 
@@ -78,6 +80,8 @@ struct sdim_circuit {
   const uint32_t* d_nthr = nullptr;  // N1 coin thresholds, padded to a multiple of 64 with 0xffffffff
   const uint2* d_nhdr = nullptr;     // N1 (threshold, opcode)
   int nsteps = 0, nwins = 0, nn1_used = 0;
+  int64_t fops_off = 0;  // frame instruction stream (frame.cuh), inside the blob
+  int nfops = 0;
 };
 
 namespace {
@@ -863,6 +867,32 @@ void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int 
   if (dev.size() & 1) dev.push_back(make_uint2(0u, 0u));
 }
 
+// Frame instruction stream (frame.cuh) of rows already checked by
+// encode_rows, appended to dev: one word per instruction other than the
+// identity (sdim/program.py:479-480 leaves I out of the frame walk).
+void append_frame_ops(const int32_t* ops, int64_t nops, const double* noise_prob, std::vector<uint2>& dev,
+                      int64_t& off, int& count) {
+  off = (int64_t)dev.size();
+  for (int64_t i = 0; i < nops; ++i) {
+    const int id = ops[4 * i], q = ops[4 * i + 1], t = ops[4 * i + 2], ch = ops[4 * i + 3];
+    if (id == 0) continue;
+    uint32_t code = (uint32_t)id, y = 0;
+    if (id >= 9 && id <= 13) y = (uint32_t)t;
+    if (id == 17) {
+      const double p = noise_prob ? noise_prob[i] : 0.01;
+      const double thr = std::floor((1.0 - p) * 4294967296.0);
+      if (thr >= 4294967296.0) {
+        code = OP_N1OFF;
+      } else {
+        code = ch == 1 ? OP_N1D : ch == 2 ? OP_N1F : OP_N1P;
+        y = thr <= 0.0 ? 0u : (uint32_t)thr;
+      }
+    }
+    dev.push_back(make_uint2(code | ((uint32_t)q << 8), y));
+  }
+  count = (int)((int64_t)dev.size() - off);
+}
+
 }  // namespace
 
 extern "C" {
@@ -1010,6 +1040,9 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
   const size_t ndev = dev.size();
   TraceSchedule sch;
   if (d == 2 && trace_words(n)) append_schedule(dev, 0, ndev, n, kTraceWinSteps, kTraceWinOps, sch);
+  int64_t fops_off = 0;
+  int nfops = 0;
+  append_frame_ops(ops, nops, noise_prob, dev, fops_off, nfops);
   cudaSetDevice(ctx->device);
   sdim_circuit* c = new sdim_circuit();
   c->device = ctx->device;
@@ -1050,6 +1083,8 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
     c->nwins = sch.nwins;
     c->nn1_used = sch.nn1_used;
   }
+  c->fops_off = fops_off;
+  c->nfops = nfops;
   *out = c;
   return SDIM_OK;
 }
@@ -1112,6 +1147,72 @@ int sdim_run(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot0,
   }
   if (bytes) CK(cudaMemcpyAsync(out, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->timing_pending) {
+    const int trc = collect_times(ctx);
+    if (trc != SDIM_OK) return trc;
+  }
+  return read_status(ctx);
+}
+
+int sdim_frame_run(sdim_ctx* ctx, const sdim_circuit* c, const sdim_circuit* ref, uint64_t seed, int64_t nshots,
+                   uint8_t* out, unsigned flags) {
+  if (!ctx || !c || !ref || nshots < 0 || (nshots > 0 && c->nmeas > 0 && !out))
+    return fail(ctx, SDIM_EINVAL, "bad argument to sdim_frame_run");
+  if (c->n != ref->n || c->d != ref->d || c->nmeas != ref->nmeas)
+    return fail(ctx, SDIM_EINVAL, "the reference-shot program does not match the frame program");
+  if (nshots > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one call");
+  if (nshots == 0) return SDIM_OK;
+  CK(cudaSetDevice(ctx->device));
+  const size_t smem = frame_smem_bytes(c->n);
+  if (nshots > 1 && smem > (size_t)ctx->smem_optin)
+    return fail(ctx, SDIM_EUNSUPPORTED, "too many qudits for the frame sampler's shared-memory frames");
+  if (!ctx->frame_smem_set) {
+    const cudaError_t e = frame_set_smem(ctx->smem_optin);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFuncSetAttribute");
+    ctx->frame_smem_set = true;
+  }
+  const bool dev_out = flags & SDIM_FLAG_OUT_DEVICE;
+  const size_t bytes = (size_t)nshots * c->nmeas;
+  int rc;
+  uint8_t* dst = out;
+  if (!dev_out) {
+    if ((rc = ensure(ctx, ctx->out, std::max<size_t>(bytes, 1))) != SDIM_OK) return rc;
+    dst = static_cast<uint8_t*>(ctx->out.p);
+    // host -> device: both instruction streams
+    CK(cudaMemcpyAsync(ref->d_ops, ref->h_ops, (size_t)ref->blob_words * sizeof(uint2), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(c->d_ops, c->h_ops, (size_t)c->blob_words * sizeof(uint2), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  }
+  cudaStream_t s = ctx->stream;
+  // shot 0: the noiseless tableau shot, into row 0
+  std::vector<Job> jobs{Job{ref, seed, 0, 1, dst}};
+  if ((rc = launch_jobs(ctx, jobs, s, flags & ~SDIM_FLAG_ASYNC)) != SDIM_OK) return rc;
+  // shots 1 .. nshots - 1: frames against row 0
+  if (nshots > 1 && c->nmeas > 0) {
+    FrameDesc fd;
+    fd.ops = c->d_ops + c->fops_off;
+    fd.ref = dst;
+    fd.out = dst + c->nmeas;
+    fd.seed = seed;
+    fd.shot0 = 1;
+    fd.nops = c->nfops;
+    fd.n = c->n;
+    fd.d = c->d;
+    fd.nmeas = c->nmeas;
+    fd.nshots = (int)(nshots - 1);
+    const long long grid = (nshots - 1 + 31) / 32;
+    launch_frame_pass((int)grid, smem, s, fd, static_cast<int*>(ctx->status.p));
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "frame pass launch");
+  }
+  if (dev_out) return finish(ctx, s, flags & ~SDIM_FLAG_ASYNC);
+  if (flags & SDIM_FLAG_TIME) {
+    CK(cudaEventRecord(ctx->ev1, s));
+    ctx->timing_pending = true;
+  }
+  if (bytes) CK(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
   if (ctx->timing_pending) {
     const int trc = collect_times(ctx);
     if (trc != SDIM_OK) return trc;

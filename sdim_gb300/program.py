@@ -4,21 +4,26 @@ Mirrors sdim/program.py:167-573: ``Program(circuit)``,
 ``simulate(shots, show_measurement, record_tableau, force_tableau, verbose,
 show_gate, exact, options)``, ``append_circuit``, ``measurement_results`` and
 the return shapes (flat list for one shot, ``[qudit][round][shot]``
-otherwise, sdim/program.py:355-365).  Every shot of every call runs the full
-tableau algorithm on the GPU through the C ABI; there is no CPU path.
+otherwise, sdim/program.py:355-365).  Every shot of every call runs on the
+GPU through the C ABI; there is no CPU path.
 
 Differences from the reference, by design:
 * outcomes of random measurements come from the Philox stream keyed by
   (seed, shot, measurement ordinal) instead of Python's ``random``
   (sdim/tableau/tableau_prime.py:332); ``seed`` is a keyword of ``simulate``;
-* N1 noise acts on the tableau (X^a then Z^b after the instruction); the
-  reference's tableau path treats N1 as the identity (sdim/program.py:31) and
-  samples noise only in its Pauli-frame route.  ``noise=False`` reproduces
-  the identity behaviour;
-* ``shots > 1`` runs every shot on the tableau (the reference switches to its
-  frame sampler unless ``force_tableau``), so shot 0 is an ordinary shot;
+* on the tableau route N1 noise acts on the tableau (X^a then Z^b after the
+  instruction); the reference's tableau path treats N1 as the identity
+  (sdim/program.py:31) and samples noise only in its Pauli-frame route.
+  ``noise=False`` reproduces the identity behaviour;
 * composite dimensions raise NotImplementedError (the reference switches to
   WeylTableau, sdim/program.py:196-199).
+
+Routes, as in sdim/program.py:244-265: ``shots > 1`` without
+``record_tableau`` or ``force_tableau`` runs the Pauli-frame sampler on the
+GPU (``sample_frames``: shot 0 is a noiseless tableau shot, the others
+propagate frames against it); every other call runs every shot on the
+tableau (``sample``).  The frame draws and N1 samples come from the Philox
+stream, keyed by shot index, instead of ``np.random``.
 """
 from __future__ import annotations
 
@@ -107,7 +112,9 @@ class Program:
         if dp is None:
             enc = encode_program(self.circuits, self.num_qudits, self.dimension, noise=noise)
             dp = DeviceProgram(self.context, enc)
-            self._cache = {key: dp}
+            # keep the other noise setting of the same circuits (the frame route uses both)
+            self._cache = {k: v for k, v in self._cache.items() if k[0] == key[0]}
+            self._cache[key] = dp
         return dp
 
     def _seed(self, seed):
@@ -143,6 +150,37 @@ class Program:
         self._last = (s, int(shot0) + int(shots) - 1, noise)
         return out
 
+    def _check_frame_noise_params(self):
+        """The frame route reads ``params['noise_channel']`` and
+        ``params['prob']`` of every N1 and raises KeyError without them
+        (sdim/program.py:486, 502)."""
+        for circ in self.circuits:
+            for ins in circ.operations:
+                if ins.gate_id == 17:
+                    params = ins.params if ins.params is not None else {}
+                    for key in ("noise_channel", "prob"):
+                        if key not in params:
+                            raise KeyError(key)
+
+    def sample_frames(self, shots: int, seed: Optional[int] = None, out: Optional[np.ndarray] = None,
+                      noise: bool = True) -> np.ndarray:
+        """Records of the reference's multi-shot route as a (shots, records)
+        uint8 array (value | deterministic << 7): row 0 is the noiseless
+        tableau shot 0, rows 1 .. shots-1 are Pauli-frame shots
+        (sdim/program.py:45-165, 244-265); ``noise=False`` leaves N1 out of
+        the frames too."""
+        ref = self.compile(False)
+        dp = self.compile(noise)
+        s = self._seed(seed)
+        if out is None:
+            out = np.empty((int(shots), dp.num_records), dtype=np.uint8)
+        if shots > 0:
+            rc = self.context.lib.sdim_frame_run(self.context.ptr, dp.ptr, ref.ptr, s, int(shots),
+                                                 out.ctypes.data if dp.num_records else None, 0)
+            _lib.check(rc, self.context.ptr, "simulate")
+        self._last = (s, 0, False)
+        return out
+
     def snapshot(self, seed: int, shot: int = 0, mode: int = _lib.SNAP_EVERY_INSTRUCTION, noise: bool = True,
                  per_shot: bool = False):
         """Tableau exports (int8, reference block order) and the shot's records.
@@ -171,21 +209,31 @@ class Program:
             options = SimulationOptions(shots, show_measurement, record_tableau, force_tableau, verbose,
                                         show_gate, exact)
         shots = int(options.shots)
-        dp = self.compile(noise)
-        enc = dp.enc
         s = self._seed(seed)
-        records = self.sample(shots, seed=s, noise=noise, plain=plain)
+        frame = shots > 1 and not options.record_tableau and not options.force_tableau and not plain
+        if frame:
+            # the reference's frame route (sdim/program.py:244-265); verbose and
+            # show_gate cover its tableau shot only, which has no noise
+            self._check_frame_noise_params()
+            dp = self.compile(noise)
+            records = self.sample_frames(shots, seed=s, noise=noise)
+            shown, shown_noise = 1, False
+        else:
+            dp = self.compile(noise)
+            records = self.sample(shots, seed=s, noise=noise, plain=plain)
+            shown, shown_noise = shots, noise
+        enc = dp.enc
         nested = records_to_nested(records, enc, self.num_qudits)
         if options.record_tableau or options.verbose:
             n, d = self.num_qudits, self.dimension
-            for shot in range(shots):
+            for shot in range(shown):
                 if options.record_tableau:
-                    snaps, _ = self.snapshot(s, shot, _lib.SNAP_AT_MEASUREMENT, noise)
+                    snaps, _ = self.snapshot(s, shot, _lib.SNAP_AT_MEASUREMENT, shown_noise)
                     for j in range(enc.num_records):
                         q, r = int(enc.meas_qudit[j]), int(enc.meas_round[j])
                         nested[q][r][shot].stabilizer_tableau = ExtendedTableau.from_export(snaps[j], n, d)
                 if options.verbose:
-                    snaps, _ = self.snapshot(s, shot, _lib.SNAP_EVERY_INSTRUCTION, noise)
+                    snaps, _ = self.snapshot(s, shot, _lib.SNAP_EVERY_INSTRUCTION, shown_noise)
                     print("Initial state")
                     ExtendedTableau(n, d).print_tableau()
                     print("\n")
@@ -194,11 +242,14 @@ class Program:
                         ExtendedTableau.from_export(snaps[t], n, d).print_tableau()
                         print("\n")
         elif options.show_gate:
-            for _ in range(shots):
+            for _ in range(shown):
                 for t in range(enc.num_instructions):
                     self._show_gate(t, enc)
         self.measurement_results = nested
-        self._last = (s, shots - 1, noise)
+        self._last = (s, 0, False) if frame else (s, shots - 1, noise)
+        if frame and not nested[0]:
+            # sdim/program.py:398-399: the route needs a measurement on qudit 0
+            raise ValueError("Empty or invalid measurement results format")
         if options.show_measurement:
             self.print_measurements()
         if shots == 1:

@@ -23,6 +23,11 @@ reference's own ``Program.simulate(force_tableau=True)`` with two injections:
 Outputs (beside this script): ``cases.json`` (programs, seeds, expected
 known answers) and ``arrays.npz`` (records, per-instruction tableaux of the
 first shot, final tableaux, record_tableau exports; int8/uint8).
+
+With ``--frames`` it drives the reference's multi-shot route instead
+(``run_reference_frames``: the Pauli-frame sampler of sdim/program.py:45-165,
+with ``np.random`` answered from the same Philox stream) and writes
+``frames.json`` / ``frames.npz``.
 """
 from __future__ import annotations
 
@@ -135,6 +140,143 @@ def run_reference(specs, seed, shot0, nshots, noise=True, snapshots=False, final
     rec = np.asarray(records, dtype=np.uint8).reshape(nshots, -1)
     return {"records": rec, "snapshots": snaps, "final": np.stack(finals) if finals else None,
             "record_tableau": np.stack(rts) if rts else None, "nested": nested}
+
+
+def run_reference_frames(specs, seed, nshots):
+    """Runs the reference's multi-shot route, ``Program.simulate(nshots)``
+    (sdim/program.py:244-265), with its draws taken from the Philox stream:
+
+    * shot 0's outcomes: ``tableau_prime.random`` as in ``run_reference``
+      (shot 0, measurement ordinal); N1 stays the identity there, as the
+      reference's tableau shot has it;
+    * ``np.random`` of sdim/program.py (``_build_ir`` and ``simulate_frame``)
+      is replaced by an object that answers, in call order,
+      ``randint(1, hi, S)`` of N1 ordinal j with ``1 + residue(word 0 of the
+      domain-2 block j, hi - 1)``, ``uniform(0, 1, S)`` of N1 ordinal j with
+      1.0 where the domain-1 coin fires and 0.0 elsewhere (so the
+      reference's ``roll < 1 - prob`` test keeps exactly the fired shots),
+      ``randint(0, d, (n, S))`` with the frame events 0 .. n-1 and the k-th
+      ``randint(0, d, S)`` with frame event n + k (oracle/frame.py);
+      frame shot s (1 .. S) uses stream shot index s.
+    Returns (nshots, records) uint8: value | deterministic << 7, program order.
+    """
+    import sdim.program as sp
+    import sdim.tableau.tableau_prime as tp
+    from sdim.circuit import Circuit
+    from sdim.program import Program
+    from oracle import frame as oframe
+
+    n, d = specs[0].num_qudits, specs[0].dimension
+    circuits = [s.build(Circuit) for s in specs]
+    prog = Program(circuits[0])
+    for c in circuits[1:]:
+        prog.append_circuit(c)
+    instrs = [ins for c in circuits for ins in c.operations]
+    thresholds = [philox.noise_threshold(float(ins.params["prob"])) for ins in instrs if ins.gate_id == 17]
+    S = nshots - 1
+    shots = np.arange(1, nshots, dtype=np.uint64)
+
+    class Outcomes:
+        mord = 0
+
+        def choice(self, seq):
+            m = int(philox.measurement_outcome(seed, 0, self.mord, len(seq)))
+            return seq[m]
+
+    class Draws:
+        choice_j = coin_j = frame_k = 0
+
+        def randint(self, low, high=None, size=None):
+            if low == 1:
+                j = self.choice_j
+                self.choice_j += 1
+                w1 = philox.stream_words(seed, shots, j, philox.DOMAIN_CHOICE)[0]
+                return (1 + philox.residue(w1, int(high) - 1)).astype(np.int64)
+            assert low == 0 and high == d
+            if isinstance(size, tuple):
+                return np.stack([oframe.frame_residues(seed, shots, q, d) for q in range(size[0])])
+            k = self.frame_k
+            self.frame_k += 1
+            return oframe.frame_residues(seed, shots, n + k, d)
+
+        def uniform(self, low, high, size=None):
+            j = self.coin_j
+            self.coin_j += 1
+            thr = thresholds[j]
+            coin = philox.stream_words(seed, shots, j >> 2, philox.DOMAIN_COIN)[j & 3].astype(np.uint64)
+            fire = coin >= np.uint64(thr) if thr < (1 << 32) else np.zeros(S, dtype=bool)
+            return np.where(fire, 1.0, 0.0)
+
+    class NumpyWithDraws:
+        def __init__(self, real, draws):
+            self._real = real
+            self.random = draws
+
+        def __getattr__(self, name):
+            return getattr(self._real, name)
+
+    outcomes = Outcomes()
+    tp.random = outcomes
+    orig = prog.apply_gate
+    st = {"mord": 0}
+
+    def wrapped(ins):
+        if ins.gate_id in MEAS:
+            outcomes.mord = st["mord"]
+            st["mord"] += 1
+        return orig(ins)
+
+    prog.apply_gate = wrapped
+    real_np = sp.np
+    sp.np = NumpyWithDraws(real_np, Draws())
+    try:
+        nested = prog.simulate(shots=nshots)
+    finally:
+        sp.np = real_np
+    counts = [0] * n
+    cols = []
+    for ins in instrs:
+        if ins.gate_id in MEAS:
+            q = ins.qudit_index
+            group = nested[q][counts[q]]
+            counts[q] += 1
+            cols.append([int(r.measurement_value) | (0x80 if r.deterministic else 0) for r in group])
+    return np.asarray(cols, dtype=np.uint8).T.reshape(nshots, len(cols))
+
+
+def frame_cases():
+    out = []
+    for s, _ in kat_cases()[:3]:
+        out.append((s, 6))
+    k = 0
+    for d in (2, 3, 5, 7):
+        for n in (2, 3, 5):
+            out.append((W.all_gates_random(n, d, 60 if n == 2 else 120, seed=3000 + k,
+                                           name=f"frame_rand_d{d}_n{n}"), 24))
+            k += 1
+    for d in (2, 5):
+        ops = [("H", 0, None, {}), ("CZ", 1, 1, {}), ("CZ_INV", 0, 0, {}), ("SWAP", 1, 1, {}),
+               ("CNOT", 0, 0, {}), ("N1", 0, None, {"prob": 0.5, "noise_channel": "d"}), ("P", 1, None, {}),
+               ("M_X", 1, None, {}), ("M", 0, None, {}), ("RESET", 1, None, {}), ("M", 1, None, {})]
+        out.append((W.CircuitSpec(2, d, ops, f"frame_aliased_d{d}"), 24))
+    out.append((W.surface_memory(3, 3, prob=0.02), 64))
+    out[-1][0].name = "frame_surface_L3_r3"
+    out.append((W.random_hpc(12, 5, 120, seed=5, weights=(0.25, 0.25, 0.5), mr_every=12, mr_fraction=0.25,
+                             name="frame_oddd_d5"), 32))
+    return out
+
+
+def main_frames():
+    cases, arrays = [], {}
+    for s, nshots in frame_cases():
+        seed = 17
+        rec = run_reference_frames([s], seed, nshots)
+        arrays[f"{s.name}__records"] = rec
+        cases.append({"name": s.name, "seed": seed, "nshots": nshots, "circuits": [s.to_json()]})
+        print(s.name, rec.shape, flush=True)
+    (HERE / "frames.json").write_text(json.dumps({"cases": cases}, indent=0))
+    np.savez_compressed(HERE / "frames.npz", **arrays)
+    print("wrote", len(cases), "frame-route cases")
 
 
 def _worker(args):
@@ -292,4 +434,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--frames" in sys.argv:
+        main_frames()
+    else:
+        main()
