@@ -17,14 +17,17 @@ Workloads (--workload):
                      {2,3,5,7}, 4n gates {H,P,CNOT} + MEASURE all, shots uniform in
                      [1,64]; one persistent launch per engine variant.
 
-Arms: the default is the GB300 engine (shot-group persistent kernels):
-`value` from CUDA events on the launching stream with records in device
-memory, `e2e` through the C ABI with pinned host records and the copies
-inside the timed region; the per-shot engine and the plain form (one
+Arms: the default is the GB300 engine (the library's choice: the trace
+engines from 128 shots, shot-group persistent kernels below): `value` from
+CUDA events on the launching stream with records in device memory, `e2e`
+through the C ABI with pinned host records and the copies inside the timed
+region; the other engines, the per-shot engine and the plain form (one
 single-warp launch per shot) on the same inputs, and the CPU oracle on a
-bounded sample, are reported beside it.  `--impl reference` times the CPU
-restatement of the reference's algorithm (the C oracle over every host core)
-on a bounded sample per step.
+bounded sample, are reported beside it.  `frame_sampler` times the
+reference's other multi-shot route (Pauli frames against a noiseless tableau
+shot, `sdim_frame_run`) on the same workload, with its NumPy port on a CPU
+sample.  `--impl reference` times the CPU restatement of the reference's
+algorithm (the C oracle over every host core) on a bounded sample per step.
 
 Multi-GPU: replicas -- rank r runs the same programs on its own shot range
 (shot0 = r * shots), no collective on the data path (weak scaling).
@@ -390,6 +393,62 @@ class Timer:
         return float(t.item())
 
 
+def frame_route(args, torch, ctx, prog, dp, spec, shots, timer):
+    """The reference's multi-shot route (Program.simulate(shots) without
+    force_tableau): noiseless tableau shot 0, Pauli frames for the rest, on
+    the same workload.  Device time by the library's CUDA events, e2e with
+    host records, and the NumPy port of the route timed on a CPU sample."""
+    from sdim_gb300 import _lib
+    ref = prog.compile(False)
+    nrec = dp.num_records
+    fout = torch.empty((shots, max(nrec, 1)), dtype=torch.uint8, device="cuda")
+
+    def fstep():
+        rc = ctx.lib.sdim_frame_run(ctx.ptr, dp.ptr, ref.ptr, 0, shots, fout.data_ptr(),
+                                    _lib.FLAG_OUT_DEVICE | _lib.FLAG_TIME)
+        _lib.check(rc, ctx.ptr, "frame run")
+
+    for _ in range(args.warmup):
+        fstep()
+    _, fk, _ = timer.run(args.steps, fstep)
+    kms = statistics.mean(fk)
+    dev = fout[:, :nrec].cpu().numpy()
+    host = torch.empty((shots, max(nrec, 1)), dtype=torch.uint8, pin_memory=True)
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        rc = ctx.lib.sdim_frame_run(ctx.ptr, dp.ptr, ref.ptr, 0, shots, host.data_ptr(), 0)
+        _lib.check(rc, ctx.ptr, "frame run")
+        if k >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    if not np.array_equal(host[:, :nrec].numpy(), dev):
+        raise AssertionError("frame route: end-to-end records differ from the device-timed run")
+    units = len(spec.ops) * shots
+    out = {"value": units / (kms / 1e3), "unit": UNIT, "kernel_ms": kms,
+           "form": "noiseless tableau shot 0, then one lane per shot carrying x / z frames (k_frame_pass)",
+           "e2e": {"value": units * args.steps / (sum(e2e_ms) / 1e3), "unit": UNIT,
+                   "ms_per_step": statistics.mean(e2e_ms), "d2h_bytes_per_step": int(shots * nrec)},
+           "gpu_launches_per_step": 2}
+    if not args.no_cpu:
+        import oracle
+        from oracle import frame
+        oprog = oracle.OracleProgram([spec], spec.num_qudits, spec.dimension)
+        sample = 257
+        while True:
+            t0 = time.perf_counter()
+            cpu = frame.simulate(oprog, 0, min(sample, shots), threads=1)
+            dt = time.perf_counter() - t0
+            if dt > args.cpu_seconds / 4 or sample >= shots:
+                break
+            sample = min(shots, sample * 4)
+        if not np.array_equal(cpu, dev[:cpu.shape[0]]):
+            raise AssertionError("frame route: GPU records differ from the NumPy port")
+        out["cpu_baseline"] = {"value": len(spec.ops) * cpu.shape[0] / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"{cpu.shape[0]} shots in {dt:.1f} s (NumPy port of the reference's "
+                                         "frame route, vectorised over shots, one thread)"}
+    return out
+
+
 def run_single(args, torch, dist, ws, rank, local):
     from sdim_gb300 import Program, _lib
 
@@ -461,6 +520,7 @@ def run_single(args, torch, dist, ws, rank, local):
                              "stages_ms": [statistics.mean(v) for v in zip(*timer.stage_ms)]}
         step()
         ctx.sync()
+    frames = frame_route(args, torch, ctx, prog, dp, spec, shots, timer) if rank == 0 else None
     det_row = (rec[0] >> 7).astype(bool) if nrec else np.zeros(0, bool)
     assert np.all((rec >> 7) == (rec[0] >> 7)), "deterministic flags differ across shots"
     meas_ids = [g for g in enc.ops[:, 0].tolist() if g in (14, 15, 16)]
@@ -575,6 +635,7 @@ def run_single(args, torch, dist, ws, rank, local):
         "engine": args.engine,
         "stages_ms": {"xz_pass": stages[0], "phase_pass": stages[1], "other_engines": stages[2]},
         "engines": engines,
+        "frame_sampler": frames,
     }
 
 

@@ -1185,9 +1185,11 @@ int sdim_frame_run(sdim_ctx* ctx, const sdim_circuit* c, const sdim_circuit* ref
                        ctx->stream));
   }
   cudaStream_t s = ctx->stream;
-  // shot 0: the noiseless tableau shot, into row 0
+  // shot 0: the noiseless tableau shot, into row 0, on the trace engines
+  // (one x / z pass) where they take the program: the shot-group engine
+  // spends a whole group's latency on a single shot
   std::vector<Job> jobs{Job{ref, seed, 0, 1, dst}};
-  if ((rc = launch_jobs(ctx, jobs, s, flags & ~SDIM_FLAG_ASYNC)) != SDIM_OK) return rc;
+  if ((rc = launch_jobs(ctx, jobs, s, (flags & ~SDIM_FLAG_ASYNC) | SDIM_FLAG_TRACE)) != SDIM_OK) return rc;
   // shots 1 .. nshots - 1: frames against row 0
   if (nshots > 1 && c->nmeas > 0) {
     FrameDesc fd;
