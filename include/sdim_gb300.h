@@ -115,6 +115,16 @@ int sdim_run_device(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int6
  * when 64 n bytes of frames do not fit in a block's shared memory. */
 int sdim_frame_run(sdim_ctx* ctx, const sdim_circuit* circ, const sdim_circuit* ref, uint64_t seed,
                    int64_t nshots, uint8_t* out, unsigned flags);
+/* Parses .chp text (the reference's read_circuit, sdim/circuit_io.py:6-83)
+ * straight into op-table rows for sdim_encode_circuit / sdim_run_tables:
+ * rows gets 4 int32 per instruction (gate id, qudit, target or -1, N1
+ * channel), probs (may be NULL) the N1 probability (0 elsewhere).  Needs no
+ * context.  With rows NULL it only counts: *nrows, *n (largest qudit index
+ * + 1) and *d are set either way.  SDIM_EINVAL (message in err) for a text
+ * the reference's reader rejects (no '#' line, malformed parameter, unknown
+ * gate, not one or two indices, bad dimension) or when cap < *nrows. */
+int sdim_parse_chp(const char* text, int64_t len, int32_t* rows, double* probs, int64_t cap, int64_t* nrows,
+                   int32_t* n, int32_t* d, char* err, size_t errlen);
 /* Many programs (uneven n, d, depth, shots) in persistent launches fed by a
  * device work queue.  outs[i] holds nshots[i] x records(circs[i]) bytes.
  * The reference has no batch API; it is Program.simulate called once per program. */

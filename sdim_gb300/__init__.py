@@ -6,9 +6,10 @@ All shots run in CUDA kernels (sm_103a) behind the C ABI in
 ``include/sdim_gb300.h``.
 """
 from .circuit import Circuit, CircuitInstruction
+from .circuit_io import read_chp_table, read_circuit, write_circuit
 from .gatedata import Gate, GateData
 from .program import Program, SimulationOptions
 from .tableau import ExtendedTableau, MeasurementResult, Tableau
 
 __all__ = ["Circuit", "CircuitInstruction", "Gate", "GateData", "Program", "SimulationOptions",
-           "MeasurementResult", "Tableau", "ExtendedTableau"]
+           "MeasurementResult", "Tableau", "ExtendedTableau", "read_circuit", "write_circuit", "read_chp_table"]

@@ -60,6 +60,8 @@ SIGNATURES = {
     "sdim_run": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, C.c_uint]),
     "sdim_run_device": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, _P, C.c_uint]),
     "sdim_frame_run": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_int64, _P, C.c_uint]),
+    "sdim_parse_chp": (C.c_int, [C.c_char_p, C.c_int64, _P, _P, C.c_int64, C.POINTER(C.c_int64),
+                               C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]),
     "sdim_run_batch": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.c_uint]),
     "sdim_sync": (C.c_int, [_P]),
     "sdim_query": (C.c_int, [_P]),

@@ -134,6 +134,13 @@ class Server:
             self._wake.notify()
         return req
 
+    def submit_chp(self, text, shots: int, seed: int, shot0: int = 0) -> Request:
+        """A request given as .chp text, parsed natively into its op table
+        (``circuit_io.read_chp_table``) with no Circuit objects."""
+        from .circuit_io import read_chp_table
+        table, probs, n, d = read_chp_table(text)
+        return self.submit(table, n, d, shots, seed, probs=probs, shot0=shot0)
+
     def close(self):
         with self._wake:
             self._stop = True

@@ -27,7 +27,9 @@ first shot, final tableaux, record_tableau exports; int8/uint8).
 With ``--frames`` it drives the reference's multi-shot route instead
 (``run_reference_frames``: the Pauli-frame sampler of sdim/program.py:45-165,
 with ``np.random`` answered from the same Philox stream) and writes
-``frames.json`` / ``frames.npz``.
+``frames.json`` / ``frames.npz``; with ``--chp`` it runs the reference's
+.chp reader and writer (sdim/circuit_io.py:6-139) on corner-case texts and
+on circuits it writes itself, and writes ``chp.json``.
 """
 from __future__ import annotations
 
@@ -279,6 +281,63 @@ def main_frames():
     print("wrote", len(cases), "frame-route cases")
 
 
+CHP_TEXTS = {
+    # hand-written texts for the reader's corner cases
+    "chp_comment_and_upper_d": "two lines\nof comment\n#\nD 5\nh 0\ncx 0 3\n\nmr 2\nN1 1 prob=0.25 noise_channel=p\n"
+                               "M 3\n",
+    "chp_default_dimension": "#\nH 0\nCNOT 0 1\nMEASURE 1\nnoise1 0 channel=f prob=1e-3\nM 0\n",
+    "chp_crlf_and_tabs": "c\r\n#\r\nd 3\r\n\tS 1\r\nSUM  1\t2\r\nM_X 2\r\nMZ 1\r\n",
+    "chp_two_qudit_params_dropped": "#\nd 7\nN1 0 1 prob=0.5 noise_channel=p\nCZ 1 0 x=1\nM 1\n",
+    "chp_junk_tokens": "#\nd 2\nH 0 junk\nCX 0 1 -3 more\nM 1 tail=end\n",
+}
+CHP_ERRORS = {
+    "chp_err_no_hash": "H 0\nM 0\n",
+    "chp_err_param": "#\nN1 0 prob=0.1=0.2\n",
+    "chp_err_three_indices": "#\nCNOT 0 1 2\n",
+    "chp_err_unknown_gate": "#\nFOO 0\n",
+    "chp_err_no_index": "#\nH\nM 0\n",
+}
+
+
+def main_chp():
+    """Fixtures of the reference's .chp reader and writer (sdim/circuit_io.py:6-139)."""
+    import tempfile
+    from sdim.circuit import Circuit
+    from sdim.circuit_io import read_circuit, write_circuit
+
+    def parsed(circ):
+        return {"n": circ.num_qudits, "d": circ.dimension,
+                "ops": [[ins.gate_name, int(ins.gate_id), int(ins.qudit_index),
+                         -1 if ins.target_index is None else int(ins.target_index),
+                         None if ins.params is None else {k: str(v) for k, v in ins.params.items()}]
+                        for ins in circ.operations]}
+
+    cases = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, text in CHP_TEXTS.items():
+            path = os.path.join(tmp, name + ".chp")
+            Path(path).write_text(text)
+            cases.append({"name": name, "text": text, "parsed": parsed(read_circuit(path))})
+        for name, text in CHP_ERRORS.items():
+            path = os.path.join(tmp, name + ".chp")
+            Path(path).write_text(text)
+            try:
+                read_circuit(path)
+                raise AssertionError(name + " parsed")
+            except Exception as e:  # the type the reference raises
+                cases.append({"name": name, "text": text, "error": type(e).__name__})
+        for k, (n, d, nops) in enumerate([(3, 2, 40), (6, 3, 90), (4, 5, 70), (9, 7, 150)]):
+            spec = W.all_gates_random(n, d, nops, seed=7000 + k, name=f"chp_written_d{d}")
+            circ = spec.build(Circuit)
+            comment = "" if k % 2 else f"written by the reference, case {k}"
+            path = write_circuit(circ, output_file=spec.name + ".chp", comment=comment, directory=tmp)
+            text = Path(path).read_text()
+            cases.append({"name": spec.name, "written_from": spec.to_json(), "comment": comment, "text": text,
+                          "parsed": parsed(read_circuit(path))})
+    (HERE / "chp.json").write_text(json.dumps({"cases": cases}, indent=0))
+    print("wrote", len(cases), ".chp cases")
+
+
 def _worker(args):
     specs_json, seed, shot0, nshots, noise = args
     _setup_paths()
@@ -436,5 +495,7 @@ def main():
 if __name__ == "__main__":
     if "--frames" in sys.argv:
         main_frames()
+    elif "--chp" in sys.argv:
+        main_chp()
     else:
         main()

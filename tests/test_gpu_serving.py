@@ -77,3 +77,22 @@ def test_tight_memory_budget_still_serves_everything():
         server.close()
     for (t, n, d, s, seed), res in zip(reqs, results):
         assert np.array_equal(res, _alone(t, n, d, s, seed))
+
+
+def test_chp_requests_match_the_circuit_route():
+    """Requests given as .chp text (native parser) give the records of the
+    same circuit read by read_circuit and sampled through Program."""
+    from sdim_gb300 import Program, circuit_io
+    texts = []
+    for k, (n, d) in enumerate([(5, 2), (9, 3), (17, 5), (4, 7)]):
+        spec = workloads.all_gates_random(n, d, 30 * n, seed=50 + k, name="chp")
+        texts.append(circuit_io.chp_text(spec.build()))
+    server = Server(lanes=2, max_batch_requests=4)
+    try:
+        reqs = [server.submit_chp(t, shots=40 + 7 * k, seed=300 + k) for k, t in enumerate(texts)]
+        got = [r.wait(120) for r in reqs]
+    finally:
+        server.close()
+    for k, (t, rec) in enumerate(zip(texts, got)):
+        want = Program(circuit_io.circuit_from_chp(t)).sample(40 + 7 * k, seed=300 + k)
+        assert np.array_equal(rec, want), k
