@@ -76,6 +76,8 @@ def parse():
                     help="single-program workloads: time the selected engine only (for profiling runs)")
     ap.add_argument("--engine", default="auto", choices=["auto", "trace", "group", "per_shot"],
                     help="batched engine of the timed run (auto: the library's choice)")
+    ap.add_argument("--route", default="tableau", choices=["tableau", "frame"],
+                    help="with --quick: time the tableau route or the frame route (sdim_frame_run)")
     return ap.parse_args()
 
 
@@ -474,6 +476,26 @@ def run_single(args, torch, dist, ws, rank, local):
                                      _lib.FLAG_ASYNC | _lib.FLAG_TIME | (engine_flags if extra is None else extra))
         _lib.check(rc, ctx.ptr, "run")
 
+    if args.quick and args.route == "frame":
+        # the frame route alone (profiling runs): shot 0 on the tableau, frames for the rest
+        ref = prog.compile(False)
+
+        def fstep():
+            rc = ctx.lib.sdim_frame_run(ctx.ptr, dp.ptr, ref.ptr, 0, shots, out.data_ptr(),
+                                        _lib.FLAG_OUT_DEVICE | _lib.FLAG_TIME)
+            _lib.check(rc, ctx.ptr, "frame run")
+
+        for _ in range(args.warmup):
+            fstep()
+        _, fk, clk = timer.run(args.steps, fstep, Clocks(local))
+        kms = timer.max_over_ranks(statistics.mean(fk))
+        return None if rank else {
+            "metric": METRIC, "value": len(spec.ops) * shots * ws / (kms / 1e3), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": kms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8 residues",
+            "data": "synthetic (seeded circuit generator, Philox frame and noise stream)",
+            "config": {"workload": desc, "shots_per_gpu": shots, "mode": "quick: frame route only"},
+            "route": "frame", "kernel_ms": kms, "gpu_launches": 2 * args.steps, "clocks": clk}
     for _ in range(args.warmup):
         step()
     ctx.sync()

@@ -34,6 +34,8 @@ struct sdim_ctx {
   cudaStream_t last_stream = nullptr;  // stream of the last launch (sdim_sync / sdim_query)
   int num_sms = 0;
   int smem_optin = 0;
+  int smem_per_sm = 0;    // shared memory of one SM
+  int smem_reserved = 0;  // shared memory the system keeps per block
   int64_t l2_bytes = 0;
   int64_t gmem_bytes = 0;
   size_t gmem_slot_budget = (size_t)8 << 30;
@@ -470,8 +472,17 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       grid = std::min(grid, 2 * ctx->num_sms);
       if ((rc = ensure(ctx, ctx->gslots, xz * (size_t)grid)) != SDIM_OK) return rc;
     }
-    launch_trace_pass(ctx->trace_threads, grid, hot + (in_smem ? xz : 0) + win, s, dd, (int)k,
-                      static_cast<uint8_t*>(ctx->gslots.p), xz, hot, in_smem ? 1 : 0, status);
+    size_t smem = hot + (in_smem ? xz : 0) + win;
+    if (coins && grid <= ctx->num_sms / 8) {
+      // shared-memory fence: a few x / z CTAs claim enough shared memory that
+      // no coin-pass block fits beside them, so the coin warps do not take
+      // the issue slots of the latency-bound x / z pass on its SM
+      const long long fence = (long long)ctx->smem_per_sm - 2LL * ctx->smem_reserved - (long long)kCoinFenceSmem + 16;
+      const long long cap = (long long)ctx->smem_optin - 4096;  // room for the kernel's static arrays
+      smem = std::max<size_t>(smem, (size_t)std::max(0LL, std::min(fence, cap)));
+    }
+    launch_trace_pass(ctx->trace_threads, grid, smem, s, dd, (int)k, static_cast<uint8_t*>(ctx->gslots.p), xz, hot,
+                      in_smem ? 1 : 0, status);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
   }
@@ -519,7 +530,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     const int block = 256;
     const long long grid = (coins + block - 1) / block;
     if (grid > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one coin pass");
-    launch_coin_pass((int)grid, block, ctx->aux, dd, (int)k, coins);
+    launch_coin_pass((int)grid, block, kCoinFenceSmem, ctx->aux, dd, (int)k, coins);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "coin pass launch");
     CK(cudaEventRecord(ctx->ev_join, ctx->aux));
@@ -966,6 +977,8 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
   }
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
+  ctx->smem_per_sm = (int)prop.sharedMemPerMultiprocessor;
+  ctx->smem_reserved = (int)prop.reservedSharedMemPerBlock;
   ctx->l2_bytes = prop.l2CacheSize;
   ctx->gmem_bytes = (int64_t)prop.totalGlobalMem;
   ctx->gmem_slot_budget = std::min<size_t>((size_t)8 << 30, (size_t)(prop.totalGlobalMem / 8));

@@ -80,8 +80,9 @@ void launch_philox_probe(int grid, cudaStream_t s, const unsigned long long* see
   k_philox_probe<<<grid, 256, 0, s>>>(seeds, iters, sink);
 }
 
-void launch_coin_pass(int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc, long long total) {
-  k_coin_pass<<<grid, block, 0, s>>>(descs, ndesc, total);
+void launch_coin_pass(int grid, int block, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc,
+                      long long total) {
+  k_coin_pass<<<grid, block, smem, s>>>(descs, ndesc, total);
 }
 
 size_t trace_pass_hot_bytes(int n) { return round16(TraceTab::hot_bytes(n)); }

@@ -145,7 +145,13 @@ void launch_philox_probe(int grid, cudaStream_t s, const unsigned long long* see
 
 // Coin pass: the fire masks of every program of descs with masks (items:
 // (chunk group, shot) pairs numbered through coin_begin).
-void launch_coin_pass(int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc, long long total);
+void launch_coin_pass(int grid, int block, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc,
+                      long long total);
+
+// Dynamic shared memory every coin-pass block requests (and leaves unused):
+// with a few x / z CTAs running alongside, those claim the rest of their SM's
+// shared memory so that no coin block lands beside them.
+constexpr size_t kCoinFenceSmem = 8192;
 
 // Phase pass: one lane per shot, one warp per 32-shot group; every program of
 // descs has trace rows of tw words.  Returns false for an unsupported tw.
