@@ -29,9 +29,10 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
 // numbered through descs[].c.item_begin).  With the group index taken from
 // blockIdx alone, every per-program value and the whole measurement loop
 // control are provably warp-uniform, so they stay out of the per-lane
-// registers.
+// registers.  Up to 16-word rows, 32 blocks per SM at 64 registers; wider
+// rows hold more delta words per lane and get 128.
 template <int TW>
-__global__ void __launch_bounds__(32, 32) k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc,
+__global__ void __launch_bounds__(32, TW >= 16 ? 16 : 32) k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc,
                                                    long long total_groups, const int* status) {
   __shared__ uint8_t rec[32 * kRecStride];
   if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
@@ -45,8 +46,11 @@ __global__ void __launch_bounds__(32, 32) k_phase_pass(const TraceDesc* __restri
 }
 
 // One thread per (chunk group, shot) item of the coin pass; descs with
-// masks only, numbered through coin_begin.
-__global__ void __launch_bounds__(256) k_coin_pass(const TraceDesc* __restrict__ descs, int ndesc, long long total) {
+// masks only, numbered through coin_begin.  Three blocks per SM leave 80
+// registers a thread: the eight interleaved Philox chains and their round
+// keys fit without spills.
+__global__ void __launch_bounds__(256, 3) k_coin_pass(const TraceDesc* __restrict__ descs, int ndesc,
+                                                      long long total) {
   const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (it >= total) return;
   const int i = find_coin_desc(descs, ndesc, it);
