@@ -308,7 +308,10 @@ def run_reference_arm(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
-TRACE_MIN_SHOTS = 128  # the library's default switch to the trace engine
+# the library's default switch to the trace engines: from this many shots,
+# and for odd d up to this many qudits
+TRACE_MIN_SHOTS = 128
+TRACE_U8_MAX_QUDITS = 2048
 
 
 def trace_words(n):
@@ -470,6 +473,8 @@ def run_single(args, torch, dist, ws, rank, local):
     engine_flags = _lib.engine_flags(None if args.engine == "auto" else args.engine)
     trace_used = (d == 2 and trace_words(n) > 0 and
                   (args.engine == "trace" or (args.engine == "auto" and shots >= TRACE_MIN_SHOTS)))
+    odd_trace_used = (d != 2 and n <= TRACE_U8_MAX_QUDITS and
+                      (args.engine == "trace" or (args.engine == "auto" and shots >= TRACE_MIN_SHOTS)))
 
     def step(extra=None):
         rc = ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 0, shot0, shots, out.data_ptr(), stream.cuda_stream,
@@ -629,6 +634,24 @@ def run_single(args, torch, dist, ws, rank, local):
     else:
         roofline = dict(group_model)
         roofline["traffic"] = None
+        if odd_trace_used:
+            # the x / z pass updates one tableau per program on a CTA pair (or
+            # one CTA): its algorithmic shared-memory bytes against the share
+            # of the measured shared-memory bandwidth of the SMs it runs on
+            xz_ms = stages[0]
+            sms = 2
+            share = peak * sms / ctx.num_sms
+            xz_ach = per_shot_bytes / (xz_ms / 1e3) / 1e9
+            roofline = {"bound": "smem (x/z pass, latency-bound on a CTA pair)", "achieved": xz_ach,
+                        "peak": share, "unit": "GB/s", "frac": xz_ach / share,
+                        "traffic": read_traffic(f"trace_engine_{args.workload}.md"),
+                        "kernel": f"k_trace_pass_split<{d}> (x/z pass), then k_phase_pass_u8<{d}>",
+                        "peak_source": f"sdim_probe_smem_bandwidth x {sms}/{ctx.num_sms} SMs",
+                        "algorithmic_bytes_per_launch": per_shot_bytes,
+                        "bytes_model": "per-instruction bytes of one tableau update (x/z pass: one tableau per program)",
+                        "kernel_ms": xz_ms,
+                        "stages_ms": {"xz_pass": stages[0], "phase_pass": stages[1]},
+                        "group_engine_model": group_model}
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
