@@ -285,15 +285,21 @@ int job_variant(const sdim_circuit* c, unsigned flags) {
 // single persistent launch keeps every SM busy.
 constexpr int64_t kTraceMinShots = 128;
 
+// From this many qudits the trace engines take a program at any shot count:
+// its x / z pass dominates, and the shot-group engine repeats it for every
+// 32 shots where the trace engine runs it once.
+constexpr int kTraceMinQudits = 160;
+
 // Jobs for the trace engine: d = 2, batched form, trace rows of at most
-// kTraceMaxWords words (n <= 512) and kTraceMinShots shots, unless
-// SDIM_FLAG_TRACE (any shot count) or a flag that names another engine.
+// kTraceMaxWords words (n <= 512) and kTraceMinShots shots or
+// kTraceMinQudits qudits, unless SDIM_FLAG_TRACE (any shot count) or a flag
+// that names another engine.
 bool use_trace(const Job& j, unsigned flags) {
   if (flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT | SDIM_FLAG_TEAM_WARP | SDIM_FLAG_TEAM_CTA |
                SDIM_FLAG_NO_TRACE))
     return false;
   if (j.c->d != 2 || trace_words(j.c->n) == 0 || !j.c->d_steps || j.nshots <= 0) return false;
-  return (flags & SDIM_FLAG_TRACE) || j.nshots >= kTraceMinShots;
+  return (flags & SDIM_FLAG_TRACE) || j.nshots >= kTraceMinShots || j.c->n >= kTraceMinQudits;
 }
 
 // Odd-d programs above this many qudits stay on the shot-group engine (the
@@ -306,14 +312,14 @@ bool use_trace_u8(const Job& j, unsigned flags) {
                SDIM_FLAG_NO_TRACE))
     return false;
   if (j.c->d == 2 || j.c->n > kTraceU8MaxQudits || j.nshots <= 0) return false;
-  return (flags & SDIM_FLAG_TRACE) || j.nshots >= kTraceMinShots;
+  return (flags & SDIM_FLAG_TRACE) || j.nshots >= kTraceMinShots || j.c->n >= kTraceMinQudits;
 }
 
 // Trace-engine launches: the x / z pass of every program (d = 2 jobs, then
 // odd-d jobs per variant of d), the coin pass of the d = 2 jobs alongside on
 // the second stream, then the phase passes (d = 2 per trace-row width, odd
-// d per variant).  d = 2 programs are ordered by n, which orders the row
-// widths; odd-d programs by (variant, n).
+// d per variant).  d = 2 programs are ordered by n, largest first, which
+// orders the row widths; odd-d programs by (variant, n), largest first.
 int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujobs, cudaStream_t s, unsigned flags,
                       int* status) {
   const bool timed = flags & SDIM_FLAG_TIME;
@@ -334,7 +340,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     ctx->trace_smem_set = true;
   }
   // ---- d = 2 descriptors
-  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& b) { return a.c->n < b.c->n; });
+  // largest first: the x / z passes of a batch start with the longest ones
+  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& b) { return a.c->n > b.c->n; });
   const size_t k = jobs.size();
   std::vector<TraceDesc> hd(k);
   long long coins = 0;
@@ -412,7 +419,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   // ---- odd-d descriptors
   std::stable_sort(ujobs.begin(), ujobs.end(), [](const Job& a, const Job& b) {
     const int va = trace_u8_variant(a.c->d), vb = trace_u8_variant(b.c->d);
-    return va != vb ? va < vb : a.c->n < b.c->n;
+    return va != vb ? va < vb : a.c->n > b.c->n;
   });
   const size_t ku = ujobs.size();
   std::vector<TraceDescU8> hu(ku);
@@ -462,7 +469,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   if (coins) CK(cudaEventRecord(ctx->ev_fork, s));
   // ---- x / z passes: one CTA per program
   if (k) {
-    const int nmax = jobs[k - 1].c->n;
+    const int nmax = jobs[0].c->n;
     const size_t hot = trace_pass_hot_bytes(nmax), xz = trace_pass_xz_bytes(nmax);
     // after the tableau: the schedule window; about 3.2 KB of static shared memory besides
     const size_t win = trace_pass_window_bytes();
@@ -503,7 +510,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     const int mode = xz_mode(hu[b].c.n);
     size_t e = b;
     while (e < ku && trace_u8_variant(hu[e].c.d) == v && xz_mode(hu[e].c.n) == mode) ++e;
-    const int nmax = hu[e - 1].c.n;
+    const int nmax = hu[b].c.n;
     if (mode == 1) {
       launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax) + win,
                             trace_u8_split_smem(nmax), s, du + b, (int)(e - b), status);
@@ -563,7 +570,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       items = hu[e].c.item_begin + (hu[e].c.nshots + 31) / 32;
       ++e;
     }
-    const int nmax = hu[e - 1].c.n;
+    const int nmax = hu[b].c.n;
     // (shot, chunk) threads: about 64 generators per thread, 32 to 512 threads
     const int nch = std::max(1, std::min(16, (2 * nmax + 63) / 64));
     if (items > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one phase pass");
