@@ -18,7 +18,7 @@ Workloads (--workload):
                      [1,64]; one persistent launch per engine variant.
 
 Arms: the default is the GB300 engine (the library's choice: the trace
-engines from 128 shots, shot-group persistent kernels below): `value` from
+engines from 128 shots or 160 qudits, shot-group persistent kernels below): `value` from
 CUDA events on the launching stream with records in device memory, `e2e`
 through the C ABI with pinned host records and the copies inside the timed
 region; the other engines, the per-shot engine and the plain form (one
@@ -308,9 +308,10 @@ def run_reference_arm(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
-# the library's default switch to the trace engines: from this many shots,
-# and for odd d up to this many qudits
+# the library's default switch to the trace engines: from this many shots or
+# this many qudits, and for odd d up to this many qudits
 TRACE_MIN_SHOTS = 128
+TRACE_MIN_QUDITS = 160
 TRACE_U8_MAX_QUDITS = 2048
 
 
@@ -329,6 +330,21 @@ def philox_peak(ctx):
     v = ctypes.c_double()
     _lib.check(ctx.lib.sdim_probe_philox_rate(ctx.ptr, ctypes.byref(v)), ctx.ptr, "philox probe")
     return v.value
+
+
+def trace_routed(n, d, shots):
+    """Whether the library runs a program on a trace engine (batched form)."""
+    if d == 2:
+        return trace_words(n) > 0 and (shots >= TRACE_MIN_SHOTS or n >= TRACE_MIN_QUDITS)
+    return n <= TRACE_U8_MAX_QUDITS and (shots >= TRACE_MIN_SHOTS or n >= TRACE_MIN_QUDITS)
+
+
+def tableau_resident(n, d, on_trace, smem_optin):
+    """Whether a program's x / z tableau lives in shared memory: bit planes for
+    d = 2, residue bytes otherwise, on one CTA (two for the odd-d trace pass)."""
+    tab = 2 * n * (-(-2 * n // 8) if d == 2 else 2 * n)
+    ctas = 2 if (on_trace and d != 2) else 1
+    return tab <= ctas * (smem_optin - 16384)
 
 
 def smem_peak(ctx):
@@ -472,9 +488,9 @@ def run_single(args, torch, dist, ws, rank, local):
 
     engine_flags = _lib.engine_flags(None if args.engine == "auto" else args.engine)
     trace_used = (d == 2 and trace_words(n) > 0 and
-                  (args.engine == "trace" or (args.engine == "auto" and shots >= TRACE_MIN_SHOTS)))
+                  (args.engine == "trace" or (args.engine == "auto" and trace_routed(n, d, shots))))
     odd_trace_used = (d != 2 and n <= TRACE_U8_MAX_QUDITS and
-                      (args.engine == "trace" or (args.engine == "auto" and shots >= TRACE_MIN_SHOTS)))
+                      (args.engine == "trace" or (args.engine == "auto" and trace_routed(n, d, shots))))
 
     def step(extra=None):
         rc = ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 0, shot0, shots, out.data_ptr(), stream.cuda_stream,
@@ -722,15 +738,26 @@ def run_uneven(args, torch, dist, ws, rank, local):
     if not np.array_equal(out.cpu().numpy(), ref_out):
         raise AssertionError("shot-group and per-shot engines disagree on the uneven batch")
 
-    # algorithmic bytes: det flags per program from its first shot
-    gb = 0.0
+    # algorithmic bytes: det flags per program from its first shot.  The x / z
+    # tableau is updated once per program on the trace engines and once per
+    # 32-shot group on the shot-group engine; each shot adds its phase-delta
+    # bytes.  Tableaux that fit in shared memory are bound by its bandwidth,
+    # larger ones stream through HBM: the step cannot beat the sum of both.
+    peak = smem_peak(ctx)
+    hbm = hbm_peak()
+    gb, t_min, streamed = 0.0, 0.0, 0.0
     for e, o in zip(entries, offs[:-1]):
         enc = e.program.enc
         nr = e.program.num_records
-        rec0 = ref_out[int(o):int(o) + nr]
-        gb += group_bytes(enc, (rec0 >> 7).astype(bool), 0.0, enc.n, enc.d, e.shots)
+        det_row = (ref_out[int(o):int(o) + nr] >> 7).astype(bool)
+        on_trace = trace_routed(enc.n, enc.d, e.shots)
+        xz = algorithmic_bytes_per_shot(enc, det_row, enc.n, enc.d) * (1 if on_trace else -(-e.shots // 32))
+        delta = e.shots * group_delta_bytes_per_shot(enc, det_row, 0.0, enc.n, enc.d)
+        resident = tableau_resident(enc.n, enc.d, on_trace, ctx.smem_optin)
+        gb += xz + delta
+        t_min += (xz / (peak if resident else hbm) + delta / peak) / 1e9
+        streamed += 0.0 if resident else xz
     mean_kern = statistics.mean(kern_ms)
-    peak = smem_peak(ctx)
 
     # end to end: host records (pinned), descriptors up and records down inside
     host = torch.empty(int(offs[-1]) + 1, dtype=torch.uint8, pin_memory=True)
@@ -780,11 +807,17 @@ def run_uneven(args, torch, dist, ws, rank, local):
         "batched_vs_plain": value / plain_rate,
         "per_shot_engine": {"value": units_per_step / (sum(ps_step_ms) / 1e3), "unit": UNIT,
                             "kernel_ms": statistics.mean(ps_kern_ms)},
-        "roofline": {"bound": "smem", "achieved": gb / (mean_kern / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": gb / (mean_kern / 1e3) / 1e9 / peak, "traffic": None,
-                     "kernel": "k_group_warp / k_group_cta over all variants",
-                     "algorithmic_bytes_per_launch": gb, "kernel_ms": mean_kern,
-                     "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth"},
+        "roofline": {"bound": "smem for resident tableaux, HBM for streamed ones",
+                     "achieved": gb / (mean_kern / 1e3) / 1e9, "peak": gb / t_min / 1e9, "unit": "GB/s",
+                     "frac": t_min * 1e3 / mean_kern, "traffic": None,
+                     "kernel": "trace engines (k_trace_pass*, k_phase_pass*) for n >= 160, k_group_warp / "
+                               "k_group_cta for the rest",
+                     "algorithmic_bytes_per_launch": gb, "streamed_bytes": streamed, "kernel_ms": mean_kern,
+                     "bound_ms": t_min * 1e3, "smem_peak_gbs": peak, "hbm_peak_gbs": hbm,
+                     "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth; "
+                                    "HBM from MEASURED_PEAKS.json",
+                     "bytes_model": "x/z tableau updates once per program (trace engines) or per 32-shot group, "
+                                    "plus per-shot phase-delta bytes"},
         "cpu_baseline": cpu,
         # one persistent launch per (dimension, team kind) present in the batch
         "gpu_launches": args.steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),

@@ -22,10 +22,13 @@
 //
 // The rowsum of a random measurement is a rank-1 update of X and Z plus the
 // column dots Z^T x_p: threads own 32-bit words (4 generators) of a set of
-// rows and keep four rows in flight, so an x / z region in global memory is
-// read and written at full width.  Per-shot work is spread over (shot,
+// rows and keep rows in flight (eight for a CTA team, whose x / z region may
+// stream from global memory; four for a warp team), so the region is read and
+// written at full width.  Per-shot work is spread over (shot,
 // chunk) thread pairs: thread t serves shot t % 32 and chunk t / 32.
 #pragma once
+#include <type_traits>
+
 #include "engine_u8.cuh"
 #include "team.cuh"
 
@@ -223,23 +226,26 @@ struct TGroupU8 {
           // x + f a <= d^2 - d stay inside a byte; dots add up in 16-bit lanes
           uint32_t dlo = 0u, dhi = 0u;
           int rows = 0;
-          // four rows in flight: their loads are issued before any store
-          for (; k + 3 * R < n; k += 4 * R) {
-            uint32_t xw[4], zw[4];
+          // RF rows in flight: their loads are issued before any store, which
+          // is what hides the latency when a large tableau (CTA teams) streams
+          // from global memory; a warp team's tableau is in shared memory
+          constexpr int RF = std::is_same<Team, CtaTeam>::value ? 8 : 4;
+          for (; k + (RF - 1) * R < n; k += RF * R) {
+            uint32_t xw[RF], zw[RF];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
+            for (int i = 0; i < RF; ++i) {
               xw[i] = xcol[(size_t)(k + i * R) * S4];
               zw[i] = zcol[(size_t)(k + i * R) * S4];
             }
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
+            for (int i = 0; i < RF; ++i) {
               const uint32_t a = CX[k + i * R], b = CZ[k + i * R];
               dlo += (zw[i] & 0x00FF00FFu) * a;
               dhi += ((zw[i] >> 8) & 0x00FF00FFu) * a;
               xcol[(size_t)(k + i * R) * S4] = packed_mod<DD>(xw[i] + fw * a);
               zcol[(size_t)(k + i * R) * S4] = packed_mod<DD>(zw[i] + fw * b);
             }
-            if ((rows += 4) >= 1024) {  // 1024 (d-1)^2 < 2^16
+            if ((rows += RF) >= 1024) {  // 1024 (d-1)^2 < 2^16
               dots[0] += (int)(dlo & 0xffffu);
               dots[2] += (int)(dlo >> 16);
               dots[1] += (int)(dhi & 0xffffu);
