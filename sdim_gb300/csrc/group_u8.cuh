@@ -22,9 +22,9 @@
 //
 // The rowsum of a random measurement is a rank-1 update of X and Z plus the
 // column dots Z^T x_p: threads own 32-bit words (4 generators) of a set of
-// rows and keep rows in flight (eight for a CTA team, whose x / z region may
-// stream from global memory; four for a warp team), so the region is read and
-// written at full width.  Per-shot work is spread over (shot,
+// rows and keep rows in flight (16 for the trace engine's x / z pass and 8
+// for a CTA team, whose x / z region may stream from global memory; four for
+// a warp team), so the region is read and written at full width.  Per-shot work is spread over (shot,
 // chunk) thread pairs: thread t serves shot t % 32 and chunk t / 32.
 #pragma once
 #include <type_traits>
@@ -227,9 +227,13 @@ struct TGroupU8 {
           uint32_t dlo = 0u, dhi = 0u;
           int rows = 0;
           // RF rows in flight: their loads are issued before any store, which
-          // is what hides the latency when a large tableau (CTA teams) streams
-          // from global memory; a warp team's tableau is in shared memory
-          constexpr int RF = std::is_same<Team, CtaTeam>::value ? 8 : 4;
+          // is what hides the latency when a large tableau streams from global
+          // memory (16 for the trace engine's x / z pass, 8 for the CTA-team
+          // group engine within its registers; a warp team's tableau is in
+          // shared memory)
+          constexpr int RF = std::is_same<Team, StreamCtaTeam>::value ? 16
+                             : std::is_same<Team, CtaTeam>::value     ? 8
+                                                                      : 4;
           for (; k + (RF - 1) * R < n; k += RF * R) {
             uint32_t xw[RF], zw[RF];
 #pragma unroll

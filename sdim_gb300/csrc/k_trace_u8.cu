@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const Trace
   uint2* win = reinterpret_cast<uint2*>(smem + hot_bytes + (xz_in_smem ? xz_bytes : 0));
   for (int i = blockIdx.x; i < ndesc; i += gridDim.x) {
     const TraceDescU8 td = descs[i];
-    TGroupU8<DD, CtaTeam> e(xz, hot, td.c.n, td.c.d, CtaTeam(red));
+    TGroupU8<DD, StreamCtaTeam> e(xz, hot, td.c.n, td.c.d, StreamCtaTeam(red));
     trace_program_u8(td, e, win, status);
     __syncthreads();
   }

@@ -56,4 +56,11 @@ struct CtaTeam {
   }
 };
 
+// A CtaTeam whose x / z region streams from global memory when it does not
+// fit in shared memory (the odd-d trace engine's single-CTA x / z pass): the
+// rank-1 update keeps more rows in flight for it.
+struct StreamCtaTeam : CtaTeam {
+  __device__ explicit StreamCtaTeam(int* red_) : CtaTeam(red_) {}
+};
+
 }  // namespace sdim
