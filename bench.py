@@ -339,6 +339,19 @@ def trace_routed(n, d, shots):
     return n <= TRACE_U8_MAX_QUDITS and (shots >= TRACE_MIN_SHOTS or n >= TRACE_MIN_QUDITS)
 
 
+def u8_single_cta(n, smem_optin):
+    """Whether the odd-d x / z pass of n qudits runs on one CTA with its
+    tableau in shared memory (else on a CTA pair or from global memory):
+    rows of 2n residue bytes padded to an odd word count, 36 rows of shot and
+    scratch state, and a 4 KB instruction window."""
+    stride = (2 * n + 3) & ~3
+    if not (stride >> 2) & 1:
+        stride += 4
+    npad = (n + 15) & ~15
+    hot = ((38 * stride + 2 * npad + 15) & ~15) + 512
+    return hot + 2 * n * stride + 4096 + 4096 <= smem_optin
+
+
 def tableau_resident(n, d, on_trace, smem_optin):
     """Whether a program's x / z tableau lives in shared memory: bit planes for
     d = 2, residue bytes otherwise, on one CTA (two for the odd-d trace pass)."""
@@ -655,13 +668,14 @@ def run_single(args, torch, dist, ws, rank, local):
             # one CTA): its algorithmic shared-memory bytes against the share
             # of the measured shared-memory bandwidth of the SMs it runs on
             xz_ms = stages[0]
-            sms = 2
+            sms = 1 if u8_single_cta(n, ctx.smem_optin) else 2
             share = peak * sms / ctx.num_sms
             xz_ach = per_shot_bytes / (xz_ms / 1e3) / 1e9
             roofline = {"bound": "smem (x/z pass, latency-bound on a CTA pair)", "achieved": xz_ach,
                         "peak": share, "unit": "GB/s", "frac": xz_ach / share,
                         "traffic": read_traffic(f"trace_engine_{args.workload}.md"),
-                        "kernel": f"k_trace_pass_split<{d}> (x/z pass), then k_phase_pass_u8<{d}>",
+                        "kernel": (f"k_trace_pass_{'u8' if sms == 1 else 'split'}<{d}> (x/z pass), "
+                                   f"then k_phase_pass_u8<{d}>"),
                         "peak_source": f"sdim_probe_smem_bandwidth x {sms}/{ctx.num_sms} SMs",
                         "algorithmic_bytes_per_launch": per_shot_bytes,
                         "bytes_model": "per-instruction bytes of one tableau update (x/z pass: one tableau per program)",
