@@ -42,6 +42,10 @@ struct sdim_ctx {
   std::string err;
   DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace, masks, tdescs_u8, trace_u8, xz_u8;
   cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
+  static constexpr int kXzStreams = 3;
+  cudaStream_t xzs[kXzStreams] = {};               // odd-d x / z passes of different runs, concurrently
+  cudaEvent_t ev_xzf = nullptr, ev_xzj[kXzStreams] = {};
+  DevBuf xz_queue;                                 // program counters of the dynamic x / z passes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void* staging = nullptr;  // pinned host staging of sdim_run_tables
   size_t staging_cap = 0;
@@ -505,32 +509,65 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     if (pair && (flags & SDIM_FLAG_SPLIT_XZ)) return 1;
     return single ? 0 : pair ? 1 : 2;
   };
+  // runs of programs with one (variant, mode); with several runs each goes
+  // on its own stream so that one run's tail overlaps the next run
+  struct Run { size_t b, e; int v, mode; size_t slot_off; };
+  std::vector<Run> runs;
+  size_t slot_total = 0;
   for (size_t b = 0; b < ku;) {
     const int v = trace_u8_variant(hu[b].c.d);
     const int mode = xz_mode(hu[b].c.n);
     size_t e = b;
     while (e < ku && trace_u8_variant(hu[e].c.d) == v && xz_mode(hu[e].c.n) == mode) ++e;
+    runs.push_back(Run{b, e, v, mode, slot_total});
+    if (mode == 2) {
+      const size_t grid = std::min<size_t>(e - b, 2 * (size_t)ctx->num_sms);
+      slot_total += trace_u8_xz_bytes(hu[b].c.n) * grid;
+    }
+    b = e;
+  }
+  if (slot_total && (rc = ensure(ctx, ctx->xz_u8, slot_total)) != SDIM_OK) return rc;
+  const bool fan = runs.size() > 1;
+  if (!runs.empty()) {
+    if ((rc = ensure(ctx, ctx->xz_queue, sizeof(unsigned) * runs.size())) != SDIM_OK) return rc;
+    CK(cudaMemsetAsync(ctx->xz_queue.p, 0, sizeof(unsigned) * runs.size(), s));
+    if (fan) CK(cudaEventRecord(ctx->ev_xzf, s));
+  }
+  bool used[sdim_ctx::kXzStreams] = {};
+  for (size_t r = 0; r < runs.size(); ++r) {
+    const Run& run = runs[r];
+    const size_t b = run.b, e = run.e;
+    const int v = run.v, mode = run.mode;
+    cudaStream_t rs = s;
+    if (fan) {
+      const int si = (int)(r % sdim_ctx::kXzStreams);
+      rs = ctx->xzs[si];
+      if (!used[si]) CK(cudaStreamWaitEvent(rs, ctx->ev_xzf, 0));
+      used[si] = true;
+    }
     const int nmax = hu[b].c.n;
     if (mode == 1) {
       launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax) + win,
-                            trace_u8_split_smem(nmax), s, du + b, (int)(e - b), status);
+                            trace_u8_split_smem(nmax), rs, du + b, (int)(e - b), status);
     } else {
       const size_t hot = trace_u8_hot_bytes(nmax), xz = trace_u8_xz_bytes(nmax);
       const bool in_smem = mode == 0;
       int grid = (int)std::min<size_t>(e - b, 65535);
-      if (!in_smem) {
-        grid = std::min(grid, 2 * ctx->num_sms);
-        if ((rc = ensure(ctx, ctx->xz_u8, xz * (size_t)grid)) != SDIM_OK) return rc;
-      }
+      if (!in_smem) grid = std::min(grid, 2 * ctx->num_sms);
       // about two generator columns per thread: 64 to kTracePassThreads threads
       const int block = std::max(64, std::min(kTracePassThreads, (nmax + 31) & ~31));
-      launch_trace_u8_xz(v, grid, block, hot + (in_smem ? xz : 0) + win, s, du + b, (int)(e - b),
-                         static_cast<uint8_t*>(ctx->xz_u8.p), xz, hot, in_smem ? 1 : 0, status);
+      unsigned* queue = in_smem ? nullptr : static_cast<unsigned*>(ctx->xz_queue.p) + r;
+      launch_trace_u8_xz(v, grid, block, hot + (in_smem ? xz : 0) + win, rs, du + b, (int)(e - b),
+                         static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, queue, status);
     }
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "odd-d trace pass launch");
-    b = e;
   }
+  for (int i = 0; i < sdim_ctx::kXzStreams; ++i)
+    if (used[i]) {
+      CK(cudaEventRecord(ctx->ev_xzj[i], ctx->xzs[i]));
+      CK(cudaStreamWaitEvent(s, ctx->ev_xzj[i], 0));
+    }
   // ---- coin pass on the second stream, alongside the x / z passes (independent work)
   if (coins) {
     CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
@@ -977,11 +1014,19 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
       cudaEventCreate(&ctx->ev_xz) != cudaSuccess || cudaEventCreate(&ctx->ev_phase) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_xzf, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return SDIM_ECUDA;
   }
+  for (int i = 0; i < sdim_ctx::kXzStreams; ++i)
+    if (cudaStreamCreateWithFlags(&ctx->xzs[i], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_xzj[i], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      delete ctx;
+      return SDIM_ECUDA;
+    }
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
   ctx->smem_per_sm = (int)prop.sharedMemPerMultiprocessor;
@@ -999,8 +1044,10 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   cudaStreamSynchronize(ctx->aux);
+  for (int i = 0; i < sdim_ctx::kXzStreams; ++i) cudaStreamSynchronize(ctx->xzs[i]);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
-                    &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8};
+                    &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8,
+                    &ctx->xz_queue};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);
@@ -1010,6 +1057,11 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaEventDestroy(ctx->ev_phase);
   cudaEventDestroy(ctx->ev_fork);
   cudaEventDestroy(ctx->ev_join);
+  cudaEventDestroy(ctx->ev_xzf);
+  for (int i = 0; i < sdim_ctx::kXzStreams; ++i) {
+    cudaEventDestroy(ctx->ev_xzj[i]);
+    cudaStreamDestroy(ctx->xzs[i]);
+  }
   cudaStreamDestroy(ctx->aux);
   cudaStreamDestroy(ctx->stream);
   delete ctx;

@@ -8,20 +8,38 @@
 namespace sdim {
 namespace {
 
+// One program per CTA at a time.  With queue (x / z in global memory, fewer
+// CTAs than programs) every CTA takes the next program from the atomic
+// counter, so the programs (largest first) are dealt out as CTAs free up;
+// without, CTA b takes programs b, b + grid, ...
 template <int DD>
 __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const TraceDescU8* __restrict__ descs, int ndesc,
                                                                      uint8_t* gxz, size_t xz_bytes, size_t hot_bytes,
-                                                                     int xz_in_smem, int* status) {
+                                                                     int xz_in_smem, unsigned* queue, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int red[40];
+  __shared__ int next;
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
   uint2* win = reinterpret_cast<uint2*>(smem + hot_bytes + (xz_in_smem ? xz_bytes : 0));
-  for (int i = blockIdx.x; i < ndesc; i += gridDim.x) {
+  int i = blockIdx.x;
+  if (queue) {
+    if (threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
+    __syncthreads();
+    i = next;
+  }
+  while (i < ndesc) {
     const TraceDescU8 td = descs[i];
     TGroupU8<DD, StreamCtaTeam> e(xz, hot, td.c.n, td.c.d, StreamCtaTeam(red));
     trace_program_u8(td, e, win, status);
     __syncthreads();
+    if (queue) {
+      if (threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
+      __syncthreads();
+      i = next;
+    } else {
+      i += gridDim.x;
+    }
   }
 }
 
@@ -62,8 +80,8 @@ struct TraceU8 {
     k_trace_pass_split<DD><<<2 * pairs, kTracePassThreads, smem, s>>>(d, nd, scratch_off, status);
   }
   static void xz(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
-                 size_t xzb, size_t hot, int in_smem, int* status) {
-    k_trace_pass_u8<DD><<<grid, block, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, status);
+                 size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status) {
+    k_trace_pass_u8<DD><<<grid, block, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, queue, status);
   }
   static void phase(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, long long total,
                     int* status) {
@@ -100,12 +118,12 @@ void launch_trace_u8_split(int variant, int pairs, size_t smem, size_t scratch_o
 }
 
 void launch_trace_u8_xz(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
-                        uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status) {
+                        uint8_t* gxz, size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status) {
   switch (variant) {
-    case 0: TraceU8<3>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
-    case 1: TraceU8<5>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
-    case 2: TraceU8<7>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
-    default: TraceU8<0>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 0: TraceU8<3>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, queue, status); break;
+    case 1: TraceU8<5>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, queue, status); break;
+    case 2: TraceU8<7>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, queue, status); break;
+    default: TraceU8<0>::xz(grid, block, smem, s, d, nd, gxz, xzb, hot, in_smem, queue, status); break;
   }
 }
 

@@ -165,8 +165,11 @@ cudaError_t trace_u8_set_smem(int optin);
 size_t trace_u8_hot_bytes(int n);
 size_t trace_u8_xz_bytes(int n);
 size_t trace_u8_phase_smem(int n);
+// x / z pass on single CTAs; queue (may be null): a zeroed counter from which
+// the CTAs take programs dynamically (the x / z regions in global memory at
+// gxz + blockIdx.x * xzb).
 void launch_trace_u8_xz(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
-                        uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status);
+                        uint8_t* gxz, size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status);
 // x / z pass on CTA pairs (trace_split_u8.cuh): `pairs` clusters of two,
 // the instruction window at trace_u8_split_smem(nmax),
 // smem = that + trace_u8_window_bytes().
