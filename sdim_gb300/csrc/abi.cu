@@ -373,6 +373,16 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       }
     }
     if (mtotal && (rc = ensure(ctx, ctx->masks, mtotal)) != SDIM_OK) return rc;
+    // shots per lane of each phase-pass launch (one per trace-row width)
+    std::vector<int> spl(k, 1);
+    for (size_t b = 0; b < k;) {
+      const int tw = trace_words(jobs[b].c->n);
+      size_t e = b;
+      long long shots = 0;
+      while (e < k && trace_words(jobs[e].c->n) == tw) shots += jobs[e++].nshots;
+      for (size_t i = b; i < e; ++i) spl[i] = shots >= kPhasePairMinShots ? 2 : 1;
+      b = e;
+    }
     long long groups = 0;
     for (size_t i = 0; i < k; ++i) {
       const Job& j = jobs[i];
@@ -390,7 +400,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.c.d = j.c->d;
       td.c.nmeas = j.c->nmeas;
       td.c.nshots = (int)j.nshots;
-      groups += (j.nshots + 31) / 32;
+      groups += (j.nshots + 32 * spl[i] - 1) / (32 * spl[i]);
+      td.spl = spl[i];
       uint8_t* b = static_cast<uint8_t*>(ctx->trace.p) + off[i];
       size_t o[4];
       trace_offsets(j.c->nmeas, j.c->nn1, tw, o);
@@ -583,17 +594,17 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   if (timed) CK(cudaEventRecord(ctx->ev_xz, s));
   // ---- phase passes
   for (size_t b = 0; b < k;) {
-    const int tw = hd[b].tw;
+    const int tw = hd[b].tw, sp = hd[b].spl;
     size_t e = b;
     long long items = 0;
     while (e < k && hd[e].tw == tw) {
-      items = hd[e].c.item_begin + (hd[e].c.nshots + 31) / 32;
+      items = hd[e].c.item_begin + (hd[e].c.nshots + 32 * sp - 1) / (32 * sp);
       ++e;
     }
     const int warps = kPhaseThreads / 32;
     const long long grid = (items + warps - 1) / warps;
     if (grid > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one phase pass");
-    if (!launch_phase_pass(tw, (int)grid, 32 * warps, s, dd + b, (int)(e - b), items, status))
+    if (!launch_phase_pass(tw, sp, (int)grid, 32 * warps, s, dd + b, (int)(e - b), items, status))
       return fail(ctx, SDIM_EINVAL, "no phase pass for trace rows of " + std::to_string(tw) + " words");
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "phase pass launch");

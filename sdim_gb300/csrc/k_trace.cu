@@ -25,24 +25,35 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
   }
 }
 
-// One single-warp block per 32-shot group (groups of all programs are
-// numbered through descs[].c.item_begin).  With the group index taken from
-// blockIdx alone, every per-program value and the whole measurement loop
+// One single-warp block per group of 32 SPL shots (groups of all programs
+// are numbered through descs[].c.item_begin).  With the group index taken
+// from blockIdx alone, every per-program value and the whole measurement loop
 // control are provably warp-uniform, so they stay out of the per-lane
-// registers.  Up to 16-word rows, 32 blocks per SM at 64 registers; wider
-// rows hold more delta words per lane and get 128.
-template <int TW>
-__global__ void __launch_bounds__(32, TW >= 16 ? 16 : 32) k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc,
-                                                   long long total_groups, const int* status) {
-  __shared__ uint8_t rec[32 * kRecStride];
+// registers.  Up to 16-word rows and one shot per lane, 32 blocks per SM at
+// 64 registers; wider rows or two shots per lane get 128.
+template <int TW, int SPL>
+__global__ void __launch_bounds__(32, (TW >= 16 || SPL == 2) ? 16 : 32)
+    k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc, long long total_groups, const int* status) {
+  __shared__ uint8_t rec[32 * SPL * kRecStride];
   if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
   const long long g = blockIdx.x;
   if (g >= total_groups) return;
   const int i = find_trace_desc(descs, ndesc, g);
-  if (descs[i].masks)
-    phase_program<TW, true>(descs + i, g - descs[i].c.item_begin, threadIdx.x, rec);
-  else
-    phase_program<TW, false>(descs + i, g - descs[i].c.item_begin, threadIdx.x, rec);
+  const long long lg = g - descs[i].c.item_begin;
+  if constexpr (SPL == 2) {
+    if (descs[i].masks) {
+      phase_program_pair<TW>(descs + i, lg, threadIdx.x, rec);
+    } else {  // no masks: the two 32-shot halves one after the other
+      phase_program<TW, false>(descs + i, 2 * lg, threadIdx.x, rec);
+      if ((2 * lg + 1) * 32 < (long long)descs[i].c.nshots)
+        phase_program<TW, false>(descs + i, 2 * lg + 1, threadIdx.x, rec);
+    }
+  } else {
+    if (descs[i].masks)
+      phase_program<TW, true>(descs + i, lg, threadIdx.x, rec);
+    else
+      phase_program<TW, false>(descs + i, lg, threadIdx.x, rec);
+  }
 }
 
 // One thread per (chunk group, shot) item of the coin pass; descs with
@@ -105,16 +116,23 @@ void launch_trace_pass(int threads, int grid, size_t smem, cudaStream_t s, const
     k_trace_pass<256><<<grid, 256, smem, s>>>(descs, ndesc, gxz, xz_bytes, hot_bytes, xz_in_smem, status);
 }
 
-bool launch_phase_pass(int tw, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
-                       long long total_groups, int* status) {
+template <int SPL>
+bool launch_phase_spl(int tw, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
+                      long long total_groups, int* status) {
   switch (tw) {
-    case 2: k_phase_pass<2><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    case 4: k_phase_pass<4><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    case 8: k_phase_pass<8><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    case 16: k_phase_pass<16><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    case 32: k_phase_pass<32><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    case 2: k_phase_pass<2, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    case 4: k_phase_pass<4, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    case 8: k_phase_pass<8, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    case 16: k_phase_pass<16, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    case 32: k_phase_pass<32, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
     default: return false;
   }
+}
+
+bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
+                       long long total_groups, int* status) {
+  return spl == 2 ? launch_phase_spl<2>(tw, grid, block, s, descs, ndesc, total_groups, status)
+                  : launch_phase_spl<1>(tw, grid, block, s, descs, ndesc, total_groups, status);
 }
 
 }  // namespace sdim

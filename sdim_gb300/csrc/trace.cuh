@@ -32,7 +32,7 @@ namespace sdim {
 // cmap its chunk map: bit i of word w * nshots + s set when pair (32 w + i)
 // of shot s is not zero (bits at or past nchunk are undefined).
 struct TraceDesc {
-  CircuitDesc c;  // item_begin counts 32-shot groups of the phase pass
+  CircuitDesc c;  // item_begin counts the phase pass's groups of 32 spl shots
   const uint4* steps;
   const uint4* lops;
   const uint4* wins;
@@ -51,6 +51,7 @@ struct TraceDesc {
   int nchunk;  // 32-ordinal chunks of fire masks (those before the last measurement)
   int tw;      // words per trace row
   int wn;      // words per generator half
+  int spl;     // shots per lane of the phase pass (item_begin counts groups of 32 spl)
 };
 
 __host__ __device__ inline size_t round_up(size_t b, size_t a) { return (b + a - 1) / a * a; }
@@ -153,10 +154,15 @@ void launch_coin_pass(int grid, int block, size_t smem, cudaStream_t s, const Tr
 // shared memory so that no coin block lands beside them.
 constexpr size_t kCoinFenceSmem = 8192;
 
-// Phase pass: one lane per shot, one warp per 32-shot group; every program of
-// descs has trace rows of tw words.  Returns false for an unsupported tw.
-bool launch_phase_pass(int tw, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
+// Phase pass: spl (1 or 2) shots per lane, one warp per group of 32 spl
+// shots (item_begin counts those groups); every program of descs has trace
+// rows of tw words.  Returns false for an unsupported tw.
+bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        long long total_groups, int* status);
+
+// From this many shots in one phase-pass launch, lanes carry two shots each:
+// with 152 SMs that still leaves 8 single-warp blocks per SM.
+constexpr long long kPhasePairMinShots = 152LL * 64 * 8;
 
 // Odd-d trace engine (k_trace_u8.cu).  variant: 0, 1, 2 for d = 3, 5, 7, 3
 // for any other odd prime.

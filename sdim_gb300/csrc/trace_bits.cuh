@@ -628,6 +628,124 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
   }
 }
 
+// Two shots per lane (coin-pass masks only): lane l of group g carries shots
+// 64 g + l and 64 g + 32 + l, each with its own delta and fire cursor, while
+// the per-measurement work that does not depend on the shot -- header and
+// factor-row loads, the measurement kind, the loop -- is done once for both.
+// Records of the group's 64 rows are staged in rec[64][kRecStride].
+template <int TW>
+__device__ __forceinline__ void phase_program_pair(const TraceDesc* __restrict__ tdp, long long group, int lane,
+                                                   uint8_t* rec) {
+  constexpr int FH = TW / 2;
+  constexpr bool kAhead = FH <= 8;
+  const uint4* __restrict__ mhdr = tdp->mhdr;
+  const uint32_t* __restrict__ mrow = tdp->mrow;
+  const int nm = tdp->nm, wn = tdp->wn, nmeas = tdp->c.nmeas, nshots = tdp->c.nshots;
+  const uint32_t nn1 = (uint32_t)tdp->nn1;
+  const long long first = group * 64;
+  const int rows = (int)min(64LL, (long long)nshots - first);
+  uint8_t* __restrict__ gout = tdp->c.out + first * (long long)nmeas;
+  const PhiloxKeys K(tdp->c.seed);
+  uint32_t d1[2][TW];
+  bool active[2];
+  uint32_t slo[2], shi[2];
+  FireCursor fc[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+#pragma unroll
+    for (int w = 0; w < TW; ++w) d1[s][w] = 0u;
+    const long long rel = first + 32 * s + lane;
+    active[s] = rel < (long long)nshots;
+    const unsigned long long shot = (unsigned long long)(tdp->c.shot0 + rel);
+    slo[s] = (uint32_t)shot;
+    shi[s] = (uint32_t)(shot >> 32);
+    fc[s].masks = reinterpret_cast<const uint2*>(tdp->masks);
+    fc[s].cmap = tdp->cmap;
+    fc[s].nshots = nshots;
+    fc[s].rel = (int)rel;
+    fc[s].nchunk = tdp->nchunk;
+    fc[s].ncw = (tdp->nchunk + 31) >> 5;
+    fc[s].cw = -1;
+    fc[s].cbits = fc[s].ax = fc[s].bz = fc[s].base = 0u;
+    fc[s].next = 0xffffffffu;
+    if (active[s]) fc[s].advance();
+  }
+  uint4 hn = make_uint4(0u, 0u, 0u, 0u);
+  uint32_t fn[FH];
+  if (nm > 0) {
+    hn = __ldg(mhdr);
+    if constexpr (kAhead) load_row<FH>(mrow, fn);
+  }
+  for (int k = 0; k < nm; ++k) {
+    const uint4 h = hn;
+    uint32_t f[FH];
+    if constexpr (kAhead) {
+#pragma unroll
+      for (int w = 0; w < FH; ++w) f[w] = fn[w];
+      if (k + 1 < nm) {
+        hn = __ldg(mhdr + k + 1);
+        load_row<FH>(mrow + (size_t)(k + 1) * 2 * TW, fn);
+      }
+    } else {
+      if (k + 1 < nm) hn = __ldg(mhdr + k + 1);
+    }
+    const uint32_t nend = h.z < nn1 ? h.z : nn1;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      while (fc[s].next < nend) {
+        const uint32_t j = fc[s].next, bit = 1u << (j & 31u);
+        const uint32_t mz = (fc[s].ax & bit) ? 0xffffffffu : 0u, mx = (fc[s].bz & bit) ? 0xffffffffu : 0u;
+        fc[s].ax &= ~bit;
+        fc[s].bz &= ~bit;
+        const uint32_t* nr = tdp->nrow + (size_t)j * 2 * TW;
+#pragma unroll
+        for (int w = 0; w < TW; ++w) d1[s][w] ^= (__ldg(nr + TW + w) & mz) ^ (__ldg(nr + w) & mx);
+        fc[s].advance();
+      }
+    }
+    const uint32_t* row = mrow + (size_t)k * 2 * TW;
+    const uint32_t det = h.x & 1u;
+    int m[2];
+    if (!det) {
+      const int p = (int)h.y, wp = p >> 5, bp = p & 31;
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const uint32_t dp = (word_at<0, TW>(d1[s], wp) >> bp) & 1u;
+        if (dp) {
+#pragma unroll
+          for (int w = 0; w < TW; ++w) d1[s][w] ^= __ldg(row + w);
+        }
+        m[s] = active[s] ? mulshift(K.block(make_uint4((uint32_t)k, slo[s], shi[s], 0u)).x, 2u) : 0;
+        put_bit<0, TW>(d1[s], wn + wp, bp, dp);
+        put_bit<0, TW>(d1[s], wp, bp, (uint32_t)m[s]);
+      }
+    } else {
+      if constexpr (!kAhead) load_row<FH>(row, f);
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        int acc = 0;
+#pragma unroll
+        for (int w = 0; w < FH; ++w) acc += __popc(f[w] & d1[s][w]);
+        m[s] = (((((int)h.w + 2 * acc) & 3) + 1) >> 1) & 1;
+      }
+    }
+    if (h.x & 2u) {
+#pragma unroll
+      for (int s = 0; s < 2; ++s)
+        if (m[s] & 1) {
+#pragma unroll
+          for (int w = 0; w < TW; ++w) d1[s][w] ^= __ldg(row + TW + w);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 2; ++s) rec[(32 * s + lane) * kRecStride + (k & (kRecWindow - 1))] = (uint8_t)(m[s] | (int)(det << 7));
+    if ((k & (kRecWindow - 1)) == kRecWindow - 1 || k == nm - 1) {
+      const int k0 = k & ~(kRecWindow - 1);
+      flush_records(rec, gout, nmeas, rows, k0, min(k + 1, nmeas) - k0, lane);
+    }
+  }
+}
+
 // Coin pass item it of td: shot it % nshots, chunks kCoinChunksPerItem *
 // (it / nshots) onwards.  For every fired N1 (rare) the Pauli is drawn here,
 // so masks[c * nshots + s] = (x mask, z mask): bit i of .x set when ordinal

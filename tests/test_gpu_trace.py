@@ -95,6 +95,25 @@ def test_coins_in_the_phase_pass_match_the_coin_pass(prob):
     assert np.array_equal(out, oracle_run([spec], 12, 7, 130)["records"])
 
 
+def test_two_shots_per_lane_partial_groups_with_and_without_masks():
+    """From 77,824 shots per launch the phase pass carries two shots per lane.
+    An odd shot count leaves a partial last 64-shot group. Run without the
+    coin pass, each group replays its two 32-shot halves in turn. Both forms
+    give the group engine's records, and the ends of the range give the
+    oracle's."""
+    spec = workloads.surface_memory(3, 2, prob=0.05)
+    prog = Program(spec.build())
+    dp = prog.compile(True)
+    ctx = prog.context
+    nshots = 80_017
+    ref = prog.sample(nshots, seed=3, shot0=5, engine="group")
+    for flags in (_lib.FLAG_TRACE, _lib.FLAG_TRACE | _lib.FLAG_NO_COIN_PASS):
+        out = np.empty((nshots, dp.num_records), dtype=np.uint8)
+        _lib.check(ctx.lib.sdim_run(ctx.ptr, dp.ptr, 3, 5, nshots, out.ctypes.data, flags), ctx.ptr, "trace")
+        assert np.array_equal(out, ref), flags
+    assert np.array_equal(ref[-40:], oracle_run([spec], 3, 5 + nshots - 40, 40)["records"])
+
+
 def test_xz_pass_in_global_memory():
     spec = workloads.random_hpc(300, 2, 1200, seed=31, mr_every=150, mr_fraction=0.2)
     prog = Program(spec.build())
