@@ -46,9 +46,10 @@ extern "C" {
 #define SDIM_FLAG_PER_SHOT 32u   /* batched runs use one warp per shot instead of the shot-group engine */
 #define SDIM_FLAG_TEAM_WARP 64u  /* shot groups on one warp each, whatever n */
 #define SDIM_FLAG_TEAM_CTA 128u  /* shot groups on one CTA each, whatever n */
-#define SDIM_FLAG_TRACE 256u     /* d = 2: trace engine (one x / z pass per program, one lane per shot)
-                                    whatever the shot count; by default it runs from 128 shots */
-#define SDIM_FLAG_NO_TRACE 512u  /* d = 2: shot-group engine only */
+#define SDIM_FLAG_TRACE 256u     /* trace engines (one x / z pass per program, then a per-shot phase
+                                    replay) whatever the shot count; by default they run from 128
+                                    shots or 160 qudits (d = 2 up to n = 512, odd d up to 2048) */
+#define SDIM_FLAG_NO_TRACE 512u  /* no trace engine: shot-group engines only */
 #define SDIM_FLAG_NO_COIN_PASS 1024u /* trace engine: draw N1 coins inside the phase pass, no coin pass */
 #define SDIM_FLAG_SPLIT_XZ 2048u /* odd-d trace engine: x / z pass on a CTA pair whenever it fits */
 

@@ -9,12 +9,13 @@ baseline; the product (``sdim_gb300``) never does.
 * ``tableau_oracle.c``-- plain-C restatement of sdim's ExtendedTableau and
                          shot loop (unreduced int64, lazy modulo, gate
                          compositions as in the reference); see its header.
-* ``numpy_port``      -- NumPy restatement in the reference's own execution
-                         model, the CPU baseline timed by ``bench.py``.
+* ``frame``           -- NumPy restatement of the reference's Pauli-frame
+                         route (multi-shot ``simulate``), with its draws on
+                         the same Philox stream.
 
 The restatements are pinned against fixtures produced by the reference
 itself (``tests/golden/make_golden.py`` imports sdim, injects this Philox
-stream and records outcomes and tableaux).
+stream and records outcomes, tableaux and frame-route records).
 """
 from __future__ import annotations
 

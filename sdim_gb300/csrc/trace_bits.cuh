@@ -5,8 +5,9 @@
 // delta_s mod 4) depending on the shot's outcomes and noise.  Nothing forces
 // the sharing to stop at 32 shots: the x / z pass runs x / z / c once per
 // program and records in a trace (trace.cuh) every value the delta updates
-// read; the phase pass then gives every shot one lane, delta_s in registers
-// (two bit planes over the 2n generators, TW words each), and replays
+// read; the phase pass then gives every shot a lane (or half of one),
+// delta_s in registers (its high bit plane over the 2n generators, TW words;
+// the low plane is always zero, see phase_program), and replays
 //   N1 before measurement k : coin per ordinal; on a fire with Pauli
 //                             X^a Z^b, delta ^= 2 (a z_q + b x_q)
 //   random M (pivot p)      : delta_g += delta_p for g in FW;
