@@ -352,12 +352,41 @@ def u8_single_cta(n, smem_optin):
     return hot + 2 * n * stride + 4096 + 4096 <= smem_optin
 
 
-def tableau_resident(n, d, on_trace, smem_optin):
-    """Whether a program's x / z tableau lives in shared memory: bit planes for
-    d = 2, residue bytes otherwise, on one CTA (two for the odd-d trace pass)."""
+def _split_stride(c):
+    s = (c + 3) & ~3
+    return s if (s >> 2) & 1 else s + 4
+
+
+def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152):
+    """Where the library runs the odd-d x / z pass of n qudits, as (CTAs per
+    program, where its columns live: "smem", "l2" or "hbm").  One CTA when its
+    tableau fits in shared memory.  Else, in a batch of at least num_sms / 2
+    odd-d trace programs, a CTA pair when that fits and one CTA streaming from
+    HBM above; in a smaller batch a cluster of 8 CTAs, columns in shared
+    memory up to n = 636 and streamed from global memory, held in L2, above."""
+    if u8_single_cta(n, smem_optin):
+        return 1, "smem"
+    r16 = lambda x: (x + 15) & ~15  # noqa: E731
+    npad, win = (n + 15) & ~15, 4096
+    if 2 * odd_trace_programs >= num_sms:
+        sl = _split_stride(n)
+        pair = r16(2 * n * sl + 2 * sl + 2 * npad) + 4 * sl + 2 * r16(16 + 3 * npad)
+        return (2, "smem") if pair + win + 4096 <= smem_optin else (1, "hbm")
+    cols = (n + 3) // 4
+    sl = _split_stride(cols)
+    xchg = 16 + 16 + 2 * npad + ((cols + 15) & ~15) + 4 * (16 + 2 * npad)
+    hot = r16(2 * sl + 2 * npad) + 4 * sl + 16 + 2 * r16(xchg)
+    return 8, ("smem" if hot + r16(2 * n * sl) + win + 4096 <= smem_optin else "l2")
+
+
+def tableau_place(n, d, on_trace, smem_optin, odd_trace_programs=1, num_sms=152):
+    """Where a program's x / z tableau lives ("smem", "l2" or "hbm"): bit
+    planes for d = 2 and the odd-d shot-group engine on one CTA, the odd-d
+    trace pass as u8_xz_layout places it."""
+    if on_trace and d != 2:
+        return u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms)[1]
     tab = 2 * n * (-(-2 * n // 8) if d == 2 else 2 * n)
-    ctas = 2 if (on_trace and d != 2) else 1
-    return tab <= ctas * (smem_optin - 16384)
+    return "smem" if tab <= smem_optin - 16384 else "hbm"
 
 
 def smem_peak(ctx):
@@ -365,6 +394,14 @@ def smem_peak(ctx):
     from sdim_gb300 import _lib
     v = ctypes.c_double()
     _lib.check(ctx.lib.sdim_probe_smem_bandwidth(ctx.ptr, ctypes.byref(v)), ctx.ptr, "smem probe")
+    return v.value
+
+
+def l2_peak(ctx):
+    import ctypes
+    from sdim_gb300 import _lib
+    v = ctypes.c_double()
+    _lib.check(ctx.lib.sdim_probe_l2_bandwidth(ctx.ptr, ctypes.byref(v)), ctx.ptr, "L2 probe")
     return v.value
 
 
@@ -664,18 +701,19 @@ def run_single(args, torch, dist, ws, rank, local):
         roofline = dict(group_model)
         roofline["traffic"] = None
         if odd_trace_used:
-            # the x / z pass updates one tableau per program on a CTA pair (or
-            # one CTA): its algorithmic shared-memory bytes against the share
-            # of the measured shared-memory bandwidth of the SMs it runs on
+            # the x / z pass updates one tableau per program on one CTA, a CTA
+            # pair or a cluster of 8: its algorithmic shared-memory bytes
+            # against the share of the measured shared-memory bandwidth of the
+            # SMs it runs on
             xz_ms = stages[0]
-            sms = 1 if u8_single_cta(n, ctx.smem_optin) else 2
+            sms, _ = u8_xz_layout(n, 1, ctx.smem_optin, ctx.num_sms)
             share = peak * sms / ctx.num_sms
             xz_ach = per_shot_bytes / (xz_ms / 1e3) / 1e9
-            roofline = {"bound": "smem (x/z pass, latency-bound on a CTA pair)", "achieved": xz_ach,
-                        "peak": share, "unit": "GB/s", "frac": xz_ach / share,
+            xz_kernel = {1: "k_trace_pass_u8", 2: "k_trace_pass_split", 8: "k_trace_pass_cluster"}[sms]
+            roofline = {"bound": f"smem (x/z pass, latency-bound on {sms} CTA{'s' if sms > 1 else ''})",
+                        "achieved": xz_ach, "peak": share, "unit": "GB/s", "frac": xz_ach / share,
                         "traffic": read_traffic(f"trace_engine_{args.workload}.md"),
-                        "kernel": (f"k_trace_pass_{'u8' if sms == 1 else 'split'}<{d}> (x/z pass), "
-                                   f"then k_phase_pass_u8<{d}>"),
+                        "kernel": f"{xz_kernel}<{d}> (x/z pass), then k_phase_pass_u8<{d}>",
                         "peak_source": f"sdim_probe_smem_bandwidth x {sms}/{ctx.num_sms} SMs",
                         "algorithmic_bytes_per_launch": per_shot_bytes,
                         "bytes_model": "per-instruction bytes of one tableau update (x/z pass: one tableau per program)",
@@ -757,9 +795,14 @@ def run_uneven(args, torch, dist, ws, rank, local):
     # 32-shot group on the shot-group engine; each shot adds its phase-delta
     # bytes.  Tableaux that fit in shared memory are bound by its bandwidth,
     # larger ones stream through HBM: the step cannot beat the sum of both.
+    # odd-d trace programs whose columns stream from global memory on CTA
+    # clusters (small batches) stay in L2: bound by the measured L2 bandwidth
     peak = smem_peak(ctx)
     hbm = hbm_peak()
-    gb, t_min, streamed = 0.0, 0.0, 0.0
+    l2 = l2_peak(ctx)
+    odd_trace = sum(1 for e in entries if e.program.enc.d != 2 and e.program.enc.n <= TRACE_U8_MAX_QUDITS
+                    and trace_routed(e.program.enc.n, e.program.enc.d, e.shots))
+    gb, t_min, streamed, in_l2 = 0.0, 0.0, 0.0, 0.0
     for e, o in zip(entries, offs[:-1]):
         enc = e.program.enc
         nr = e.program.num_records
@@ -767,10 +810,11 @@ def run_uneven(args, torch, dist, ws, rank, local):
         on_trace = trace_routed(enc.n, enc.d, e.shots)
         xz = algorithmic_bytes_per_shot(enc, det_row, enc.n, enc.d) * (1 if on_trace else -(-e.shots // 32))
         delta = e.shots * group_delta_bytes_per_shot(enc, det_row, 0.0, enc.n, enc.d)
-        resident = tableau_resident(enc.n, enc.d, on_trace, ctx.smem_optin)
+        place = tableau_place(enc.n, enc.d, on_trace, ctx.smem_optin, odd_trace, ctx.num_sms)
         gb += xz + delta
-        t_min += (xz / (peak if resident else hbm) + delta / peak) / 1e9
-        streamed += 0.0 if resident else xz
+        t_min += (xz / {"smem": peak, "l2": l2, "hbm": hbm}[place] + delta / peak) / 1e9
+        streamed += xz if place == "hbm" else 0.0
+        in_l2 += xz if place == "l2" else 0.0
     mean_kern = statistics.mean(kern_ms)
 
     # end to end: host records (pinned), descriptors up and records down inside
@@ -821,15 +865,18 @@ def run_uneven(args, torch, dist, ws, rank, local):
         "batched_vs_plain": value / plain_rate,
         "per_shot_engine": {"value": units_per_step / (sum(ps_step_ms) / 1e3), "unit": UNIT,
                             "kernel_ms": statistics.mean(ps_kern_ms)},
-        "roofline": {"bound": "smem for resident tableaux, HBM for streamed ones",
+        "roofline": {"bound": "smem for resident tableaux, L2 for columns streamed by CTA clusters, HBM for "
+                              "other streamed tableaux",
                      "achieved": gb / (mean_kern / 1e3) / 1e9, "peak": gb / t_min / 1e9, "unit": "GB/s",
                      "frac": t_min * 1e3 / mean_kern, "traffic": None,
                      "kernel": "trace engines (k_trace_pass*, k_phase_pass*) for n >= 160, k_group_warp / "
                                "k_group_cta for the rest",
-                     "algorithmic_bytes_per_launch": gb, "streamed_bytes": streamed, "kernel_ms": mean_kern,
-                     "bound_ms": t_min * 1e3, "smem_peak_gbs": peak, "hbm_peak_gbs": hbm,
-                     "peak_source": "shared-memory read bandwidth measured live by sdim_probe_smem_bandwidth; "
-                                    "HBM from MEASURED_PEAKS.json",
+                     "algorithmic_bytes_per_launch": gb, "streamed_bytes": streamed, "l2_bytes": in_l2,
+                     "kernel_ms": mean_kern, "bound_ms": t_min * 1e3, "smem_peak_gbs": peak, "l2_peak_gbs": l2,
+                     "hbm_peak_gbs": hbm,
+                     "peak_source": "shared-memory read and L2 read+write bandwidth measured live by "
+                                    "sdim_probe_smem_bandwidth / sdim_probe_l2_bandwidth; HBM from "
+                                    "MEASURED_PEAKS.json",
                      "bytes_model": "x/z tableau updates once per program (trace engines) or per 32-shot group, "
                                     "plus per-shot phase-delta bytes"},
         "cpu_baseline": cpu,

@@ -52,6 +52,12 @@ extern "C" {
 #define SDIM_FLAG_NO_TRACE 512u  /* no trace engine: shot-group engines only */
 #define SDIM_FLAG_NO_COIN_PASS 1024u /* trace engine: draw N1 coins inside the phase pass, no coin pass */
 #define SDIM_FLAG_SPLIT_XZ 2048u /* odd-d trace engine: x / z pass on a CTA pair whenever it fits */
+#define SDIM_FLAG_CLUSTER_XZ 4096u /* odd-d trace engine: x / z pass on a cluster of 8 CTAs whatever n,
+                                      columns in shared memory where they fit (global memory with
+                                      SDIM_FLAG_FORCE_GMEM); by default the cluster takes the programs
+                                      that do not fit one CTA in batches of fewer than 76 odd-d trace
+                                      programs (larger batches use CTA pairs, then single CTAs streaming
+                                      from global memory) */
 
 /* snapshot modes for sdim_snapshot */
 #define SDIM_SNAP_EVERY_INSTRUCTION 1
@@ -149,6 +155,12 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
  * the roofline denominator for tableaux resident in shared memory.  No
  * counterpart in the reference (which has no device code). */
 int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs);
+/* Measured L2 read + write bandwidth in GB/s: every 16-byte word of a 48 MB
+ * buffer read and rewritten, 40 passes after two warm-up passes.  The
+ * roofline denominator for tableau columns that stream from global memory
+ * but stay in L2 (the odd-d trace engine's streamed CTA clusters).  No
+ * counterpart in the reference. */
+int sdim_probe_l2_bandwidth(sdim_ctx* ctx, double* gbs);
 /* Philox4x32-10 blocks per second the device draws at most (eight
  * independent chains per thread, keys per thread, as the trace engine's coin
  * pass draws them): the compute roofline of sampling N1 coins.  No

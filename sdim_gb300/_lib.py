@@ -30,6 +30,7 @@ FLAG_TRACE = 256
 FLAG_NO_TRACE = 512
 FLAG_NO_COIN_PASS = 1024
 FLAG_SPLIT_XZ = 2048
+FLAG_CLUSTER_XZ = 4096
 
 
 def engine_flags(engine) -> int:
@@ -72,6 +73,7 @@ SIGNATURES = {
     "sdim_last_stage_ms": (C.c_int, [_P, _P]),
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "sdim_probe_l2_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_probe_philox_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_run_noalloc": (C.c_int, [_P, C.c_int64, _P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_int64, _P,
                                    _P, C.c_char_p, C.c_size_t]),

@@ -508,17 +508,33 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
   }
-  // odd d: one CTA with the tableau in shared memory when it fits, else a
-  // CTA pair splitting the generator columns (trace_split_u8.cuh) when that
-  // fits, else one CTA with the tableau in global memory
+  // odd d, by mode: 0, one CTA with the tableau in shared memory when it
+  // fits.  Otherwise, in a batch with programs enough to fill the SMs (76 or
+  // more), for throughput: 1, a CTA pair splitting the generator columns
+  // (trace_split_u8.cuh) when that fits, else 2, one CTA with the tableau in
+  // global memory.  In a smaller batch, for latency: a cluster of
+  // kTraceClusterCtas CTAs (trace_cluster_u8.cuh) with its columns in shared
+  // memory (3) or global memory (4).  A cluster shares each measurement's
+  // fixed cost (two cluster barriers, pivot search, broadcast) among 8 SMs,
+  // so it finishes one program sooner but a full batch later.
   const size_t optin = (size_t)ctx->smem_optin;
   const size_t win = trace_u8_window_bytes();
+  const bool few = ku * 2 < (size_t)ctx->num_sms;
   auto xz_mode = [&](int n) {
     const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
     const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
+    const bool cl_smem = trace_u8_cluster_hot(n) + trace_u8_cluster_xz(n) + win + 4096 <= optin;
+    if (flags & SDIM_FLAG_CLUSTER_XZ) return cl_smem && !force_gmem ? 3 : 4;
     if (force_gmem) return 2;
     if (pair && (flags & SDIM_FLAG_SPLIT_XZ)) return 1;
-    return single ? 0 : pair ? 1 : 2;
+    if (single) return 0;
+    if (few) return cl_smem ? 3 : 4;
+    return pair ? 1 : 2;
+  };
+  // clusters of a mode-4 run: one per kTraceClusterCtas SMs, each CTA alone
+  // on its SM, so the programs in flight keep their columns in L2
+  auto stream_clusters = [&](size_t programs) {
+    return std::min<size_t>(programs, (size_t)std::max(1, ctx->num_sms / kTraceClusterCtas));
   };
   // runs of programs with one (variant, mode); with several runs each goes
   // on its own stream so that one run's tail overlaps the next run
@@ -534,6 +550,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     if (mode == 2) {
       const size_t grid = std::min<size_t>(e - b, 2 * (size_t)ctx->num_sms);
       slot_total += trace_u8_xz_bytes(hu[b].c.n) * grid;
+    } else if (mode == 4) {
+      slot_total += trace_u8_cluster_xz(hu[b].c.n) * kTraceClusterCtas * stream_clusters(e - b);
     }
     b = e;
   }
@@ -560,6 +578,15 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     if (mode == 1) {
       launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax) + win,
                             trace_u8_split_smem(nmax), rs, du + b, (int)(e - b), status);
+    } else if (mode >= 3) {
+      const bool in_smem = mode == 3;
+      const size_t hot = trace_u8_cluster_hot(nmax), xz = trace_u8_cluster_xz(nmax);
+      size_t smem = hot + (in_smem ? xz : 0) + win;
+      // streamed columns: more than half an SM's shared memory keeps one CTA per SM
+      if (!in_smem) smem = std::max(smem, (size_t)ctx->smem_per_sm / 2);
+      const size_t clusters = in_smem ? std::min<size_t>(e - b, 65535 / kTraceClusterCtas) : stream_clusters(e - b);
+      launch_trace_u8_cluster(v, (int)clusters, smem, rs, du + b, (int)(e - b),
+                              static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, status);
     } else {
       const size_t hot = trace_u8_hot_bytes(nmax), xz = trace_u8_xz_bytes(nmax);
       const bool in_smem = mode == 0;
@@ -735,6 +762,32 @@ __global__ void __launch_bounds__(1024) k_smem_probe(int iters, uint4* sink) {
     idx += blockDim.x + 1;
   }
   if ((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9e3779b9u) sink[blockIdx.x] = acc;
+}
+
+// L2 read-write bandwidth probe: every pass reads and rewrites each 16-byte
+// word of a buffer that fits in L2, as the rank-1 update of columns held in
+// L2 does; four words in flight per thread.
+__global__ void __launch_bounds__(512) k_l2_probe(uint4* buf, size_t words, int passes) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int p = 0; p < passes; ++p) {
+    size_t i = t0;
+    for (; i + 3 * stride < words; i += 4 * stride) {
+      uint4 v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = buf[i + j * stride];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        v[j].x ^= 1u;
+        buf[i + j * stride] = v[j];
+      }
+    }
+    for (; i < words; i += stride) {
+      uint4 v = buf[i];
+      v.x ^= 1u;
+      buf[i] = v;
+    }
+  }
 }
 
 // Op-table rows (gate id, qudit, target, channel) -> device instruction
@@ -979,6 +1032,28 @@ int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   *gbs = (double)blocks * threads * iters * 16.0 / (ms * 1e-3) / 1e9;
+  return SDIM_OK;
+}
+
+int sdim_probe_l2_bandwidth(sdim_ctx* ctx, double* gbs) {
+  if (!ctx || !gbs) return fail(ctx, SDIM_EINVAL, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  const size_t bytes = (size_t)48 << 20;  // well inside the 129 MB L2
+  int rc = ensure(ctx, ctx->snap, bytes);
+  if (rc != SDIM_OK) return rc;
+  uint4* buf = static_cast<uint4*>(ctx->snap.p);
+  const size_t words = bytes / sizeof(uint4);
+  const int blocks = 2 * ctx->num_sms, threads = 512, passes = 40;
+  CK(cudaMemsetAsync(buf, 0, bytes, ctx->stream));
+  k_l2_probe<<<blocks, threads, 0, ctx->stream>>>(buf, words, 2);  // warm-up: the buffer into L2
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  k_l2_probe<<<blocks, threads, 0, ctx->stream>>>(buf, words, passes);
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *gbs = 2.0 * (double)bytes * passes / (ms * 1e-3) / 1e9;
   return SDIM_OK;
 }
 

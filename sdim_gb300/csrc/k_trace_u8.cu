@@ -2,7 +2,7 @@
 // program, TGroupU8 team with no live shots) and the phase pass (one CTA
 // per 32-shot group, (shot, chunk) threads).  Instantiated for d = 3, 5, 7
 // and a generic d.
-#include "trace_split_u8.cuh"
+#include "trace_cluster_u8.cuh"
 #include "variants.cuh"
 
 namespace sdim {
@@ -50,10 +50,30 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTracePassThreads)
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int red[40];
   uint2* win = reinterpret_cast<uint2*>(smem + win_off);
+  cluster_sync_all();  // both CTAs run before either writes into the other's shared memory
   for (int i = (int)(blockIdx.x >> 1); i < ndesc; i += (int)(gridDim.x >> 1)) {
     const TraceDescU8 td = descs[i];
     SplitU8<DD> e(smem, td.c.n, td.c.d, red);
     split_program(td, e, win, status);
+  }
+}
+
+// One program per cluster of kTraceClusterCtas CTAs (grid-stride over programs,
+// largest first).  kStream: each CTA's columns in its slot of gxz, else in
+// its shared memory after the hot region.
+template <int DD, bool kStream>
+__global__ void __cluster_dims__(kTraceClusterCtas, 1, 1) __launch_bounds__(kTracePassThreads)
+    k_trace_pass_cluster(const TraceDescU8* __restrict__ descs, int ndesc, uint8_t* gxz, size_t xz_bytes,
+                         size_t hot_bytes, int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int red[40];
+  uint8_t* xz = kStream ? gxz + (size_t)blockIdx.x * xz_bytes : smem + hot_bytes;
+  uint2* win = reinterpret_cast<uint2*>(smem + hot_bytes + (kStream ? 0 : xz_bytes));
+  cluster_sync_all();  // every CTA of the cluster runs before any writes into its shared memory
+  for (int i = (int)(blockIdx.x / kTraceClusterCtas); i < ndesc; i += (int)(gridDim.x / kTraceClusterCtas)) {
+    const TraceDescU8 td = descs[i];
+    ClusterU8<DD, kTraceClusterCtas, kStream> e(smem, xz, td.c.n, td.c.d, red);
+    cluster_program(td, e, win, status);
   }
 }
 
@@ -73,7 +93,17 @@ struct TraceU8 {
   static cudaError_t set_smem(int optin) {
     cudaError_t e = set_dynamic_smem(k_trace_pass_u8<DD>, optin);
     if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_split<DD>, optin);
+    if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_cluster<DD, false>, optin);
+    if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_cluster<DD, true>, optin);
     return e != cudaSuccess ? e : set_dynamic_smem(k_phase_pass_u8<DD>, optin);
+  }
+  static void cluster(int clusters, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
+                      size_t xzb, size_t hot, int in_smem, int* status) {
+    const int grid = kTraceClusterCtas * clusters;
+    if (in_smem)
+      k_trace_pass_cluster<DD, false><<<grid, kTracePassThreads, smem, s>>>(d, nd, gxz, xzb, hot, status);
+    else
+      k_trace_pass_cluster<DD, true><<<grid, kTracePassThreads, smem, s>>>(d, nd, gxz, xzb, hot, status);
   }
   static void split(int pairs, size_t smem, size_t scratch_off, cudaStream_t s, const TraceDescU8* d, int nd,
                     int* status) {
@@ -106,6 +136,18 @@ size_t trace_u8_xz_bytes(int n) { return round16(SlotGroupU8::xz_bytes(n)); }
 size_t trace_u8_phase_smem(int n) { return round16(phase_u8_smem(n)); }
 size_t trace_u8_split_smem(int n) { return round16(split_smem_bytes(n)); }
 size_t trace_u8_window_bytes() { return sizeof(uint2) * kOpWindow; }
+size_t trace_u8_cluster_hot(int n) { return round16(cluster_hot_bytes(n, kTraceClusterCtas)); }
+size_t trace_u8_cluster_xz(int n) { return round16(cluster_xz_bytes(n, kTraceClusterCtas)); }
+
+void launch_trace_u8_cluster(int variant, int clusters, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+                             uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status) {
+  switch (variant) {
+    case 0: TraceU8<3>::cluster(clusters, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 1: TraceU8<5>::cluster(clusters, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    case 2: TraceU8<7>::cluster(clusters, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+    default: TraceU8<0>::cluster(clusters, smem, s, d, nd, gxz, xzb, hot, in_smem, status); break;
+  }
+}
 
 void launch_trace_u8_split(int variant, int pairs, size_t smem, size_t scratch_off, cudaStream_t s,
                            const TraceDescU8* d, int nd, int* status) {

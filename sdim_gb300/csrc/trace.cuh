@@ -185,6 +185,15 @@ size_t trace_u8_split_smem(int n);
 size_t trace_u8_window_bytes();
 void launch_trace_u8_split(int variant, int pairs, size_t smem, size_t scratch_off, cudaStream_t s,
                            const TraceDescU8* d, int nd, int* status);
+// x / z pass on clusters of kTraceClusterCtas CTAs (trace_cluster_u8.cuh).
+// Each CTA holds trace_u8_cluster_xz(n) bytes of columns: in its shared
+// memory after trace_u8_cluster_hot(nmax) bytes (in_smem), else at gxz +
+// blockIdx.x * xzb; the instruction window follows in shared memory.
+constexpr int kTraceClusterCtas = 8;
+size_t trace_u8_cluster_hot(int n);
+size_t trace_u8_cluster_xz(int n);
+void launch_trace_u8_cluster(int variant, int clusters, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
+                             uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status);
 void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
                            int nd, long long total, int* status);
 

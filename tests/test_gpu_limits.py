@@ -1,8 +1,9 @@
 """GPU: the largest programs each engine takes, against the oracle and the
 other engines.  Each program is 2n random {H, P, CNOT} gates, a MEASURE+RESET
 sweep and MEASURE on every 32nd qudit, so the oracle stays quick at n = 2048:
-- n = 2048 is the odd-d trace engine's limit, with the x/z tableau streamed
-  from global memory, and beyond the d = 2 trace engine's 512;
+- n = 2048 is the odd-d trace engine's limit, with the x/z columns of a
+  lone program streamed from global memory by a cluster of 8 CTAs, and
+  beyond the d = 2 trace engine's 512;
 - n = 2049 sends odd d back to the shot-group engine."""
 import numpy as np
 import pytest
