@@ -151,6 +151,17 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
                     const double* noise_prob, const int32_t* n, const int32_t* d, const uint64_t* seeds,
                     const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs, void* stream,
                     unsigned flags);
+/* The form the odd-d trace engine's x / z pass takes for a program of n
+ * qudits in a run with odd_trace_programs odd-d trace programs, on a device
+ * with smem_optin bytes of opt-in shared memory per block and num_sms SMs:
+ * 0 one CTA, tableau in shared memory; 1 a CTA pair; 2 one CTA, tableau in
+ * global memory; 3 a cluster of 8 CTAs, columns in shared memory; 4 the
+ * cluster, columns in global memory.  Host-only (no device is touched), so
+ * callers such as a roofline model can mirror the library's routing.
+ * SDIM_EINVAL for n outside [1, 2048] or non-positive sizes.  No
+ * counterpart in the reference. */
+int sdim_trace_xz_mode(int32_t n, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
+                       int32_t num_sms);
 /* Measured shared-memory read bandwidth of the device in GB/s (all SMs):
  * the roofline denominator for tableaux resident in shared memory.  No
  * counterpart in the reference (which has no device code). */

@@ -74,6 +74,7 @@ SIGNATURES = {
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_probe_l2_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "sdim_trace_xz_mode": (C.c_int, [C.c_int32, C.c_int64, C.c_uint, C.c_int32, C.c_int32]),
     "sdim_probe_philox_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_run_noalloc": (C.c_int, [_P, C.c_int64, _P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_int64, _P,
                                    _P, C.c_char_p, C.c_size_t]),

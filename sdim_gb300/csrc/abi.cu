@@ -311,6 +311,31 @@ bool use_trace(const Job& j, unsigned flags) {
 constexpr int kTraceU8MaxQudits = 2048;
 
 // Jobs for the odd-d trace engine: same rule with d odd.
+// The odd-d x / z pass form of a program of n qudits in a run with
+// `programs` odd-d trace programs: 0, one CTA with the tableau in shared
+// memory when it fits.  Otherwise, in a batch with programs enough to fill
+// the SMs (num_sms / 2 or more), for throughput: 1, a CTA pair splitting the
+// generator columns (trace_split_u8.cuh) when that fits, else 2, one CTA
+// with the tableau in global memory.  In a smaller batch, for latency: a
+// cluster of kTraceClusterCtas CTAs (trace_cluster_u8.cuh) with its columns
+// in shared memory (3) or global memory (4).  A cluster shares each
+// measurement's fixed cost (two cluster barriers, pivot search, broadcast)
+// among 8 SMs, so it finishes one program sooner but a full batch later.
+int odd_xz_mode(int n, long long programs, unsigned flags, size_t optin, int num_sms) {
+  const size_t win = trace_u8_window_bytes();
+  const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
+  const bool few = programs * 2 < (long long)num_sms;
+  const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
+  const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
+  const bool cl_smem = trace_u8_cluster_hot(n) + trace_u8_cluster_xz(n) + win + 4096 <= optin;
+  if (flags & SDIM_FLAG_CLUSTER_XZ) return cl_smem && !force_gmem ? 3 : 4;
+  if (force_gmem) return 2;
+  if (pair && (flags & SDIM_FLAG_SPLIT_XZ)) return 1;
+  if (single) return 0;
+  if (few) return cl_smem ? 3 : 4;
+  return pair ? 1 : 2;
+}
+
 bool use_trace_u8(const Job& j, unsigned flags) {
   if (flags & (SDIM_FLAG_PLAIN | SDIM_FLAG_PER_SHOT | SDIM_FLAG_TEAM_WARP | SDIM_FLAG_TEAM_CTA |
                SDIM_FLAG_NO_TRACE))
@@ -508,29 +533,10 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
   }
-  // odd d, by mode: 0, one CTA with the tableau in shared memory when it
-  // fits.  Otherwise, in a batch with programs enough to fill the SMs (76 or
-  // more), for throughput: 1, a CTA pair splitting the generator columns
-  // (trace_split_u8.cuh) when that fits, else 2, one CTA with the tableau in
-  // global memory.  In a smaller batch, for latency: a cluster of
-  // kTraceClusterCtas CTAs (trace_cluster_u8.cuh) with its columns in shared
-  // memory (3) or global memory (4).  A cluster shares each measurement's
-  // fixed cost (two cluster barriers, pivot search, broadcast) among 8 SMs,
-  // so it finishes one program sooner but a full batch later.
+  // odd d: the x / z pass form of each program (odd_xz_mode)
   const size_t optin = (size_t)ctx->smem_optin;
   const size_t win = trace_u8_window_bytes();
-  const bool few = ku * 2 < (size_t)ctx->num_sms;
-  auto xz_mode = [&](int n) {
-    const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
-    const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
-    const bool cl_smem = trace_u8_cluster_hot(n) + trace_u8_cluster_xz(n) + win + 4096 <= optin;
-    if (flags & SDIM_FLAG_CLUSTER_XZ) return cl_smem && !force_gmem ? 3 : 4;
-    if (force_gmem) return 2;
-    if (pair && (flags & SDIM_FLAG_SPLIT_XZ)) return 1;
-    if (single) return 0;
-    if (few) return cl_smem ? 3 : 4;
-    return pair ? 1 : 2;
-  };
+  auto xz_mode = [&](int n) { return odd_xz_mode(n, (long long)ku, flags, optin, ctx->num_sms); };
   // clusters of a mode-4 run: one per kTraceClusterCtas SMs, each CTA alone
   // on its SM, so the programs in flight keep their columns in L2
   auto stream_clusters = [&](size_t programs) {
@@ -1015,6 +1021,13 @@ void append_frame_ops(const int32_t* ops, int64_t nops, const double* noise_prob
 }  // namespace
 
 extern "C" {
+
+int sdim_trace_xz_mode(int32_t n, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
+                       int32_t num_sms) {
+  if (n < 1 || n > kTraceU8MaxQudits || odd_trace_programs < 0 || smem_optin <= 0 || num_sms <= 0)
+    return SDIM_EINVAL;
+  return odd_xz_mode(n, (long long)odd_trace_programs, flags, (size_t)smem_optin, num_sms);
+}
 
 int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs) {
   if (!ctx || !gbs) return fail(ctx, SDIM_EINVAL, "null argument");

@@ -76,7 +76,7 @@ def test_large_programs_every_odd_d_pass(n, d):
 def test_mixed_batch_routes_every_mode(large):
     """Default routing in one run, against each program alone on the
     shot-group engine.  Fewer than 76 odd-d trace programs: one CTA
-    (n <= 223), clusters in shared memory and streamed clusters.  76 or
+    (n <= 226), clusters in shared memory and streamed clusters.  76 or
     more: one CTA, CTA pairs and single CTAs streaming from global memory."""
     sizes = [(40, 3), (300, 5), (500, 7), (700, 3), (260, 7), (190, 5), (800, 5), (331, 3)]
     if large:
