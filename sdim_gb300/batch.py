@@ -61,16 +61,25 @@ class BatchRunner:
 
     def run(self, plain: bool = False, per_shot: bool = False, time_kernels: bool = False,
             entries: Optional[Sequence[BatchEntry]] = None,
-            outs: Optional[Sequence[np.ndarray]] = None, engine: Optional[str] = None) -> List[np.ndarray]:
+            outs: Optional[Sequence[np.ndarray]] = None, engine: Optional[str] = None,
+            flags: int = 0) -> List[np.ndarray]:
         """Runs every entry; returns one (shots, records) uint8 array each
-        (into ``outs`` when given, e.g. views of a pinned buffer)."""
+        (into ``outs`` when given, e.g. views of a pinned buffer).
+
+        ``engine="tuned"`` runs the route the autotuner picked for this
+        batch's composition (timing the routes on the first call);
+        ``flags`` adds raw SDIM_FLAG_* route flags."""
         entries = list(self.entries if entries is None else entries)
+        if engine == "tuned":
+            from .autotune import default_tuner
+            flags |= default_tuner(self.ctx).flags_for_batch(BatchRunner._view(self.ctx, entries))
+            engine = None
         if outs is None:
             outs = [np.empty((e.shots, e.program.num_records), dtype=np.uint8) for e in entries]
         ptrs = (C.c_void_p * len(entries))(*[o.ctypes.data for o in outs])
         circs, seeds, shot0, nshots = self._arrays(entries)
         rc = self.ctx.lib.sdim_run_batch(self.ctx.ptr, len(entries), circs, seeds, shot0, nshots, ptrs, None,
-                                         self._flags(plain, per_shot, time_kernels, engine=engine))
+                                         self._flags(plain, per_shot, time_kernels, engine=engine) | int(flags))
         _lib.check(rc, self.ctx.ptr, "batch")
         return list(outs)
 
@@ -85,6 +94,12 @@ class BatchRunner:
                                          C.c_void_p(stream) if stream else None,
                                          self._flags(plain, per_shot, time_kernels, asynchronous, True, engine))
         _lib.check(rc, self.ctx.ptr, "batch")
+
+    @staticmethod
+    def _view(ctx, entries) -> "BatchRunner":
+        r = BatchRunner(ctx)
+        r.entries = list(entries)
+        return r
 
     def total_shots(self) -> int:
         return sum(e.shots for e in self.entries)

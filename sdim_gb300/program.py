@@ -133,13 +133,20 @@ class Program:
 
         ``engine`` picks the batched engine: None (by shot count and d),
         "trace" (d = 2: one x / z pass, one lane per shot), "group" (32-shot
-        groups), "per_shot" (one warp per shot; same as ``per_shot=True``)."""
+        groups), "per_shot" (one warp per shot; same as ``per_shot=True``),
+        "tuned" (the route the autotuner timed fastest for this program's
+        class of d, n and shots; the first call of a class times them)."""
         dp = self.compile(noise)
         s = self._seed(seed)
         if out is None:
             out = np.empty((int(shots), dp.num_records), dtype=np.uint8)
         flags = (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_PER_SHOT if per_shot else 0)
-        flags |= _lib.engine_flags(engine)
+        if engine == "tuned":
+            from .autotune import default_tuner
+            if shots > 0:
+                flags |= default_tuner(self.context).flags_for_program(dp, int(shots), noise)
+        else:
+            flags |= _lib.engine_flags(engine)
         if shots > 0 and dp.num_records > 0:
             rc = self.context.lib.sdim_run(self.context.ptr, dp.ptr, s, int(shot0), int(shots),
                                            out.ctypes.data, flags)
