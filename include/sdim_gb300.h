@@ -66,6 +66,7 @@ extern "C" {
 
 typedef struct sdim_ctx sdim_ctx;
 typedef struct sdim_circuit sdim_circuit;
+typedef struct sdim_graph sdim_graph;
 
 /* Context on one CUDA device: stream, device buffers, error string.
  * Replaces the state Program keeps between calls (sdim/program.py:194-204). */
@@ -138,6 +139,31 @@ int sdim_parse_chp(const char* text, int64_t len, int32_t* rows, double* probs, 
 int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, const uint64_t* seeds,
                    const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs, void* stream,
                    unsigned flags);
+/* A batch run captured once into a CUDA graph and replayed: the whole shot
+ * loop of every program (descriptor upload, work-queue resets, the x / z,
+ * coin, phase and shot-group kernels on their streams) is one graph launch.
+ * Arguments as sdim_run_batch with device outputs; the circuits and the
+ * output buffers must outlive the graph.  Creation runs the batch once
+ * uncaptured (which writes its records) to size every buffer, then captures
+ * it on a private context, so no later call on ctx can move memory that the
+ * graph's nodes use.  SDIM_FLAG_PLAIN is refused; TIME and ASYNC are
+ * ignored.  Replaces the reference's Python loop over shots
+ * (sdim/program.py:206-267, 269-365), which has no graph form. */
+int sdim_graph_create(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, const uint64_t* seeds,
+                      const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs_dev, unsigned flags,
+                      sdim_graph** out);
+/* Queues one replay on `stream` (NULL: the graph's own stream).  seeds and
+ * shot0 (each NULL or ncirc entries, batch order) replace the seeds and
+ * first shot indices of the programs for this and later replays; records
+ * equal an sdim_run_batch with the same values.  Replacing them first waits
+ * for the previous replay.  Does not wait for the replay itself. */
+int sdim_graph_launch(sdim_graph* g, const uint64_t* seeds, const int64_t* shot0, void* stream);
+/* Waits for the last replay and reports a device-side error, if any. */
+int sdim_graph_sync(sdim_graph* g);
+/* info[0] graph nodes, info[1] kernel nodes, info[2] pinned descriptor bytes. */
+int sdim_graph_info(const sdim_graph* g, int64_t info[3]);
+const char* sdim_graph_last_error(const sdim_graph* g);
+int sdim_graph_destroy(sdim_graph* g);
 /* Many programs given as op tables, encoded and run in one call: the serving
  * path.  Program i is rows[row_begin[i] .. row_begin[i+1]) (4 int32 per row as
  * in sdim_encode_circuit), noise_prob (may be NULL) is indexed like rows, and

@@ -76,6 +76,12 @@ SIGNATURES = {
     "sdim_probe_l2_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_trace_xz_mode": (C.c_int, [C.c_int32, C.c_int64, C.c_uint, C.c_int32, C.c_int32]),
     "sdim_probe_philox_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "sdim_graph_create": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, C.c_uint, C.POINTER(_P)]),
+    "sdim_graph_launch": (C.c_int, [_P, _P, _P, _P]),
+    "sdim_graph_sync": (C.c_int, [_P]),
+    "sdim_graph_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sdim_graph_last_error": (C.c_char_p, [_P]),
+    "sdim_graph_destroy": (C.c_int, [_P]),
     "sdim_run_noalloc": (C.c_int, [_P, C.c_int64, _P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_int64, _P,
                                    _P, C.c_char_p, C.c_size_t]),
 }

@@ -95,6 +95,14 @@ class BatchRunner:
                                          self._flags(plain, per_shot, time_kernels, asynchronous, True, engine))
         _lib.check(rc, self.ctx.ptr, "batch")
 
+    def capture(self, outs_dev: Sequence[int], engine: Optional[str] = None, flags: int = 0,
+                entries: Optional[Sequence[BatchEntry]] = None):
+        """The batch as a CUDA graph (graph.CapturedRun) with device outputs;
+        creating it runs the batch once."""
+        from .graph import CapturedRun
+        entries = list(self.entries if entries is None else entries)
+        return CapturedRun(self.ctx, entries, outs_dev, self._flags(engine=engine) | int(flags))
+
     @staticmethod
     def _view(ctx, entries) -> "BatchRunner":
         r = BatchRunner(ctx)

@@ -5,10 +5,12 @@
 #include <cmath>
 #include <cstdio>
 #include <climits>
+#include <cstddef>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/sdim_gb300.h"
@@ -27,6 +29,20 @@ struct DevBuf {
 };
 
 }  // namespace
+
+// Descriptor staging of a run captured into a CUDA graph (sdim_graph_create).
+// In the uncaptured first run (sizing) the descriptor uploads only add up
+// their bytes.  In the captured run each descriptor array is copied into
+// pinned host memory that the graph's copy node reads at every replay, and
+// the byte offsets of every descriptor's seed and shot0 are noted with the
+// batch index of its job, for sdim_graph_launch to rewrite.
+struct GraphCapture {
+  bool sizing = true;
+  size_t need = 0;
+  uint8_t* host = nullptr;
+  size_t cap = 0, used = 0;
+  std::vector<std::pair<size_t, int>> seed_at, shot0_at;  // (offset in host, job index)
+};
 
 struct sdim_ctx {
   int device = 0;
@@ -59,6 +75,20 @@ struct sdim_ctx {
   bool trace_smem_set = false;
   bool frame_smem_set = false;
   int trace_threads = kTracePassThreads;  // x / z pass CTA size (SDIM_TRACE_PASS_THREADS: 256 or 512)
+  GraphCapture* capture = nullptr;  // set while sdim_graph_create runs on its private context
+  unsigned long long reallocs = 0;  // device buffers moved by ensure()
+};
+
+// A batch run captured into a CUDA graph.  It owns a private context, so the
+// device buffers its nodes point into move only when the graph is destroyed.
+struct sdim_graph {
+  sdim_ctx* own = nullptr;
+  GraphCapture cap;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t done = nullptr;  // end of the last replay
+  bool launched = false;
+  int njobs = 0;
 };
 
 // Where the trace schedule of a program sits in its blob (uint2 words).
@@ -115,6 +145,7 @@ int ensure(sdim_ctx* ctx, DevBuf& b, size_t bytes) {
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.cap = 0;
+  ++ctx->reallocs;
   cudaError_t e = cudaMalloc(&b.p, cap);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -272,7 +303,34 @@ struct Job {
   uint64_t seed;
   int64_t shot0, nshots;
   uint8_t* out_dev;
+  int index = -1;  // position in the caller's batch (graph capture: whose seed a descriptor holds)
 };
+
+// Host -> device copy of `count` descriptors of `each` bytes, each holding a
+// CircuitDesc at byte `cdesc_off`; job_index(k) is the batch index of
+// descriptor k.  Outside a graph capture this is one cudaMemcpyAsync.
+template <class JobIndex>
+int upload_descs(sdim_ctx* ctx, void* dst, const void* src, size_t each, size_t count, size_t cdesc_off,
+                 JobIndex job_index, cudaStream_t s) {
+  const size_t bytes = each * count;
+  GraphCapture* g = ctx->capture;
+  if (g && !g->sizing) {
+    if (g->used + bytes > g->cap) return fail(ctx, SDIM_ECUDA, "graph descriptor staging overflow");
+    const size_t off = g->used;
+    std::memcpy(g->host + off, src, bytes);
+    g->used += (bytes + 255) & ~(size_t)255;
+    for (size_t k = 0; k < count; ++k) {
+      const size_t base = off + k * each + cdesc_off;
+      g->seed_at.emplace_back(base + offsetof(CircuitDesc, seed), job_index(k));
+      g->shot0_at.emplace_back(base + offsetof(CircuitDesc, shot0), job_index(k));
+    }
+    CK(cudaMemcpyAsync(dst, g->host + off, bytes, cudaMemcpyHostToDevice, s));
+    return SDIM_OK;
+  }
+  if (g) g->need += (bytes + 255) & ~(size_t)255;
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  return SDIM_OK;
+}
 
 // Engine used for a job: the shot-group engine for batched runs (unless
 // SDIM_FLAG_PER_SHOT; SDIM_FLAG_TEAM_* override the team kind), the
@@ -454,7 +512,9 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.wn = (j.c->n + 31) >> 5;
     }
     dd = static_cast<TraceDesc*>(ctx->tdescs.p);
-    CK(cudaMemcpyAsync(dd, hd.data(), sizeof(TraceDesc) * k, cudaMemcpyHostToDevice, s));
+    if ((rc = upload_descs(ctx, dd, hd.data(), sizeof(TraceDesc), k, offsetof(TraceDesc, c),
+                           [&](size_t i) { return jobs[i].index; }, s)) != SDIM_OK)
+      return rc;
   }
   // ---- odd-d descriptors
   std::stable_sort(ujobs.begin(), ujobs.end(), [](const Job& a, const Job& b) {
@@ -504,7 +564,9 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.nn1 = j.c->nn1;
     }
     du = static_cast<TraceDescU8*>(ctx->tdescs_u8.p);
-    CK(cudaMemcpyAsync(du, hu.data(), sizeof(TraceDescU8) * ku, cudaMemcpyHostToDevice, s));
+    if ((rc = upload_descs(ctx, du, hu.data(), sizeof(TraceDescU8), ku, offsetof(TraceDescU8, c),
+                           [&](size_t i) { return ujobs[i].index; }, s)) != SDIM_OK)
+      return rc;
   }
   if (coins) CK(cudaEventRecord(ctx->ev_fork, s));
   // ---- x / z passes: one CTA per program
@@ -721,8 +783,9 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsig
     g.end = (int)k + 1;
   }
   CircuitDesc* ddesc = static_cast<CircuitDesc*>(ctx->descs.p);
-  if (!hd.empty())
-    CK(cudaMemcpyAsync(ddesc, hd.data(), sizeof(CircuitDesc) * hd.size(), cudaMemcpyHostToDevice, s));
+  if (!hd.empty() && (rc = upload_descs(ctx, ddesc, hd.data(), sizeof(CircuitDesc), hd.size(), 0,
+                                        [&](size_t k) { return jobs[order[k]].index; }, s)) != SDIM_OK)
+    return rc;
   CK(cudaMemsetAsync(ctx->status.p, 0, sizeof(int), s));
   CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * V_COUNT, s));
   if (flags & SDIM_FLAG_TIME) CK(cudaEventRecord(ctx->ev0, s));
@@ -1441,6 +1504,144 @@ int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, c
     if (trc != SDIM_OK) return trc;
   }
   return read_status(ctx);
+}
+
+int sdim_graph_create(sdim_ctx* parent, int ncirc, const sdim_circuit* const* circs, const uint64_t* seeds,
+                      const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs_dev, unsigned flags,
+                      sdim_graph** out) {
+  sdim_ctx* ctx = parent;
+  if (!ctx || !out || ncirc < 0 || (ncirc > 0 && (!circs || !seeds || !shot0 || !nshots || !outs_dev)))
+    return fail(ctx, SDIM_EINVAL, "bad argument to sdim_graph_create");
+  *out = nullptr;
+  if (flags & SDIM_FLAG_PLAIN) return fail(ctx, SDIM_EINVAL, "the plain form (one launch per shot) is not captured");
+  std::vector<Job> jobs;
+  jobs.reserve(ncirc);
+  for (int i = 0; i < ncirc; ++i) {
+    if (!circs[i] || nshots[i] < 0 || nshots[i] > 0x7fffffffLL)
+      return fail(ctx, SDIM_EINVAL, "bad circuit or shot count at batch index " + std::to_string(i));
+    if (circs[i]->device != ctx->device)
+      return fail(ctx, SDIM_EINVAL, "circuit at batch index " + std::to_string(i) + " lives on another device");
+    if (nshots[i] > 0 && circs[i]->nmeas > 0 && !outs_dev[i])
+      return fail(ctx, SDIM_EINVAL, "null output at batch index " + std::to_string(i));
+    jobs.push_back(Job{circs[i], seeds[i], shot0[i], nshots[i], outs_dev[i], i});
+  }
+  CK(cudaSetDevice(ctx->device));
+  sdim_graph* g = new sdim_graph();
+  g->njobs = ncirc;
+  int rc = sdim_ctx_create(ctx->device, &g->own);
+  if (rc != SDIM_OK) {
+    delete g;
+    return fail(ctx, rc, "graph: context creation failed");
+  }
+  auto bail = [&](int code) {
+    const std::string why = "graph: " + g->own->err;
+    g->own->capture = nullptr;
+    sdim_graph_destroy(g);
+    return fail(parent, code, why);
+  };
+  ctx = g->own;
+  const unsigned f = (flags & ~(SDIM_FLAG_TIME | SDIM_FLAG_ASYNC)) | SDIM_FLAG_OUT_DEVICE;
+  // 1. the run, uncaptured: checks the programs, sizes every device buffer
+  //    and the descriptor staging, sets the kernels' shared-memory limits
+  ctx->capture = &g->cap;
+  rc = launch_jobs(ctx, jobs, ctx->stream, f);
+  if (rc == SDIM_OK) rc = finish(ctx, ctx->stream, f);
+  if (rc != SDIM_OK) return bail(rc);
+  if (g->cap.need) {
+    void* h = nullptr;
+    if (cudaMallocHost(&h, g->cap.need) != cudaSuccess) {
+      cudaGetLastError();
+      fail(ctx, SDIM_ENOMEM, "pinned descriptor staging");
+      return bail(SDIM_ENOMEM);
+    }
+    g->cap.host = static_cast<uint8_t*>(h);
+    g->cap.cap = g->cap.need;
+  }
+  g->cap.sizing = false;
+  // 2. the same run, captured: buffers are already large enough, so nothing
+  //    is allocated and every node points at memory that stays put
+  const unsigned long long moved = ctx->reallocs;
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaStreamBeginCapture"));
+  rc = launch_jobs(ctx, jobs, ctx->stream, f);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  ctx->capture = nullptr;
+  g->graph = graph;
+  if (rc != SDIM_OK) return bail(rc);
+  if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaStreamEndCapture"));
+  if (ctx->reallocs != moved) {
+    fail(ctx, SDIM_ECUDA, "a device buffer moved during capture");
+    return bail(SDIM_ECUDA);
+  }
+  e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaGraphInstantiate"));
+  *out = g;
+  return SDIM_OK;
+}
+
+int sdim_graph_launch(sdim_graph* g, const uint64_t* seeds, const int64_t* shot0, void* stream) {
+  if (!g || !g->exec) return SDIM_EINVAL;
+  sdim_ctx* ctx = g->own;
+  CK(cudaSetDevice(ctx->device));
+  if (seeds || shot0) {
+    // the last replay's copy node may not have read the staging yet
+    if (g->launched) CK(cudaEventSynchronize(g->done));
+    if (seeds)
+      for (const auto& a : g->cap.seed_at) std::memcpy(g->cap.host + a.first, &seeds[a.second], sizeof(uint64_t));
+    if (shot0)
+      for (const auto& a : g->cap.shot0_at) std::memcpy(g->cap.host + a.first, &shot0[a.second], sizeof(int64_t));
+  }
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  CK(cudaGraphLaunch(g->exec, s));
+  CK(cudaEventRecord(g->done, s));
+  g->launched = true;
+  return SDIM_OK;
+}
+
+int sdim_graph_sync(sdim_graph* g) {
+  if (!g) return SDIM_EINVAL;
+  sdim_ctx* ctx = g->own;
+  CK(cudaSetDevice(ctx->device));
+  if (!g->launched) return SDIM_OK;
+  CK(cudaEventSynchronize(g->done));
+  return read_status(ctx);
+}
+
+int sdim_graph_info(const sdim_graph* g, int64_t info[3]) {
+  if (!g || !info || !g->graph) return SDIM_EINVAL;
+  size_t count = 0;
+  if (cudaGraphGetNodes(g->graph, nullptr, &count) != cudaSuccess) return SDIM_ECUDA;
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (count && cudaGraphGetNodes(g->graph, nodes.data(), &count) != cudaSuccess) return SDIM_ECUDA;
+  int64_t kernels = 0;
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) != cudaSuccess) return SDIM_ECUDA;
+    kernels += t == cudaGraphNodeTypeKernel;
+  }
+  info[0] = (int64_t)count;
+  info[1] = kernels;
+  info[2] = (int64_t)g->cap.cap;
+  return SDIM_OK;
+}
+
+const char* sdim_graph_last_error(const sdim_graph* g) { return g ? g->own->err.c_str() : "null graph"; }
+
+int sdim_graph_destroy(sdim_graph* g) {
+  if (!g) return SDIM_EINVAL;
+  if (g->own) {
+    cudaSetDevice(g->own->device);
+    if (g->launched) cudaEventSynchronize(g->done);
+  }
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->done) cudaEventDestroy(g->done);
+  if (g->cap.host) cudaFreeHost(g->cap.host);
+  if (g->own) sdim_ctx_destroy(g->own);
+  delete g;
+  return SDIM_OK;
 }
 
 int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t* row_begin,
