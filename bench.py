@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--circuits", type=int, default=8192, help="programs of the uneven batch")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="uneven batch: also time the autotuner's batch-wide routes")
     ap.add_argument("--plain-shots", type=int, default=256)
     ap.add_argument("--quick", action="store_true",
                     help="single-program workloads: time the selected engine only (for profiling runs)")
@@ -464,6 +466,50 @@ class Timer:
         return float(t.item())
 
 
+def graph_replay(args, torch, ctx, timer, stream, entries, units_per_step, expect):
+    """The same step captured once as a CUDA graph (sdim_graph_create) and
+    replayed over fresh shot ranges: every replay moves each program's
+    first shot on by its shot count, as a sampling loop does.  CUDA events
+    on the launching stream around each replay, L2 flushed in between; the
+    step's records are checked against the ordinary run (``expect``: the
+    device output of a replay at the original shot ranges)."""
+    from sdim_gb300.graph import CapturedRun
+    sizes = [e.shots * e.program.num_records for e in entries]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    gout = torch.empty(int(offs[-1]) + 1, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    run = CapturedRun(ctx, entries, [gout.data_ptr() + int(o) for o in offs[:-1]])
+    try:
+        info = run.info()
+
+        def moved(k):
+            return [e.shot0 + k * e.shots for e in entries]
+
+        for k in range(args.warmup):
+            run.launch(shot0=moved(k + 1), stream=stream.cuda_stream)
+        run.sync()
+        ms = []
+        for k in range(args.steps):
+            timer.flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run.launch(shot0=moved(args.warmup + 1 + k), stream=stream.cuda_stream)
+            e1.record(stream)
+            run.sync()
+            ms.append(e0.elapsed_time(e1))
+        run.launch(shot0=moved(0), stream=stream.cuda_stream)
+        run.sync()
+        if not np.array_equal(gout[:-1].cpu().numpy(), expect()):
+            raise AssertionError("graph replay records differ from the ordinary run")
+    finally:
+        run.close()
+    return {"value": units_per_step * args.steps / (sum(ms) / 1e3), "unit": UNIT,
+            "ms_per_step": statistics.mean(ms),
+            "form": "the step as one CUDA graph (descriptor upload, queue resets, every kernel on its stream), "
+                    "new shot offsets written into its pinned descriptors before each replay",
+            "graph_nodes": info["nodes"], "kernel_nodes": info["kernel_nodes"]}
+
+
 def frame_route(args, torch, ctx, prog, dp, spec, shots, timer):
     """The reference's multi-shot route (Program.simulate(shots) without
     force_tableau): noiseless tableau shot 0, Pauli frames for the rest, on
@@ -614,6 +660,11 @@ def run_single(args, torch, dist, ws, rank, local):
         step()
         ctx.sync()
     frames = frame_route(args, torch, ctx, prog, dp, spec, shots, timer) if rank == 0 else None
+    graph = None
+    if rank == 0:
+        from sdim_gb300.batch import BatchEntry
+        graph = graph_replay(args, torch, ctx, timer, stream, [BatchEntry(dp, shots, 0, shot0)],
+                             len(spec.ops) * shots, lambda: full.reshape(-1))
     det_row = (rec[0] >> 7).astype(bool) if nrec else np.zeros(0, bool)
     assert np.all((rec >> 7) == (rec[0] >> 7)), "deterministic flags differ across shots"
     meas_ids = [g for g in enc.ops[:, 0].tolist() if g in (14, 15, 16)]
@@ -749,6 +800,7 @@ def run_single(args, torch, dist, ws, rank, local):
         "stages_ms": {"xz_pass": stages[0], "phase_pass": stages[1], "other_engines": stages[2]},
         "engines": engines,
         "frame_sampler": frames,
+        "graph_replay": graph,
     }
 
 
@@ -789,6 +841,17 @@ def run_uneven(args, torch, dist, ws, rank, local):
     ps_step_ms, ps_kern_ms, _ = timer.run(1, lambda: step(_lib.FLAG_PER_SHOT))
     if not np.array_equal(out.cpu().numpy(), ref_out):
         raise AssertionError("shot-group and per-shot engines disagree on the uneven batch")
+    graph = graph_replay(args, torch, ctx, timer, stream, entries, units_per_step,
+                         lambda: ref_out[:-1]) if rank == 0 else None
+    tuned = None
+    if rank == 0 and args.autotune:
+        # the autotuner over the batch-wide routes (records checked equal to
+        # the default route's; kernel time by the library's CUDA events)
+        from sdim_gb300.autotune import Autotuner
+        res = Autotuner(ctx, reps=2).tune_batch(br)
+        tuned = {"best": res.best.name, "flags": res.best.flags, "kernel_ms": res.times_ms,
+                 "aborted_after_one_run": res.aborted,
+                 "value": units_per_step / (res.times_ms[res.best.name] / 1e3), "unit": UNIT}
 
     # algorithmic bytes: det flags per program from its first shot.  The x / z
     # tableau is updated once per program on the trace engines and once per
@@ -883,6 +946,8 @@ def run_uneven(args, torch, dist, ws, rank, local):
         # one persistent launch per (dimension, team kind) present in the batch
         "gpu_launches": args.steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),
         "clocks": clk,
+        "graph_replay": graph,
+        "autotune": tuned,
     }
 
 
