@@ -51,6 +51,7 @@ class Request:
     done: float = 0.0
     records: Optional[np.ndarray] = None
     error: Optional[str] = None
+    solo: bool = False         # run alone: its batch was refused, so each request is retried by itself
     event: threading.Event = field(default_factory=threading.Event)
 
     def wait(self, timeout: Optional[float] = None) -> np.ndarray:
@@ -91,8 +92,8 @@ class _PinnedBuffer:
 
 
 class _Lane:
-    def __init__(self, device: int):
-        self.ctx = _lib.Context(device)
+    def __init__(self, device: int, context=_lib.Context):
+        self.ctx = context(device)
         self.buf = _PinnedBuffer(self.ctx.lib)
         self.requests: List[Request] = []
         self.offsets: List[int] = []
@@ -102,8 +103,9 @@ class _Lane:
 
 class Server:
     def __init__(self, device: int = 0, lanes: int = 4, max_batch_requests: int = 1024,
-                 max_batch_shots: int = 1 << 20, memory_fraction: float = 0.5):
-        self.lanes = [_Lane(device) for _ in range(max(1, lanes))]
+                 max_batch_shots: int = 1 << 20, memory_fraction: float = 0.5, context=_lib.Context):
+        # context: the class that opens a lane's library context (a test passes a fake)
+        self.lanes = [_Lane(device, context) for _ in range(max(1, lanes))]
         self.max_batch_requests = max_batch_requests
         self.max_batch_shots = max_batch_shots
         info = (C.c_int64 * 3)()
@@ -168,13 +170,17 @@ class Server:
         # device records + a generous bound on slots and instruction arena
         return 2 * req.shots * max(req.nmeas, 1) + 64 * req.table.shape[0] + 8 * req.n * req.n
 
-    def _retire(self, lane: _Lane):
+    def _error_text(self, lane: _Lane, rc: int) -> str:
+        raw = lane.ctx.lib.sdim_last_error(lane.ctx.ptr)
+        return (raw.decode() if raw else "") or f"status {rc}"
+
+    def _retire(self, lane: _Lane, err: Optional[str] = None):
+        """Hands the lane's records to its requests.  ``err``: the batch
+        failed before it reached the device (its records were never written)."""
         rc = lane.ctx.lib.sdim_sync(lane.ctx.ptr)
         now = time.perf_counter()
-        err = None
-        if rc != 0:
-            raw = lane.ctx.lib.sdim_last_error(lane.ctx.ptr)
-            err = (raw.decode() if raw else "") or f"status {rc}"
+        if err is None and rc != 0:
+            err = self._error_text(lane, rc)
         for req, off in zip(lane.requests, lane.offsets):
             if err is None:
                 nb = req.shots * req.nmeas
@@ -189,6 +195,30 @@ class Server:
             lane.requests, lane.offsets, lane.busy = [], [], False
 
     def _launch(self, lane: _Lane, batch: List[Request]):
+        """Launches a batch on a free lane.  A batch that the library refuses
+        (one request with a bad gate, qudit or dimension fails the whole call)
+        goes back to the head of the queue with every request marked to run
+        alone, so only the bad request fails."""
+        try:
+            rc = self._start(lane, batch)
+        except Exception as exc:  # the scheduler thread must outlive any one batch
+            lane.requests, lane.offsets, lane.busy = batch, [0] * len(batch), True
+            self._retire(lane, f"{type(exc).__name__}: {exc}")
+            return
+        if rc == 0:
+            return
+        err = self._error_text(lane, rc)
+        if len(batch) > 1:
+            with self._lock:
+                self.mem_in_use -= sum(self._cost(r) for r in batch)
+                for r in reversed(batch):
+                    r.solo = True
+                    self._pending.appendleft(r)
+                lane.requests, lane.offsets, lane.busy = [], [], False
+            return
+        self._retire(lane, err)
+
+    def _start(self, lane: _Lane, batch: List[Request]) -> int:
         k = len(batch)
         rows = np.concatenate([r.table for r in batch], axis=0)
         row_begin = np.zeros(k + 1, dtype=np.int64)
@@ -217,15 +247,15 @@ class Server:
                                           probs.ctypes.data if probs is not None else None, ns.ctypes.data,
                                           ds.ctypes.data, seeds, shot0, nshots, outs, None, _lib.FLAG_ASYNC)
         self.batches += 1
-        if rc != 0:
-            self._retire(lane)
+        return rc
 
     def _admit(self) -> List[Request]:
         batch, shots = [], 0
         while self._pending and len(batch) < self.max_batch_requests:
             req = self._pending[0]
             cost = self._cost(req)
-            if batch and (shots + req.shots > self.max_batch_shots or self.mem_in_use + cost > self.mem_budget):
+            if batch and (req.solo or batch[0].solo or shots + req.shots > self.max_batch_shots
+                          or self.mem_in_use + cost > self.mem_budget):
                 break
             if not batch and self.mem_in_use + cost > self.mem_budget and any(l.busy for l in self.lanes):
                 break  # wait for memory to free up
@@ -245,7 +275,9 @@ class Server:
                     return
                 free = [l for l in self.lanes if not l.busy]
                 batch = self._admit() if (free and self._pending) else []
-                if not batch and not any(l.busy for l in self.lanes):
+                if batch:
+                    free[0].busy = True  # under the lock: drain() never sees the batch in neither place
+                elif not any(l.busy for l in self.lanes):
                     self._wake.wait(timeout=0.01)
                     continue
             if batch:
