@@ -29,7 +29,12 @@ With ``--frames`` it drives the reference's multi-shot route instead
 with ``np.random`` answered from the same Philox stream) and writes
 ``frames.json`` / ``frames.npz``; with ``--chp`` it runs the reference's
 .chp reader and writer (sdim/circuit_io.py:6-139) on corner-case texts and
-on circuits it writes itself, and writes ``chp.json``.
+on circuits it writes itself, and writes ``chp.json``.  With ``--stats``
+it runs the reference's ``Program.simulate(shots)`` with its own random
+number generators (seeded ``random`` and ``np.random``, no injection) on the
+circuits of ``stat_cases`` and writes the outcome histograms to
+``stats.json``: the counts that the chi-square tests compare runs with
+different random streams against.
 """
 from __future__ import annotations
 
@@ -268,6 +273,70 @@ def frame_cases():
     return out
 
 
+def stat_cases():
+    """Circuits of the statistical tests, each with its shot count.  The
+    first five restate the reference's own statistical tests
+    (tests/test_noise_and_io.py:101-186, tests/test_reset.py:11-37) at fixed
+    dimensions and probabilities; the last two correlate several records
+    (a GHZ state under depolarizing noise; a mid-circuit MEASURE + RESET)."""
+    def c(n, d, ops, name):
+        return W.CircuitSpec(n, d, ops, name)
+
+    nz = lambda q, p, ch: ("N1", q, None, {"prob": p, "noise_channel": ch})  # noqa: E731
+    m = lambda q: ("M", q, None, {})  # noqa: E731
+    out = [
+        (c(1, 3, [nz(0, 0.55, "d"), m(0)], "stat_depolarizing_d3"), 100_000),
+        (c(1, 7, [nz(0, 0.8, "d"), m(0)], "stat_depolarizing_d7"), 100_000),
+        (c(1, 5, [nz(0, 0.37, "f"), m(0)], "stat_flip_d5"), 100_000),
+        (c(1, 11, [("H", 0, None, {}), nz(0, 0.42, "p"), ("H_INV", 0, None, {}), m(0)], "stat_phase_d11"), 100_000),
+        (c(1, 5, [nz(0, 24 / 25, "d"), ("RESET", 0, None, {})] + [("X", 0, None, {})] * 3 + [m(0)],
+           "stat_reset_skip_d5"), 100_000),
+        (c(3, 3, [("H", 0, None, {}), ("CNOT", 0, 1, {}), ("CNOT", 1, 2, {})]
+           + [nz(q, 0.3, "d") for q in range(3)] + [m(q) for q in range(3)], "stat_ghz_d3"), 100_000),
+        (c(3, 2, [("H", 0, None, {}), ("CNOT", 0, 1, {}), nz(1, 0.2, "d"), m(1), ("RESET", 1, None, {}),
+                  ("CNOT", 0, 1, {}), ("CNOT", 1, 2, {}), nz(2, 0.1, "f"), m(0), m(1), m(2)],
+           "stat_midcircuit_reset_d2"), 100_000),
+    ]
+    return out
+
+
+def main_stats():
+    import random as pyrandom
+
+    from sdim.circuit import Circuit
+    from sdim.program import Program
+
+    cases = []
+    for k, (spec_, shots) in enumerate(stat_cases()):
+        seed = 1000 + k
+        pyrandom.seed(seed)
+        np.random.seed(seed)
+        nested = Program(spec_.build(Circuit)).simulate(shots=shots)
+        counts = [0] * spec_.num_qudits
+        cols, kinds = [], []
+        for op in spec_.ops:
+            if op[0] in ("M", "RESET"):
+                q = op[1]
+                cols.append([int(r.measurement_value) for r in nested[q][counts[q]]])
+                kinds.append(op[0])
+                counts[q] += 1
+        vals = np.asarray(cols, dtype=np.int64).T
+        d = spec_.dimension
+        # the reference's frame route gives every shot shot 0's value at a
+        # RESET (sdim/program.py:146-157), so RESET records are left out of
+        # the joint histogram: it is over the M records, first record in the
+        # lowest digit
+        keep = [j for j, k in enumerate(kinds) if k == "M"]
+        index = (vals[:, keep] * (d ** np.arange(len(keep)))).sum(axis=1)
+        hist = np.bincount(index, minlength=d ** len(keep))
+        resets = [sorted(set(vals[:, j].tolist())) for j, k in enumerate(kinds) if k == "RESET"]
+        cases.append({"name": spec_.name, "shots": shots, "reference_seed": seed, "circuit": spec_.to_json(),
+                      "record_kinds": kinds, "histogram": hist.tolist(), "reset_values": resets})
+        print(spec_.name, hist[:8].tolist(), resets, flush=True)
+    (HERE / "stats.json").write_text(json.dumps({"cases": cases}, indent=0))
+    print("wrote", len(cases), "statistical cases")
+
+
 def main_frames():
     cases, arrays = [], {}
     for s, nshots in frame_cases():
@@ -495,6 +564,8 @@ def main():
 if __name__ == "__main__":
     if "--frames" in sys.argv:
         main_frames()
+    elif "--stats" in sys.argv:
+        main_stats()
     elif "--chp" in sys.argv:
         main_chp()
     else:
