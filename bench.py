@@ -429,6 +429,19 @@ def hbm_peak():
         return 6800.0
 
 
+def hbm_view(traffic, kernel_ms):
+    """The step's measured DRAM traffic (ncu, one step) over its CUDA-event
+    kernel time, against the measured HBM copy bandwidth: how far the step is
+    from being memory-bound.  None without a traffic figure."""
+    if not traffic or not kernel_ms or kernel_ms <= 0:
+        return None
+    peak = hbm_peak()
+    gbs = traffic / (kernel_ms / 1e3) / 1e9
+    return {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": "hbm_gbs of MEASURED_PEAKS.json (fallback 6,800 GB/s)",
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one step under ncu"}
+
+
 class Timer:
     """Per-step CUDA events on a dedicated stream; L2 flushed between steps."""
 
@@ -748,6 +761,7 @@ def run_single(args, torch, dist, ws, rank, local):
                     "kernel_ms": mean_kern,
                     "stages_ms": {"xz_pass_and_coin_pass": stages[0], "phase_pass": stages[1]},
                     "group_engine_model": group_model}
+        roofline["hbm_view"] = hbm_view(roofline["traffic"], mean_kern)
     else:
         roofline = dict(group_model)
         roofline["traffic"] = None

@@ -170,3 +170,15 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     for progs in (1, 75, 76, 5000):
         for n in range(1, 2049):
             assert bench.u8_xz_layout(n, progs, optin, sms) == forms[mode(n, progs)], (n, progs)
+
+
+def test_bench_hbm_view_of_the_trace_step():
+    """The headline roofline's HBM view: ncu DRAM bytes of one step over the
+    step's kernel time, against the measured copy bandwidth."""
+    import bench
+    traffic = bench.read_traffic("trace_engine_surface_L7.md")
+    assert traffic and traffic > 0
+    v = bench.hbm_view(traffic, 0.5)
+    assert v["achieved"] == pytest.approx(traffic / 0.5e-3 / 1e9)
+    assert v["frac"] == pytest.approx(v["achieved"] / bench.hbm_peak())
+    assert bench.hbm_view(None, 0.5) is None and bench.hbm_view(traffic, 0) is None
