@@ -138,6 +138,19 @@ def test_library_builds_and_exports_every_header_symbol():
     assert set(syms) <= set(_lib.SIGNATURES)
 
 
+def test_ctypes_bindings_match_header_arity():
+    """Every prototype of the header is bound with as many ctypes argument
+    types as it has parameters."""
+    from sdim_gb300 import _lib
+    text = (ROOT / "include" / "sdim_gb300.h").read_text()
+    protos = re.findall(r"^(?:int|double|const char\*)\s+(sdim_\w+)\s*\(([^;]*?)\);", text, re.M | re.S)
+    assert len(protos) == len(_header_symbols())
+    for name, params in protos:
+        params = " ".join(params.split())
+        arity = 0 if params in ("", "void") else len(params.split(","))
+        assert len(_lib.SIGNATURES[name][1]) == arity, name
+
+
 def test_library_without_device_reports_error_not_fallback():
     """With no CUDA device the context cannot be created: the API raises."""
     import torch
