@@ -9,6 +9,7 @@ run on the GPU, so these carry state and printing only.
 from __future__ import annotations
 
 from dataclasses import dataclass
+from math import gcd
 from typing import Optional
 
 import numpy as np
@@ -30,6 +31,21 @@ class Tableau:
             self.z_block = np.eye(n, dtype=np.int64)
         if self.x_block is None:
             self.x_block = np.zeros((n, n), dtype=np.int64)
+
+    @property
+    def coprime_order(self) -> set:
+        """Integers in [1, order) coprime to the order (sdim/tableau/dataclasses.py:48-56)."""
+        return {i for i in range(1, self.order) if gcd(i, self.order) == 1}
+
+    @property
+    def coprime_dimension(self) -> set:
+        """Integers in [1, d) coprime to d (sdim/tableau/dataclasses.py:58-66)."""
+        return {i for i in range(1, self.dimension) if gcd(i, self.dimension) == 1}
+
+    @property
+    def prime(self) -> bool:
+        """Whether d is prime, by the reference's trial division (sdim/tableau/dataclasses.py:68-76)."""
+        return not any(self.dimension % i == 0 for i in range(2, self.dimension))
 
     @property
     def even(self) -> bool:

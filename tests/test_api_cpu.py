@@ -195,3 +195,14 @@ def test_bench_hbm_view_of_the_trace_step():
     assert v["achieved"] == pytest.approx(traffic / 0.5e-3 / 1e9)
     assert v["frac"] == pytest.approx(v["achieved"] / bench.hbm_peak())
     assert bench.hbm_view(None, 0.5) is None and bench.hbm_view(traffic, 0) is None
+
+
+def test_tableau_properties_as_the_reference_defines_them():
+    """sdim/tableau/dataclasses.py:48-119: coprime sets, primality, order."""
+    from sdim_gb300.tableau import ExtendedTableau, Tableau
+    t = ExtendedTableau(3, 2)
+    assert (t.order, t.phase_order, t.pauli_size) == (4, 2, 7)
+    assert t.coprime_order == {1, 3} and t.coprime_dimension == {1} and t.prime
+    t = Tableau(2, 9)
+    assert t.order == 9 and t.coprime_order == {1, 2, 4, 5, 7, 8} and not t.prime
+    assert Tableau(1, 7).coprime_dimension == {1, 2, 3, 4, 5, 6}
