@@ -69,6 +69,17 @@ class GateData:
     def __str__(self):
         return "\n".join(str(g) for g in self.gateMap.values())
 
+    def add_gate(self, name: str, arg_count: int):
+        """Registers a gate under the next id (sdim/gatedata.py:55-59).  A
+        program that uses an id outside 0-17 is refused when it is encoded,
+        as the reference's apply_gate refuses it (sdim/program.py:381-382)."""
+        self.gateMap[name] = Gate(name, arg_count, self.num_gates)
+        self.num_gates += 1
+
+    def add_gate_alias(self, name: str, list_alias):
+        for alias in list_alias:
+            self.aliasMap[alias] = name
+
     def get_gate_id(self, gate_name: str) -> Optional[int]:
         if gate_name in self.gateMap:
             return self.gateMap[gate_name].gate_id
@@ -77,6 +88,16 @@ class GateData:
         return None
 
     def get_gate_name(self, gate_id: int) -> str:
-        if 0 <= gate_id < len(_GATES):
-            return _GATES[gate_id][0]
+        for name, gate in self.gateMap.items():
+            if gate.gate_id == gate_id:
+                return name
+        raise ValueError(f"Gate ID {gate_id} not found")
+
+    def get_gate_matrix(self, gate_id: int):
+        """The gate's ``unitary_matrix`` (sdim/gatedata.py:118-122).  No gate
+        carries one, in the reference or here, so a known id raises
+        AttributeError and an unknown one ValueError, as there."""
+        for gate in self.gateMap.values():
+            if gate.gate_id == gate_id:
+                return gate.unitary_matrix
         raise ValueError(f"Gate ID {gate_id} not found")

@@ -206,3 +206,24 @@ def test_tableau_properties_as_the_reference_defines_them():
     t = Tableau(2, 9)
     assert t.order == 9 and t.coprime_order == {1, 2, 4, 5, 7, 8} and not t.prime
     assert Tableau(1, 7).coprime_dimension == {1, 2, 3, 4, 5, 6}
+
+
+def test_gatedata_registration_as_the_reference():
+    """sdim/gatedata.py:55-122: add_gate takes the next id, aliases resolve,
+    get_gate_matrix fails for every id (no gate has a matrix)."""
+    from sdim_gb300 import Circuit, GateData
+    g = GateData(3)
+    g.add_gate("FOO", 1)
+    g.add_gate_alias("FOO", ["BAR"])
+    assert g.get_gate_id("FOO") == 18 and g.get_gate_id("BAR") == 18 and g.get_gate_name(18) == "FOO"
+    assert g.get_gate_name(9) == "CNOT" and g.get_gate_id("SUM") == 9
+    with pytest.raises(ValueError):
+        g.get_gate_name(19)
+    with pytest.raises(AttributeError):
+        g.get_gate_matrix(5)
+    with pytest.raises(ValueError):
+        g.get_gate_matrix(40)
+    c = Circuit(2, 3)
+    c.gate_data.add_gate("FOO", 1)
+    c.add_gate("foo", [0, 1])
+    assert [op.gate_id for op in c.operations] == [18, 18]
