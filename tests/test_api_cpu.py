@@ -227,3 +227,19 @@ def test_gatedata_registration_as_the_reference():
     c.gate_data.add_gate("FOO", 1)
     c.add_gate("foo", [0, 1])
     assert [op.gate_id for op in c.operations] == [18, 18]
+
+
+def test_table_encoder_equals_circuit_encoder():
+    """encode_table (arrays, the batch and serving path) gives the op table,
+    record qudits, record rounds and gate counts of encode_program (Circuit
+    objects) for the same program."""
+    from sdim_gb300 import workloads
+    from sdim_gb300.encode import encode_table
+    for n, d, seed in ((5, 3, 1), (40, 7, 2), (97, 2, 3)):
+        spec = workloads.random_hpc(n, d, 6 * n, seed=seed, mr_every=n, mr_fraction=0.3)
+        a = encode_table(spec.table, n, d)
+        b = encode_program([spec.build()], n, d)
+        assert np.array_equal(a.ops, b.ops)
+        assert np.array_equal(a.meas_qudit, b.meas_qudit) and np.array_equal(a.meas_round, b.meas_round)
+        assert a.gate_counts == b.gate_counts
+        assert a.num_records == b.num_records > n
