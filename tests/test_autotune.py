@@ -130,3 +130,57 @@ def test_batch_key_depends_on_composition_only():
     assert t.batch_key(a) == t.batch_key(list(reversed(a)))
     assert t.batch_key(a) != t.batch_key(a[:1])
     assert [c.flags for c in autotune.batch_candidates()][0] == 0
+
+
+class _BatchProgram:
+    def __init__(self, n, d, records):
+        self.enc = _Enc(n, d)
+        self.num_instructions = 4 * n
+        self.num_records = records
+
+
+class _Entry:
+    def __init__(self, prog, shots):
+        self.program, self.shots = prog, shots
+
+
+class _FakeRunner:
+    """Writes records that depend only on the entry, as every route does,
+    and reports a kernel time per route."""
+
+    def __init__(self, ctx, times, wrong_flags=None):
+        self.ctx, self.times, self.wrong_flags = ctx, times, wrong_flags
+        self.entries = [_Entry(_BatchProgram(8, 3, 2), 5), _Entry(_BatchProgram(200, 2, 3), 70)]
+        self.calls = []
+
+    def run(self, time_kernels=False, outs=None, flags=0):
+        self.calls.append(flags)
+        for i, o in enumerate(outs):
+            o[:] = i + 1 + (1 if flags == self.wrong_flags else 0)
+        self.ctx.last_ms = self.times.get(flags, 10.0)
+        return outs
+
+
+class _TimedCtx(_Ctx):
+    last_ms = 0.0
+
+    def last_kernel_ms(self):
+        return self.last_ms
+
+
+def test_tune_batch_picks_the_fastest_route_and_caches_it():
+    ctx = _TimedCtx()
+    runner = _FakeRunner(ctx, {0: 5.0, _lib.FLAG_SPLIT_XZ: 3.0, _lib.FLAG_TRACE: 50.0})
+    t = autotune.Autotuner(ctx=ctx, reps=2)
+    assert t.flags_for_batch(runner) == _lib.FLAG_SPLIT_XZ
+    res = t.results[t.batch_key(t._batch_items(runner))]
+    assert "trace engines at any shot count" in res.aborted
+    n_calls = len(runner.calls)
+    assert t.flags_for_batch(runner) == _lib.FLAG_SPLIT_XZ and len(runner.calls) == n_calls
+
+
+def test_tune_batch_rejects_a_route_that_changes_records():
+    ctx = _TimedCtx()
+    runner = _FakeRunner(ctx, {}, wrong_flags=_lib.FLAG_NO_TRACE)
+    with pytest.raises(RuntimeError, match="shot groups only"):
+        autotune.Autotuner(ctx=ctx, reps=1).tune_batch(runner)
