@@ -87,6 +87,7 @@ SIGNATURES = {
 }
 
 _lock = threading.Lock()
+_default_lock = threading.Lock()
 _lib = None
 
 
@@ -155,9 +156,12 @@ class Context:
 
     @classmethod
     def default(cls, device: int = 0) -> "Context":
-        if device not in cls._default:
-            cls._default[device] = Context(device)
-        return cls._default[device]
+        """The process-wide context of a device (created once, also when
+        several threads ask at the same time)."""
+        with _default_lock:
+            if device not in cls._default:
+                cls._default[device] = Context(device)
+            return cls._default[device]
 
     def close(self):
         if self.ptr:
