@@ -115,7 +115,12 @@ class Program:
         return self._ctx
 
     def _program_key(self, noise: bool):
-        return (tuple((id(c), len(c.operations), c.num_qudits) for c in self.circuits), bool(noise))
+        """Cache key of the encoded program: every circuit and every
+        instruction object in it, so that adding, removing, replacing or
+        reordering instructions re-encodes (the reference re-reads the
+        circuit on every simulate, sdim/program.py:311-320).  An instruction
+        edited in place keeps its key: build a new one instead."""
+        return (tuple((id(c), c.num_qudits, tuple(map(id, c.operations))) for c in self.circuits), bool(noise))
 
     def compile(self, noise: bool = True) -> DeviceProgram:
         """Encoded program on the device (cached until the circuits change)."""

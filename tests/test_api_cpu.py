@@ -243,3 +243,23 @@ def test_table_encoder_equals_circuit_encoder():
         assert np.array_equal(a.meas_qudit, b.meas_qudit) and np.array_equal(a.meas_round, b.meas_round)
         assert a.gate_counts == b.gate_counts
         assert a.num_records == b.num_records > n
+
+
+def test_program_cache_key_follows_the_instructions():
+    """Replacing, adding or reordering instructions changes the key under
+    which the encoded program is cached (no device needed)."""
+    from sdim_gb300 import Program
+    from sdim_gb300.circuit import CircuitInstruction
+    c = Circuit(2, 3)
+    c.add_gate("H", 0)
+    c.add_gate("M", 0)
+    prog = Program(c)
+    k0 = prog._program_key(True)
+    assert prog._program_key(True) == k0 and prog._program_key(False) != k0
+    c.operations[0] = CircuitInstruction(c.gate_data, "P", 0)
+    k1 = prog._program_key(True)
+    assert k1 != k0
+    c.operations.reverse()
+    assert prog._program_key(True) != k1
+    c.add_gate("M", 1)
+    assert len(prog._program_key(True)[0][0][2]) == 3
