@@ -114,24 +114,42 @@ class Program:
             self._ctx = _lib.Context.default(self.device)
         return self._ctx
 
+    @staticmethod
+    def _instruction_content(ins) -> tuple:
+        """What the encoder reads from one instruction: gate id, qudit,
+        target, and for N1 the channel keys and probability."""
+        gid = ins.gate_id
+        if gid == 17:
+            p = ins.params or {}
+            return (gid, ins.qudit_index, ins.target_index,
+                    (p.get("noise_channel"), p.get("channel"), p.get("prob")))
+        return (gid, ins.qudit_index, ins.target_index)
+
     def _program_key(self, noise: bool):
-        """Cache key of the encoded program: every circuit and every
-        instruction object in it, so that adding, removing, replacing or
-        reordering instructions re-encodes (the reference re-reads the
-        circuit on every simulate, sdim/program.py:311-320).  An instruction
-        edited in place keeps its key: build a new one instead."""
-        return (tuple((id(c), c.num_qudits, tuple(map(id, c.operations))) for c in self.circuits), bool(noise))
+        """Cache key of the encoded program: the content of every instruction
+        of every circuit (and each circuit's qudit count), read afresh on
+        every call as the reference re-reads ``circuit.operations`` on every
+        simulate (sdim/program.py:311-320).  Added, removed, replaced,
+        reordered or edited-in-place instructions all change it; object
+        identities play no part, so a new instruction that reuses a freed
+        object's address cannot alias an old one."""
+        content = self._instruction_content
+        return (tuple((c.num_qudits, tuple([content(o) for o in c.operations])) for c in self.circuits),
+                bool(noise))
 
     def compile(self, noise: bool = True) -> DeviceProgram:
-        """Encoded program on the device (cached until the circuits change)."""
+        """Encoded program on the device (cached while the circuits' content
+        stays the same)."""
         key = self._program_key(noise)
-        dp = self._cache.get(key)
-        if dp is None:
-            enc = encode_program(self.circuits, self.num_qudits, self.dimension, noise=noise)
-            dp = DeviceProgram(self.context, enc)
-            # keep the other noise setting of the same circuits (the frame route uses both)
-            self._cache = {k: v for k, v in self._cache.items() if k[0] == key[0]}
-            self._cache[key] = dp
+        hit = self._cache.get(key[1])
+        if hit is not None and hit[0] == key[0]:
+            return hit[1]
+        enc = encode_program(self.circuits, self.num_qudits, self.dimension, noise=noise)
+        dp = DeviceProgram(self.context, enc)
+        # keep the other noise setting only while it encodes the same circuits
+        # (the frame route uses both)
+        self._cache = {k: v for k, v in self._cache.items() if v[0] == key[0]}
+        self._cache[key[1]] = (key[0], dp)
         return dp
 
     def _seed(self, seed):

@@ -262,4 +262,50 @@ def test_program_cache_key_follows_the_instructions():
     c.operations.reverse()
     assert prog._program_key(True) != k1
     c.add_gate("M", 1)
-    assert len(prog._program_key(True)[0][0][2]) == 3
+    assert len(prog._program_key(True)[0][0][1]) == 3
+    # an instruction edited in place changes the key too
+    k2 = prog._program_key(True)
+    c.operations[-1].qudit_index = 0
+    assert prog._program_key(True) != k2
+
+
+class _FakeDeviceProgram:
+    """Stands in for DeviceProgram: records what compile() encoded."""
+    made = 0
+
+    def __init__(self, ctx, enc):
+        _FakeDeviceProgram.made += 1
+        self.enc = enc
+
+
+def test_program_recompiles_after_pop_and_add_gate(monkeypatch):
+    """1,000 rounds of operations.pop() + add_gate() on a live Program: each
+    round's compile() encodes the circuit as it now stands (the freed
+    instruction's address is reused by CPython within a few rounds, so a key
+    built on object ids would hand back the stale program)."""
+    import sdim_gb300.program as P
+    monkeypatch.setattr(P, "DeviceProgram", _FakeDeviceProgram)
+    c = Circuit(3, 3)
+    c.add_gate("H", 0)
+    c.add_gate("CNOT", 0, 1)
+    c.add_gate("M", 0)
+    prog = P.Program(c)
+    prog._ctx = object()
+    dp = prog.compile()
+    assert prog.compile() is dp  # unchanged circuit: cached
+    _FakeDeviceProgram.made = 0
+    prev_key = prog._program_key(True)
+    for r in range(1000):
+        c.operations.pop()
+        c.add_gate("M", (r + 1) % 3)
+        key = prog._program_key(True)
+        assert key != prev_key
+        prev_key = key
+        dp = prog.compile()
+        assert int(dp.enc.ops[-1, 0]) == 14 and int(dp.enc.ops[-1, 1]) == (r + 1) % 3
+        assert prog.compile() is dp
+    assert _FakeDeviceProgram.made == 1000
+    # the same content again is a cache hit, also with fresh instruction objects
+    c.operations.pop()
+    c.add_gate("M", 1000 % 3)
+    assert prog.compile() is dp and _FakeDeviceProgram.made == 1000

@@ -229,3 +229,26 @@ def test_noiseless_surface_code_properties_100k_shots():
     assert np.all(det[0, n_anc:7 * n_anc] == 1)     # later rounds are deterministic
     frac_one = rounds[:, 0, :24].mean()
     assert 0.48 < frac_one < 0.52                    # X checks start random
+
+
+def test_simulate_follows_circuit_mutations_against_oracle():
+    """A live Program whose circuit is changed between calls (last
+    instruction popped and a different one added, an instruction edited in
+    place) simulates the circuit as it now stands: every call's records
+    equal the oracle's on the same circuit object (the reference re-reads
+    circuit.operations on every simulate, sdim/program.py:311-320)."""
+    spec = workloads.random_hpc(6, 3, 60, seed=21)
+    c = spec.build()
+    prog = Program(c)
+    for r in range(40):
+        if r:
+            c.operations.pop()
+            c.add_gate("M" if r % 2 else "P", r % 6)
+        if r % 7 == 3 and c.operations[r].target_index is None:
+            c.operations[r].qudit_index = (c.operations[r].qudit_index + 1) % 6
+        got = prog.sample(64, seed=100 + r)
+        ref = oracle.simulate(oracle.OracleProgram([c], 6, 3), 100 + r, 0, 64)["records"]
+        assert np.array_equal(got, ref), r
+        res = prog.simulate(shots=4, force_tableau=True, seed=100 + r)
+        flat = [[m.measurement_value for m in rounds] for per_q in res for rounds in per_q]
+        assert sum(len(f) for f in flat) == 4 * ref.shape[1]
