@@ -20,15 +20,23 @@
 //     tableau slots); larger programs are rejected with SDIM_EINVAL;
 //   * the first call on a device resolves the array's device address with
 //     cudaGetSymbolAddress (with that device current) and sets the kernels'
-//     shared-memory attribute; make that first call before any stream capture;
+//     shared-memory attribute; make that first call before any stream capture.
+//     Host threads that make their first calls at the same time are
+//     serialised by a lock; later calls read the published setup without it;
 //   * every call shares the array, which keeps the last call's contents: the
 //     counter and the status word are cleared at the start of each call, and
 //     calls that overlap on the GPU (several streams or host threads at once)
 //     race on it;
+//   * a program rejected part-way through encoding (a bad gate, qudit or
+//     probability after the first 1,024 instructions) has already overwritten
+//     the start of the array's instruction area; nothing reads it until the
+//     next call rewrites it, so this is harmless under the rules above;
 //   * the call is synchronous on the given stream.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "../../include/sdim_gb300.h"
 #include "kernels.cuh"
@@ -48,9 +56,10 @@ struct DeviceSetup {
   unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
   int smem_optin = 0;
   int num_sms = 0;
-  bool done = false;
+  std::atomic<bool> done{false};     // set (release) after the fields above
 };
 DeviceSetup g_setup[kMaxDevices];
+std::mutex g_setup_lock;  // serialises first calls; done is re-checked under it
 
 template <class E>
 __global__ void __launch_bounds__(1024) k_persistent_noalloc(CircuitDesc c, long long total_items,
@@ -122,35 +131,41 @@ extern "C" int sdim_run_noalloc(const int32_t* ops, int64_t nops, const double* 
     return fail(SDIM_ECUDA, "no current CUDA device");
   }
   DeviceSetup& ds = g_setup[dev];
-  if (!ds.done) {
+  if (!ds.done.load(std::memory_order_acquire)) {
     // once per device, with that device current
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(SDIM_ECUDA, "cudaGetSymbolAddress of the scratch array failed");
+    std::lock_guard<std::mutex> hold(g_setup_lock);
+    if (!ds.done.load(std::memory_order_relaxed)) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SDIM_ECUDA, "cudaGetSymbolAddress of the scratch array failed");
+      }
+      int smem = 0, sms = 0;
+      if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SDIM_ECUDA, "device attribute query failed");
+      }
+      if (set_attr<EngineBits>(smem) != cudaSuccess || set_attr<EngineU8<3>>(smem) != cudaSuccess ||
+          set_attr<EngineU8<5>>(smem) != cudaSuccess || set_attr<EngineU8<7>>(smem) != cudaSuccess ||
+          set_attr<EngineU8<0>>(smem) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SDIM_ECUDA, "cudaFuncSetAttribute failed");
+      }
+      ds.scratch = static_cast<unsigned char*>(p);
+      ds.smem_optin = smem;
+      ds.num_sms = sms;
+      ds.done.store(true, std::memory_order_release);
     }
-    int smem = 0, sms = 0;
-    if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(SDIM_ECUDA, "device attribute query failed");
-    }
-    if (set_attr<EngineBits>(smem) != cudaSuccess || set_attr<EngineU8<3>>(smem) != cudaSuccess ||
-        set_attr<EngineU8<5>>(smem) != cudaSuccess || set_attr<EngineU8<7>>(smem) != cudaSuccess ||
-        set_attr<EngineU8<0>>(smem) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(SDIM_ECUDA, "cudaFuncSetAttribute failed");
-    }
-    ds.scratch = static_cast<unsigned char*>(p);
-    ds.smem_optin = smem;
-    ds.num_sms = sms;
-    ds.done = true;
   }
   const size_t slot = ((d == 2 ? EngineBits::slot_bytes(n) : SlotU8::bytes(n)) + 15) & ~(size_t)15;
   if (slot > (size_t)ds.smem_optin)
     return fail(SDIM_EINVAL, "tableau does not fit in shared memory: sdim_run_noalloc keeps no global slots");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // encode in fixed chunks on the stack and copy them into the scratch array
+  // encode in fixed chunks on the stack and copy them into the scratch array.
+  // The chunk is pageable host memory: cudaMemcpyAsync from pageable memory
+  // returns only once the source has been staged, so the chunk can be
+  // refilled as soon as the call returns.
   uint2 chunk[1024];
   int nchunk = 0, ndev = 0, nmeas = 0;
   auto flush = [&]() -> int {
