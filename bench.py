@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--circuits", type=int, default=8192, help="programs of the uneven batch")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true",
+                    help="default workload: leave out the uneven-batch sub-object")
     ap.add_argument("--autotune", action="store_true",
                     help="uneven batch: also time the autotuner's batch-wide routes")
     ap.add_argument("--plain-shots", type=int, default=256)
@@ -101,6 +103,24 @@ def single_workload(args):
         desc = (f"odd d={d}, n=256, 2,560 gates (H 25%, P 25%, CNOT 50%), MEASURE+RESET on 10% every 256 gates, "
                 "MEASURE all")
     return spec, (args.shots or shots), desc
+
+
+def single_config(spec, shots, desc, ws):
+    """The config dict of a single-program workload, the same on both arms."""
+    return {"workload": desc, "qudits": spec.num_qudits, "dimension": spec.dimension,
+            "instructions": len(spec.ops), "shots_per_gpu": shots, "records_per_shot": spec.num_measurements(),
+            "seed": 0, "l2": "flushed (256 MB write) between timed steps, outside the events",
+            "parallelism": f"replicas x{ws}: per-GPU shot ranges, no collective"}
+
+
+def uneven_config(items, ws):
+    """The config dict of the uneven batch, the same on both arms."""
+    ns = np.array([it.spec.num_qudits for it in items])
+    return {"workload": f"uneven batch: {len(items)} programs, n log-uniform [8,1024] (median "
+                        f"{int(np.median(ns))}), d in {{2,3,5,7}}, 4n gates + MEASURE all, shots 1-64",
+            "programs": len(items), "shots_per_gpu": int(sum(it.shots for it in items)),
+            "gate_updates_per_step": int(sum(it.shots * len(it.spec.ops) for it in items)),
+            "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"}
 
 
 def uneven_items(args):
@@ -278,14 +298,12 @@ def run_reference_arm(args):
     if args.workload == "uneven":
         items = uneven_items(args)
         fn = lambda budget, k: cpu_rate_uneven(items, budget)  # noqa: E731
-        desc = f"uneven batch of {len(items)} programs"
-        cfg = {"workload": desc}
+        cfg = uneven_config(items, ws)
         unit_desc = "programs (systematic sample, min(shots,4) shots each)"
     else:
         spec, shots, desc = single_workload(args)
         fn = lambda budget, k: cpu_rate_single(spec, budget, shot0=k * 1_000_000)  # noqa: E731
-        cfg = {"workload": desc, "qudits": spec.num_qudits, "dimension": spec.dimension,
-               "instructions": len(spec.ops), "shots_per_gpu": shots}
+        cfg = single_config(spec, shots, desc, ws)
         unit_desc = "shots of the workload"
     for k in range(args.warmup):
         fn(min(1.0, per_step), k)
@@ -791,10 +809,7 @@ def run_single(args, torch, dist, ws, rank, local):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "u32 bit planes (d=2) / u8 residues (odd d): exact integer mod d",
         "data": "synthetic (seeded circuit generator, Philox outcome and noise stream)",
-        "config": {"workload": desc, "qudits": n, "dimension": d, "instructions": len(spec.ops),
-                   "shots_per_gpu": shots, "records_per_shot": nrec, "seed": 0,
-                   "l2": "flushed (256 MB write) between timed steps, outside the events",
-                   "parallelism": f"replicas x{ws}: per-GPU shot ranges, no collective"},
+        "config": single_config(spec, shots, desc, ws),
         "shots_per_s": shots * ws * args.steps / (total_ms / 1e3),
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(dp.num_device_ops * 8),
@@ -818,16 +833,56 @@ def run_single(args, torch, dist, ws, rank, local):
     }
 
 
-def run_uneven(args, torch, dist, ws, rank, local):
+def _leg(name, t0):
+    """Wall time of one bench leg, on stderr (the JSON line stays on stdout)."""
+    print(f"[bench] {name}: {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
+
+
+def plain_uneven(br, entries, budget_s):
+    """Plain form (one single-warp launch per shot) on a systematic sample
+    of the batch: every 128th program, one shot each, timed by itself.  A
+    plain run is one launch sequence per shot, so a program's plain time is
+    its one-shot time times its shot count; the rate is the sample's
+    gate-updates over that time.  Programs are visited from the smallest
+    up and the leg stops once budget_s is spent, so the largest programs of
+    the sample may be left out (the count is reported)."""
+    from sdim_gb300.batch import BatchEntry, BatchRunner
+    sample = sorted(entries[::128], key=lambda e: e.program.num_instructions * e.program.n ** 2)
+    units, est_s, spent, used = 0, 0.0, 0.0, 0
+    for e in sample:
+        one = BatchRunner._view(br.ctx, [BatchEntry(e.program, 1, e.seed, e.shot0)])
+        t0 = time.perf_counter()
+        one.run(plain=True)
+        dt = time.perf_counter() - t0
+        spent += dt
+        units += e.shots * e.program.num_instructions
+        est_s += dt * e.shots
+        used += 1
+        if spent > budget_s:
+            break
+    return units / est_s, used, len(sample), spent
+
+
+def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
+    """The uneven batch (8,192 programs by default): device-timed steps, the
+    end-to-end run with host records, the plain form on a bounded sample, the
+    roofline bound of the batch, and (full run only) the per-shot engine, the
+    CPU oracle, the graph replay and the autotuner.  ``sub``: the bounded
+    form attached to the default bench line (steps capped, no per-shot
+    engine)."""
     from sdim_gb300 import _lib
     from sdim_gb300.batch import BatchRunner
 
+    t_leg = time.perf_counter()
     items = uneven_items(args)
     br = BatchRunner(_lib.Context.default(local))
     ctx = br.ctx
     for it in items:
         br.add_spec(it.spec, it.shots, it.seed, shot0=rank * 64)
     entries = br.entries
+    _leg("uneven: generate and encode", t_leg)
+    steps = min(args.steps, 10) if sub else args.steps
+    warmup = max(3, min(args.warmup, 3)) if sub else args.warmup
     sizes = [e.shots * e.program.num_records for e in entries]
     offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     out = torch.empty(int(offs[-1]) + 1, dtype=torch.uint8, device="cuda")
@@ -840,32 +895,46 @@ def run_uneven(args, torch, dist, ws, rank, local):
         br.run_device(ptrs, stream=stream.cuda_stream, time_kernels=True, asynchronous=True,
                       per_shot=bool(extra & _lib.FLAG_PER_SHOT))
 
-    for _ in range(args.warmup):
+    t_leg = time.perf_counter()
+    for _ in range(warmup):
         step()
     ctx.sync()
-    step_ms, kern_ms, clk = timer.run(args.steps, step, Clocks(local))
+    step_ms, kern_ms, clk = timer.run(steps, step, Clocks(local))
     total_ms = timer.max_over_ranks(sum(step_ms))
+    stages = [statistics.mean(v) for v in zip(*timer.stage_ms)]
     units_per_step = br.total_gate_updates()
-    value = units_per_step * ws * args.steps / (total_ms / 1e3)
+    value = units_per_step * ws * steps / (total_ms / 1e3)
     ref_out = out.cpu().numpy()
+    _leg(f"uneven: {warmup} warm-up + {steps} timed steps", t_leg)
 
-    # the per-shot engine on the same batch
-    step(_lib.FLAG_PER_SHOT)
-    ctx.sync()
-    ps_step_ms, ps_kern_ms, _ = timer.run(1, lambda: step(_lib.FLAG_PER_SHOT))
-    if not np.array_equal(out.cpu().numpy(), ref_out):
-        raise AssertionError("shot-group and per-shot engines disagree on the uneven batch")
-    graph = graph_replay(args, torch, ctx, timer, stream, entries, units_per_step,
-                         lambda: ref_out[:-1]) if rank == 0 else None
+    ps = None
+    if not sub:
+        # the per-shot engine on the same batch
+        t_leg = time.perf_counter()
+        step(_lib.FLAG_PER_SHOT)
+        ctx.sync()
+        ps_step_ms, ps_kern_ms, _ = timer.run(1, lambda: step(_lib.FLAG_PER_SHOT))
+        if not np.array_equal(out.cpu().numpy(), ref_out):
+            raise AssertionError("shot-group and per-shot engines disagree on the uneven batch")
+        ps = {"value": units_per_step / (sum(ps_step_ms) / 1e3), "unit": UNIT,
+              "kernel_ms": statistics.mean(ps_kern_ms)}
+        _leg("uneven: per-shot engine", t_leg)
+    graph = None
+    if rank == 0 and not sub:
+        t_leg = time.perf_counter()
+        graph = graph_replay(args, torch, ctx, timer, stream, entries, units_per_step, lambda: ref_out[:-1])
+        _leg("uneven: graph replay", t_leg)
     tuned = None
     if rank == 0 and args.autotune:
         # the autotuner over the batch-wide routes (records checked equal to
         # the default route's; kernel time by the library's CUDA events)
+        t_leg = time.perf_counter()
         from sdim_gb300.autotune import Autotuner
         res = Autotuner(ctx, reps=2).tune_batch(br)
         tuned = {"best": res.best.name, "flags": res.best.flags, "kernel_ms": res.times_ms,
                  "aborted_after_one_run": res.aborted,
                  "value": units_per_step / (res.times_ms[res.best.name] / 1e3), "unit": UNIT}
+        _leg("uneven: autotuner", t_leg)
 
     # algorithmic bytes: det flags per program from its first shot.  The x / z
     # tableau is updated once per program on the trace engines and once per
@@ -895,59 +964,56 @@ def run_uneven(args, torch, dist, ws, rank, local):
     mean_kern = statistics.mean(kern_ms)
 
     # end to end: host records (pinned), descriptors up and records down inside
+    t_leg = time.perf_counter()
     host = torch.empty(int(offs[-1]) + 1, dtype=torch.uint8, pin_memory=True)
     host_np = host.numpy()
     houts = [host_np[int(a):int(b)].reshape(e.shots, e.program.num_records)
              for a, b, e in zip(offs[:-1], offs[1:], entries)]
+    e2e_steps = min(steps, 3) if sub else steps
     e2e_ms = []
-    for k in range(args.warmup + args.steps):
+    for k in range(warmup + e2e_steps):
         t0 = time.perf_counter()
         br.run(outs=houts)
-        if k >= args.warmup:
+        if k >= warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     if not np.array_equal(host_np[:-1], ref_out[:-1]):
         raise AssertionError("end-to-end records differ")
     e2e_total = timer.max_over_ranks(sum(e2e_ms))
-    e2e_value = units_per_step * ws * args.steps / (e2e_total / 1e3)
+    e2e_value = units_per_step * ws * e2e_steps / (e2e_total / 1e3)
+    _leg("uneven: end to end", t_leg)
     if rank != 0:
         return None
-    # plain form (one single-warp launch per shot) on a systematic sample of programs
-    sample = entries[::128]
-    t0 = time.perf_counter()
-    br.run(plain=True, entries=sample)
-    plain_s = time.perf_counter() - t0
-    plain_units = sum(e.shots * e.program.num_instructions for e in sample)
-    plain_rate = plain_units / plain_s
+    t_leg = time.perf_counter()
+    plain_rate, plain_used, plain_sample, plain_s = plain_uneven(br, entries, 15.0 if sub else 60.0)
+    _leg("uneven: plain form", t_leg)
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and not sub:
+        t_leg = time.perf_counter()
         r, used, cdt, threads = cpu_rate_uneven(items, args.cpu_seconds)
         cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{used} programs, min(shots,4) shots each, in {cdt:.1f} s (C oracle, OpenMP)"}
-    ns = np.array([it.spec.num_qudits for it in items])
+        _leg("uneven: CPU oracle", t_leg)
     return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u32 bit planes (d=2) / u8 residues (odd d): exact integer mod d",
-        "data": "synthetic (seeded generator, Philox outcome stream)",
-        "config": {"workload": f"uneven batch: {len(items)} programs, n log-uniform [8,1024] (median "
-                               f"{int(np.median(ns))}), d in {{2,3,5,7}}, 4n gates + MEASURE all, shots 1-64",
-                   "programs": len(items), "shots_per_gpu": br.total_shots(),
-                   "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
-        "shots_per_s": br.total_shots() * ws * args.steps / (total_ms / 1e3),
+        "value": value, "unit": UNIT, "steps": steps, "warmup": warmup, "ms_per_step": total_ms / steps,
+        "config": uneven_config(items, ws),
+        "shots_per_s": br.total_shots() * ws * steps / (total_ms / 1e3),
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "kernel_ms": mean_kern,
+        "stages_ms": {"xz_pass_and_coin_pass": stages[0], "phase_pass": stages[1], "shot_group_engines": stages[2]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 80 * len(items),
-                "d2h_bytes_per_step": int(offs[-1]), "ms_per_step": e2e_total / args.steps},
-        "plain_gpu": {"value": plain_rate, "unit": UNIT, "programs": len(sample),
-                      "form": "one single-warp launch per shot, systematic sample of programs"},
+                "d2h_bytes_per_step": int(offs[-1]), "ms_per_step": e2e_total / e2e_steps, "steps": e2e_steps},
+        "plain_gpu": {"value": plain_rate, "unit": UNIT, "programs_timed": plain_used,
+                      "programs_in_sample": plain_sample, "seconds": plain_s,
+                      "form": "one single-warp launch per shot; every 128th program, one shot each timed, "
+                              "times its shot count, smallest programs first within a time budget"},
         "batched_vs_plain": value / plain_rate,
-        "per_shot_engine": {"value": units_per_step / (sum(ps_step_ms) / 1e3), "unit": UNIT,
-                            "kernel_ms": statistics.mean(ps_kern_ms)},
+        "per_shot_engine": ps,
         "roofline": {"bound": "smem for resident tableaux, L2 for columns streamed by CTA clusters, HBM for "
                               "other streamed tableaux",
                      "achieved": gb / (mean_kern / 1e3) / 1e9, "peak": gb / t_min / 1e9, "unit": "GB/s",
                      "frac": t_min * 1e3 / mean_kern, "traffic": None,
-                     "kernel": "trace engines (k_trace_pass*, k_phase_pass*) for n >= 160, k_group_warp / "
-                               "k_group_cta for the rest",
+                     "kernel": "trace engines (k_trace_pass*, k_phase_pass*) for n >= 160 or 128+ shots, "
+                               "k_group_warp / k_group_cta for the rest",
                      "algorithmic_bytes_per_launch": gb, "streamed_bytes": streamed, "l2_bytes": in_l2,
                      "kernel_ms": mean_kern, "bound_ms": t_min * 1e3, "smem_peak_gbs": peak, "l2_peak_gbs": l2,
                      "hbm_peak_gbs": hbm,
@@ -955,14 +1021,27 @@ def run_uneven(args, torch, dist, ws, rank, local):
                                     "sdim_probe_smem_bandwidth / sdim_probe_l2_bandwidth; HBM from "
                                     "MEASURED_PEAKS.json",
                      "bytes_model": "x/z tableau updates once per program (trace engines) or per 32-shot group, "
-                                    "plus per-shot phase-delta bytes"},
+                                    "plus per-shot phase-delta bytes; frac = bound_ms / kernel_ms"},
         "cpu_baseline": cpu,
         # one persistent launch per (dimension, team kind) present in the batch
-        "gpu_launches": args.steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),
+        "gpu_launches": steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),
         "clocks": clk,
         "graph_replay": graph,
         "autotune": tuned,
     }
+
+
+def run_uneven(args, torch, dist, ws, rank, local):
+    m = uneven_measure(args, torch, dist, ws, rank, local)
+    if m is None:
+        return None
+    line = {"metric": METRIC, "value": m.pop("value"), "unit": UNIT, "n_gpus": ws, "steps": m.pop("steps"),
+            "warmup": m.pop("warmup"), "ms_per_step": m.pop("ms_per_step"), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32 bit planes (d=2) / u8 residues (odd d): exact integer mod d",
+            "data": "synthetic (seeded generator, Philox outcome stream)"}
+    line.update(m)
+    return line
 
 
 def serving_trace(args, seed=0):
@@ -1043,6 +1122,11 @@ def run_gb300(args):
         line = run_serving(args, rank, local)
     else:
         line = run_single(args, torch, dist, ws, rank, local)
+        if args.workload == "surface" and not args.quick and not args.no_uneven:
+            # the batching target: the uneven batch, bounded, beside the headline
+            sub = uneven_measure(args, torch, dist, ws, rank, local, sub=True)
+            if line is not None:
+                line["uneven"] = sub
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()

@@ -1,9 +1,10 @@
 """Generates the golden fixtures by running the reference sdim itself.
 
-Run in a container that holds the reference source (path in $SDIM_REFERENCE,
-default /root/reference):
+Run in a container that holds the reference source, with its path in
+$SDIM_REFERENCE (required; there is no default):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
+    SDIM_REFERENCE=<path to the sdim source tree> PYTHONDONTWRITEBYTECODE=1 \
+        python tests/golden/make_golden.py
 
 It imports sdim from the reference tree (with import-time stand-ins for
 numba, cirq and Diophantine from ``_stubs``, none of which the
@@ -48,10 +49,12 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REF = os.environ.get("SDIM_REFERENCE", "/root/reference")
+REF = os.environ.get("SDIM_REFERENCE", "")
 
 
 def _setup_paths():
+    if not REF or not (Path(REF) / "sdim").is_dir():
+        raise SystemExit("set SDIM_REFERENCE to the reference sdim source tree (the directory holding sdim/)")
     sys.dont_write_bytecode = True
     for p in (str(ROOT), REF, str(HERE / "_stubs")):
         if p not in sys.path:
