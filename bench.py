@@ -440,6 +440,28 @@ def read_traffic(name):
     return None
 
 
+def read_profile_value(name, key):
+    """A 'key: <number>' line of a committed ncu summary under profiles/, else None."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith(key + ":"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def philox_model_peak(num_sms, sm_mhz):
+    """Philox4x32-10 blocks/s the integer-multiply pipe allows: 20 wide
+    (32 x 32 -> 64-bit) multiplies per block, each taking two of the 64
+    32-bit multiply results an SM retires per clock, at the SM clock sampled
+    during the timed steps."""
+    return num_sms * 64 / (2 * 20) * sm_mhz * 1e6
+
+
 def hbm_peak():
     try:
         return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0)
@@ -470,7 +492,7 @@ class Timer:
     def run(self, steps, step_fn, clocks=None):
         torch = self.torch
         step_ms, kern_ms = [], []
-        self.stage_ms = []
+        self.stage_ms, self.pass_ms = [], []
         if self.ws > 1:
             self.dist.barrier()
         torch.cuda.synchronize()
@@ -486,6 +508,7 @@ class Timer:
             step_ms.append(e0.elapsed_time(e1))
             kern_ms.append(self.ctx.last_kernel_ms())
             self.stage_ms.append(self.ctx.last_stage_ms())
+            self.pass_ms.append(self.ctx.last_pass_ms())
         torch.cuda.synchronize()
         return step_ms, kern_ms, (clocks.stop() if clocks else None)
 
@@ -649,6 +672,7 @@ def run_single(args, torch, dist, ws, rank, local):
     ctx.sync()
     step_ms, kern_ms, clk = timer.run(args.steps, step, Clocks(local))
     stages = [statistics.mean(v) for v in zip(*timer.stage_ms)]
+    passes = [statistics.mean(v) for v in zip(*timer.pass_ms)]
     total_ms = timer.max_over_ranks(sum(step_ms))
     units_per_step = len(spec.ops) * shots
     value = units_per_step * ws * args.steps / (total_ms / 1e3)
@@ -726,6 +750,16 @@ def run_single(args, torch, dist, ws, rank, local):
         raise AssertionError("end-to-end records differ from the device-timed run")
     e2e_total = timer.max_over_ranks(sum(e2e_ms))
     e2e_value = units_per_step * ws * args.steps / (e2e_total / 1e3)
+    # the same call with the records staged in device memory and copied down
+    staged_ms = []
+    for k in range(args.warmup + min(args.steps, 5)):
+        t0 = time.perf_counter()
+        rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 0, shot0, shots, host.data_ptr(), _lib.FLAG_STAGE_HOST)
+        _lib.check(rc, ctx.ptr, "run")
+        if k >= args.warmup:
+            staged_ms.append((time.perf_counter() - t0) * 1e3)
+    if not np.array_equal(host[:, :nrec].numpy(), full):
+        raise AssertionError("staged end-to-end records differ from the device-timed run")
 
     if rank != 0:
         return None
@@ -765,8 +799,15 @@ def run_single(args, torch, dist, ws, rank, local):
         nn1_used = int((gids[:meas_at[-1]] == 17).sum()) if len(meas_at) else 0
         n_random = int((~det_row).sum())
         blocks = shots * (-(-nn1_used // 4) + n_random)
+        coin_blocks = shots * (-(-nn1_used // 32) * 8)
         prate = philox_peak(ctx)
         ach = blocks / (mean_kern / 1e3)
+        sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+        model = philox_model_peak(ctx.num_sms, sm_mhz)
+        issue_rate = ctx.num_sms * 4 * sm_mhz * 1e6  # warp instructions per second (4 schedulers per SM)
+        phase_instr = read_profile_value("trace_engine_surface_L7.md", "phase_pass_warp_instructions") \
+            if args.workload == "surface" else None
+        n_meas = int(np.isin(gids, (14, 15, 16)).sum())
         roofline = {"bound": "int-multiply (Philox4x32-10 blocks)", "achieved": ach / 1e9, "peak": prate / 1e9,
                     "unit": "Gblock/s", "frac": ach / prate,
                     "traffic": read_traffic("trace_engine_surface_L7.md") if args.workload == "surface" else None,
@@ -778,8 +819,37 @@ def run_single(args, torch, dist, ws, rank, local):
                                     "random-outcome blocks",
                     "kernel_ms": mean_kern,
                     "stages_ms": {"xz_pass_and_coin_pass": stages[0], "phase_pass": stages[1]},
+                    "peak_cross_check": {
+                        "value": model / 1e9, "unit": "Gblock/s", "probe_over_model": prate / model,
+                        "model": f"{ctx.num_sms} SMs x 64 32-bit multiplies per clock / (2 per wide multiply x "
+                                 "20 wide multiplies per Philox4x32-10 block) x the SM clock sampled in the timed "
+                                 "steps",
+                        "sm_mhz": sm_mhz},
+                    "kernels": {
+                        "coin_pass": {
+                            "ms": passes[1], "blocks": coin_blocks,
+                            "achieved": coin_blocks / (passes[1] / 1e3) / 1e9 if passes[1] else None,
+                            "peak": prate / 1e9, "unit": "Gblock/s",
+                            "frac": coin_blocks / (passes[1] / 1e3) / prate if passes[1] else None,
+                            "timed": "CUDA events around k_coin_pass on its own stream"},
+                        "xz_pass": {
+                            "ms": passes[0], "measurements": n_meas,
+                            "us_per_measurement": 1e3 * passes[0] / max(n_meas, 1),
+                            "bound": "latency: one CTA walks the layered schedule; barriers and dependent "
+                                     "shared-memory chains per measurement block",
+                            "timed": "CUDA events from the step's first kernel to the end of k_trace_pass"},
+                        "phase_pass": {
+                            "ms": stages[1], "warp_instructions": phase_instr,
+                            "issue_bound_ms": (1e3 * phase_instr / issue_rate) if phase_instr else None,
+                            "frac": (1e3 * phase_instr / issue_rate / stages[1]) if phase_instr else None,
+                            "issue_rate_warp_instr_per_s": issue_rate,
+                            "source": "warp instructions of one launch from ncu (smsp__inst_executed.sum, "
+                                      "profiles/trace_engine_surface_L7.md); issue rate = SMs x 4 schedulers x "
+                                      "the sampled SM clock"}},
                     "group_engine_model": group_model}
         roofline["hbm_view"] = hbm_view(roofline["traffic"], mean_kern)
+        roofline["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one step under ncu, read "
+                                      "from profiles/trace_engine_surface_L7.md (not measured in this run)")
     else:
         roofline = dict(group_model)
         roofline["traffic"] = None
@@ -796,6 +866,8 @@ def run_single(args, torch, dist, ws, rank, local):
             roofline = {"bound": f"smem (x/z pass, latency-bound on {sms} CTA{'s' if sms > 1 else ''})",
                         "achieved": xz_ach, "peak": share, "unit": "GB/s", "frac": xz_ach / share,
                         "traffic": read_traffic(f"trace_engine_{args.workload}.md"),
+                        "traffic_source": "DRAM bytes of one step under ncu, read from profiles/ (not measured "
+                                          "in this run)",
                         "kernel": f"{xz_kernel}<{d}> (x/z pass), then k_phase_pass_u8<{d}>",
                         "peak_source": f"sdim_probe_smem_bandwidth x {sms}/{ctx.num_sms} SMs",
                         "algorithmic_bytes_per_launch": per_shot_bytes,
@@ -813,7 +885,14 @@ def run_single(args, torch, dist, ws, rank, local):
         "shots_per_s": shots * ws * args.steps / (total_ms / 1e3),
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(dp.num_device_ops * 8),
-                "d2h_bytes_per_step": int(shots * nrec), "ms_per_step": e2e_total / args.steps},
+                "d2h_bytes_per_step": int(shots * nrec), "ms_per_step": e2e_total / args.steps,
+                "form": "sdim_run with a page-locked host record buffer: instruction stream copied up, records "
+                        "stored into host memory by the kernels (no device buffer, no copy down), wall clock "
+                        "per call",
+                "staged": {"value": units_per_step * len(staged_ms) / (sum(staged_ms) / 1e3), "unit": UNIT,
+                           "ms_per_step": statistics.mean(staged_ms),
+                           "form": "the same call with SDIM_FLAG_STAGE_HOST: records into device memory, "
+                                   "then one device-to-host copy"}},
         "plain_gpu": {"value": plain_rate, "unit": UNIT, "shots": pshots, "form": "one single-warp launch per shot"},
         "batched_vs_plain": value / plain_rate,
         "per_shot_engine": {

@@ -58,6 +58,9 @@ extern "C" {
                                       that do not fit one CTA in batches of fewer than 76 odd-d trace
                                       programs (larger batches use CTA pairs, then single CTAs streaming
                                       from global memory) */
+#define SDIM_FLAG_STAGE_HOST 8192u /* host outputs: stage records in device memory and copy them down
+                                      even when the host buffer is page-locked (by default the kernels
+                                      write page-locked host buffers directly, with no copy) */
 
 /* snapshot modes for sdim_snapshot */
 #define SDIM_SNAP_EVERY_INSTRUCTION 1
@@ -104,7 +107,10 @@ int sdim_circuit_destroy(sdim_circuit* circ);
 int sdim_circuit_info(const sdim_circuit* circ, int64_t info[8]);
 
 /* Runs shots [shot0, shot0 + nshots) of one program; out holds
- * nshots x records bytes (host memory unless SDIM_FLAG_OUT_DEVICE).
+ * nshots x records bytes (host memory unless SDIM_FLAG_OUT_DEVICE).  A
+ * page-locked host buffer (cudaHostAlloc / cudaMallocHost / sdim_host_alloc,
+ * or registered with cudaHostRegister) is written by the kernels directly;
+ * pageable host memory gets the records through a device buffer and a copy.
  * Replaces Program.simulate(shots, force_tableau=True) (sdim/program.py:206-267, 269-365). */
 int sdim_run(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot0, int64_t nshots,
              uint8_t* out, unsigned flags);
@@ -220,6 +226,11 @@ double sdim_last_kernel_ms(const sdim_ctx* ctx);
  * out[1] its phase passes, out[2] every other engine's kernels.  No
  * counterpart in the reference (its shot loop is not staged). */
 int sdim_last_stage_ms(const sdim_ctx* ctx, double out[3]);
+/* Two passes of that span timed by themselves: out[0] from the start of the
+ * kernels to the end of the last x / z pass (the coin pass runs alongside on
+ * another stream), out[1] the d = 2 coin pass alone (0 when none ran).  No
+ * counterpart in the reference. */
+int sdim_last_pass_ms(const sdim_ctx* ctx, double out[2]);
 
 /* Tableau export of one shot in the reference's int8 block order
  * x[n][n], z[n][n], phase[n], destab_x[n][n], destab_z[n][n], destab_phase[n]

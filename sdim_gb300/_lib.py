@@ -31,6 +31,7 @@ FLAG_NO_TRACE = 512
 FLAG_NO_COIN_PASS = 1024
 FLAG_SPLIT_XZ = 2048
 FLAG_CLUSTER_XZ = 4096
+FLAG_STAGE_HOST = 8192
 
 
 def engine_flags(engine) -> int:
@@ -71,6 +72,7 @@ SIGNATURES = {
     "sdim_host_free": (C.c_int, [_P]),
     "sdim_last_kernel_ms": (C.c_double, [_P]),
     "sdim_last_stage_ms": (C.c_int, [_P, _P]),
+    "sdim_last_pass_ms": (C.c_int, [_P, _P]),
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_probe_l2_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
@@ -175,6 +177,12 @@ class Context:
         """(x / z passes, phase passes, other engines) of the last timed call."""
         buf = (C.c_double * 3)()
         check(self.lib.sdim_last_stage_ms(self.ptr, buf), self.ptr, "sdim_last_stage_ms")
+        return tuple(float(v) for v in buf)
+
+    def last_pass_ms(self):
+        """(x / z passes alone, d = 2 coin pass alone) of the last timed call."""
+        buf = (C.c_double * 2)()
+        check(self.lib.sdim_last_pass_ms(self.ptr, buf), self.ptr, "sdim_last_pass_ms")
         return tuple(float(v) for v in buf)
 
     def sync(self):

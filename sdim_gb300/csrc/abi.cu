@@ -67,10 +67,14 @@ struct sdim_ctx {
   size_t staging_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev_xz = nullptr, ev_phase = nullptr;  // trace engine stage ends (SDIM_FLAG_TIME)
+  cudaEvent_t ev_xzo = nullptr;                      // end of the x / z passes alone
+  cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;      // coin pass start and end (on aux)
   bool timing_pending = false;
   bool stages_recorded = false;  // ev_xz / ev_phase belong to the pending span
+  bool coin_recorded = false;    // ev_c0 / ev_c1 belong to the pending span
   double last_ms = 0.0;
   double stage_ms[3] = {0.0, 0.0, 0.0};  // x / z passes, phase passes, other engines
+  double pass_ms[2] = {0.0, 0.0};        // x / z passes alone, coin pass alone
   int smem_attr_set[V_COUNT] = {};
   bool trace_smem_set = false;
   bool frame_smem_set = false;
@@ -264,16 +268,21 @@ int read_status(sdim_ctx* ctx) {
 
 // Kernel times of the last SDIM_FLAG_TIME call: the whole span and its stages.
 int collect_times(sdim_ctx* ctx) {
-  float all = 0.f, a = 0.f, b = 0.f, c = 0.f;
+  float all = 0.f, a = 0.f, b = 0.f, c = 0.f, xo = 0.f, co = 0.f;
   CK(cudaEventElapsedTime(&all, ctx->ev0, ctx->ev1));
   if (ctx->stages_recorded) {
     CK(cudaEventElapsedTime(&a, ctx->ev0, ctx->ev_xz));
     CK(cudaEventElapsedTime(&b, ctx->ev_xz, ctx->ev_phase));
     CK(cudaEventElapsedTime(&c, ctx->ev_phase, ctx->ev1));
+    CK(cudaEventElapsedTime(&xo, ctx->ev0, ctx->ev_xzo));
   } else {
     c = all;
   }
+  if (ctx->coin_recorded) CK(cudaEventElapsedTime(&co, ctx->ev_c0, ctx->ev_c1));
+  ctx->pass_ms[0] = xo;
+  ctx->pass_ms[1] = co;
   ctx->stages_recorded = false;
+  ctx->coin_recorded = false;
   ctx->last_ms = all;
   ctx->stage_ms[0] = a;
   ctx->stage_ms[1] = b;
@@ -296,6 +305,21 @@ int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
     if (trc != SDIM_OK) return trc;
   }
   return read_status(ctx);
+}
+
+// Device address through which the kernels can write the host buffer p
+// directly (page-locked memory: cudaHostAlloc, cudaMallocHost,
+// cudaHostRegister), or null for pageable memory and with
+// SDIM_FLAG_STAGE_HOST.  Records written this way reach the host with the
+// kernels' own stores, so no device-to-host copy follows.
+uint8_t* mapped_host(void* p, unsigned flags) {
+  if (!p || (flags & SDIM_FLAG_STAGE_HOST)) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer ? static_cast<uint8_t*>(a.devicePointer) : nullptr;
 }
 
 struct Job {
@@ -412,6 +436,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   const bool timed = flags & SDIM_FLAG_TIME;
   if (jobs.empty() && ujobs.empty()) {
     if (timed) {
+      CK(cudaEventRecord(ctx->ev_xzo, s));
       CK(cudaEventRecord(ctx->ev_xz, s));
       CK(cudaEventRecord(ctx->ev_phase, s));
       ctx->stages_recorded = true;
@@ -674,15 +699,21 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       CK(cudaEventRecord(ctx->ev_xzj[i], ctx->xzs[i]));
       CK(cudaStreamWaitEvent(s, ctx->ev_xzj[i], 0));
     }
+  if (timed) CK(cudaEventRecord(ctx->ev_xzo, s));
   // ---- coin pass on the second stream, alongside the x / z passes (independent work)
   if (coins) {
     CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
     const int block = 256;
     const long long grid = (coins + block - 1) / block;
     if (grid > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one coin pass");
+    if (timed) CK(cudaEventRecord(ctx->ev_c0, ctx->aux));
     launch_coin_pass((int)grid, block, kCoinFenceSmem, ctx->aux, dd, (int)k, coins);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "coin pass launch");
+    if (timed) {
+      CK(cudaEventRecord(ctx->ev_c1, ctx->aux));
+      ctx->coin_recorded = true;
+    }
     CK(cudaEventRecord(ctx->ev_join, ctx->aux));
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
   }
@@ -1174,6 +1205,8 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
       cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
       cudaEventCreate(&ctx->ev_xz) != cudaSuccess || cudaEventCreate(&ctx->ev_phase) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev_xzo) != cudaSuccess || cudaEventCreate(&ctx->ev_c0) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev_c1) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
@@ -1217,6 +1250,9 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaEventDestroy(ctx->ev1);
   cudaEventDestroy(ctx->ev_xz);
   cudaEventDestroy(ctx->ev_phase);
+  cudaEventDestroy(ctx->ev_xzo);
+  cudaEventDestroy(ctx->ev_c0);
+  cudaEventDestroy(ctx->ev_c1);
   cudaEventDestroy(ctx->ev_fork);
   cudaEventDestroy(ctx->ev_join);
   cudaEventDestroy(ctx->ev_xzf);
@@ -1367,19 +1403,21 @@ int sdim_run(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot0,
   if (nshots > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one call");
   CK(cudaSetDevice(ctx->device));
   const size_t bytes = (size_t)nshots * c->nmeas;
-  int rc = ensure(ctx, ctx->out, std::max<size_t>(bytes, 1));
+  uint8_t* direct = bytes ? mapped_host(out, flags) : nullptr;
+  int rc = direct ? SDIM_OK : ensure(ctx, ctx->out, std::max<size_t>(bytes, 1));
   if (rc != SDIM_OK) return rc;
   // host -> device: the program's instruction stream; device -> host: records
+  // (written into page-locked host memory by the kernels, else copied down)
   CK(cudaMemcpyAsync(c->d_ops, c->h_ops, (size_t)c->blob_words * sizeof(uint2), cudaMemcpyHostToDevice,
                      ctx->stream));
-  std::vector<Job> jobs{Job{c, seed, shot0, nshots, static_cast<uint8_t*>(ctx->out.p)}};
+  std::vector<Job> jobs{Job{c, seed, shot0, nshots, direct ? direct : static_cast<uint8_t*>(ctx->out.p)}};
   rc = launch_jobs(ctx, jobs, ctx->stream, flags & ~SDIM_FLAG_ASYNC);
   if (rc != SDIM_OK) return rc;
   if (flags & SDIM_FLAG_TIME) {
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->timing_pending = true;
   }
-  if (bytes) CK(cudaMemcpyAsync(out, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (bytes && !direct) CK(cudaMemcpyAsync(out, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->timing_pending) {
     const int trc = collect_times(ctx);
@@ -1477,9 +1515,17 @@ int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, c
     total += (size_t)nshots[i] * circs[i]->nmeas;
   }
   int rc;
-  if (!on_dev && (rc = ensure(ctx, ctx->out, std::max<size_t>(total, 1))) != SDIM_OK) return rc;
+  // host outputs in page-locked memory are written by the kernels directly
+  std::vector<uint8_t*> direct(ncirc, nullptr);
+  bool staged = false;
+  for (int i = 0; i < ncirc && !on_dev; ++i) {
+    if ((size_t)nshots[i] * circs[i]->nmeas == 0) continue;
+    direct[i] = mapped_host(outs[i], flags);
+    staged |= !direct[i];
+  }
+  if (staged && (rc = ensure(ctx, ctx->out, std::max<size_t>(total, 1))) != SDIM_OK) return rc;
   for (int i = 0; i < ncirc; ++i) {
-    uint8_t* o = on_dev ? outs[i] : static_cast<uint8_t*>(ctx->out.p) + offs[i];
+    uint8_t* o = on_dev ? outs[i] : direct[i] ? direct[i] : static_cast<uint8_t*>(ctx->out.p) + offs[i];
     jobs.push_back(Job{circs[i], seeds[i], shot0[i], nshots[i], o});
   }
   rc = launch_jobs(ctx, jobs, s, flags);
@@ -1491,7 +1537,8 @@ int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, c
   }
   for (int i = 0; i < ncirc; ++i) {
     const size_t b = (size_t)nshots[i] * circs[i]->nmeas;
-    if (b) CK(cudaMemcpyAsync(outs[i], static_cast<uint8_t*>(ctx->out.p) + offs[i], b, cudaMemcpyDeviceToHost, s));
+    if (b && !direct[i])
+      CK(cudaMemcpyAsync(outs[i], static_cast<uint8_t*>(ctx->out.p) + offs[i], b, cudaMemcpyDeviceToHost, s));
   }
   if (flags & SDIM_FLAG_ASYNC) {
     // the caller keeps the (pinned) host buffers alive until sdim_query / sdim_sync
@@ -1719,12 +1766,20 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
     offs[i] = total;
     total += (size_t)nshots[i] * circs[i].nmeas;
   }
-  if (!on_dev && (rc = ensure(ctx, ctx->out, std::max<size_t>(total, 1))) != SDIM_OK) return rc;
+  // host outputs in page-locked memory are written by the kernels directly
+  std::vector<uint8_t*> direct(ncirc, nullptr);
+  bool staged = false;
+  for (int i = 0; i < ncirc && !on_dev; ++i) {
+    if ((size_t)nshots[i] * circs[i].nmeas == 0) continue;
+    direct[i] = mapped_host(outs[i], flags);
+    staged |= !direct[i];
+  }
+  if (staged && (rc = ensure(ctx, ctx->out, std::max<size_t>(total, 1))) != SDIM_OK) return rc;
   std::vector<Job> jobs;
   jobs.reserve(ncirc);
   for (int i = 0; i < ncirc; ++i)
     jobs.push_back(Job{&circs[i], seeds[i], shot0[i], nshots[i],
-                       on_dev ? outs[i] : static_cast<uint8_t*>(ctx->out.p) + offs[i]});
+                       on_dev ? outs[i] : direct[i] ? direct[i] : static_cast<uint8_t*>(ctx->out.p) + offs[i]});
   rc = launch_jobs(ctx, jobs, s, flags);
   if (rc != SDIM_OK) return rc;
   if (on_dev) return finish(ctx, s, flags);
@@ -1734,7 +1789,8 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
   }
   for (int i = 0; i < ncirc; ++i) {
     const size_t b = (size_t)nshots[i] * circs[i].nmeas;
-    if (b) CK(cudaMemcpyAsync(outs[i], static_cast<uint8_t*>(ctx->out.p) + offs[i], b, cudaMemcpyDeviceToHost, s));
+    if (b && !direct[i])
+      CK(cudaMemcpyAsync(outs[i], static_cast<uint8_t*>(ctx->out.p) + offs[i], b, cudaMemcpyDeviceToHost, s));
   }
   if (flags & SDIM_FLAG_ASYNC) return SDIM_OK;
   CK(cudaStreamSynchronize(s));
@@ -1788,6 +1844,13 @@ double sdim_last_kernel_ms(const sdim_ctx* ctx) { return ctx ? ctx->last_ms : -1
 int sdim_last_stage_ms(const sdim_ctx* ctx, double out[3]) {
   if (!ctx || !out) return SDIM_EINVAL;
   for (int i = 0; i < 3; ++i) out[i] = ctx->stage_ms[i];
+  return SDIM_OK;
+}
+
+int sdim_last_pass_ms(const sdim_ctx* ctx, double out[2]) {
+  if (!ctx || !out) return SDIM_EINVAL;
+  out[0] = ctx->pass_ms[0];
+  out[1] = ctx->pass_ms[1];
   return SDIM_OK;
 }
 

@@ -309,3 +309,14 @@ def test_program_recompiles_after_pop_and_add_gate(monkeypatch):
     c.operations.pop()
     c.add_gate("M", 1000 % 3)
     assert prog.compile() is dp and _FakeDeviceProgram.made == 1000
+
+
+def test_header_flags_match_the_bindings():
+    """Every SDIM_FLAG_* of include/sdim_gb300.h has the same value in _lib."""
+    import re
+    from sdim_gb300 import _lib
+    text = (Path(__file__).resolve().parent.parent / "include" / "sdim_gb300.h").read_text()
+    flags = dict(re.findall(r"#define SDIM_FLAG_(\w+) (\d+)u", text))
+    assert len(flags) >= 14
+    for name, v in flags.items():
+        assert getattr(_lib, "FLAG_" + name) == int(v), name
