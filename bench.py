@@ -750,16 +750,17 @@ def run_single(args, torch, dist, ws, rank, local):
         raise AssertionError("end-to-end records differ from the device-timed run")
     e2e_total = timer.max_over_ranks(sum(e2e_ms))
     e2e_value = units_per_step * ws * args.steps / (e2e_total / 1e3)
-    # the same call with the records staged in device memory and copied down
+    # the same call with the kernels storing the records into the page-locked
+    # host buffer directly
     staged_ms = []
     for k in range(args.warmup + min(args.steps, 5)):
         t0 = time.perf_counter()
-        rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 0, shot0, shots, host.data_ptr(), _lib.FLAG_STAGE_HOST)
+        rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, 0, shot0, shots, host.data_ptr(), _lib.FLAG_DIRECT_HOST)
         _lib.check(rc, ctx.ptr, "run")
         if k >= args.warmup:
             staged_ms.append((time.perf_counter() - t0) * 1e3)
     if not np.array_equal(host[:, :nrec].numpy(), full):
-        raise AssertionError("staged end-to-end records differ from the device-timed run")
+        raise AssertionError("direct-store end-to-end records differ from the device-timed run")
 
     if rank != 0:
         return None
@@ -886,13 +887,12 @@ def run_single(args, torch, dist, ws, rank, local):
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(dp.num_device_ops * 8),
                 "d2h_bytes_per_step": int(shots * nrec), "ms_per_step": e2e_total / args.steps,
-                "form": "sdim_run with a page-locked host record buffer: instruction stream copied up, records "
-                        "stored into host memory by the kernels (no device buffer, no copy down), wall clock "
-                        "per call",
-                "staged": {"value": units_per_step * len(staged_ms) / (sum(staged_ms) / 1e3), "unit": UNIT,
-                           "ms_per_step": statistics.mean(staged_ms),
-                           "form": "the same call with SDIM_FLAG_STAGE_HOST: records into device memory, "
-                                   "then one device-to-host copy"}},
+                "form": "sdim_run into a page-locked host record buffer: instruction stream copied up, records "
+                        "into device memory, then one device-to-host copy; wall clock per call",
+                "direct_host": {"value": units_per_step * len(staged_ms) / (sum(staged_ms) / 1e3), "unit": UNIT,
+                                "ms_per_step": statistics.mean(staged_ms),
+                                "form": "the same call with SDIM_FLAG_DIRECT_HOST: the kernels store the records "
+                                        "into the host buffer directly, no copy"}},
         "plain_gpu": {"value": plain_rate, "unit": UNIT, "shots": pshots, "form": "one single-warp launch per shot"},
         "batched_vs_plain": value / plain_rate,
         "per_shot_engine": {

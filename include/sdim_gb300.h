@@ -58,9 +58,9 @@ extern "C" {
                                       that do not fit one CTA in batches of fewer than 76 odd-d trace
                                       programs (larger batches use CTA pairs, then single CTAs streaming
                                       from global memory) */
-#define SDIM_FLAG_STAGE_HOST 8192u /* host outputs: stage records in device memory and copy them down
-                                      even when the host buffer is page-locked (by default the kernels
-                                      write page-locked host buffers directly, with no copy) */
+#define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
+                                       into the host buffer directly, with no device buffer and no copy
+                                       (by default records go to device memory, then one copy down) */
 
 /* snapshot modes for sdim_snapshot */
 #define SDIM_SNAP_EVERY_INSTRUCTION 1
@@ -107,10 +107,11 @@ int sdim_circuit_destroy(sdim_circuit* circ);
 int sdim_circuit_info(const sdim_circuit* circ, int64_t info[8]);
 
 /* Runs shots [shot0, shot0 + nshots) of one program; out holds
- * nshots x records bytes (host memory unless SDIM_FLAG_OUT_DEVICE).  A
- * page-locked host buffer (cudaHostAlloc / cudaMallocHost / sdim_host_alloc,
- * or registered with cudaHostRegister) is written by the kernels directly;
- * pageable host memory gets the records through a device buffer and a copy.
+ * nshots x records bytes (host memory unless SDIM_FLAG_OUT_DEVICE).  The
+ * records go through a device buffer and one copy down; with
+ * SDIM_FLAG_DIRECT_HOST a page-locked host buffer (cudaHostAlloc /
+ * cudaMallocHost / sdim_host_alloc, or registered with cudaHostRegister) is
+ * written by the kernels directly.
  * Replaces Program.simulate(shots, force_tableau=True) (sdim/program.py:206-267, 269-365). */
 int sdim_run(sdim_ctx* ctx, const sdim_circuit* circ, uint64_t seed, int64_t shot0, int64_t nshots,
              uint8_t* out, unsigned flags);

@@ -31,7 +31,7 @@ FLAG_NO_TRACE = 512
 FLAG_NO_COIN_PASS = 1024
 FLAG_SPLIT_XZ = 2048
 FLAG_CLUSTER_XZ = 4096
-FLAG_STAGE_HOST = 8192
+FLAG_DIRECT_HOST = 8192
 
 
 def engine_flags(engine) -> int:

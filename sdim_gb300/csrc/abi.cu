@@ -307,13 +307,15 @@ int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
   return read_status(ctx);
 }
 
-// Device address through which the kernels can write the host buffer p
-// directly (page-locked memory: cudaHostAlloc, cudaMallocHost,
-// cudaHostRegister), or null for pageable memory and with
-// SDIM_FLAG_STAGE_HOST.  Records written this way reach the host with the
-// kernels' own stores, so no device-to-host copy follows.
+// With SDIM_FLAG_DIRECT_HOST: the device address through which the kernels
+// can write the host buffer p directly (page-locked memory: cudaHostAlloc,
+// cudaMallocHost, cudaHostRegister), or null for pageable memory.  Records
+// written this way reach the host with the kernels' own stores, so no
+// device-to-host copy follows.  Without the flag (null) they are staged in
+// device memory and copied down, which measured faster for the d = 2 trace
+// engine's record runs (0.67 against 0.95 ms for 38.5 MB of records).
 uint8_t* mapped_host(void* p, unsigned flags) {
-  if (!p || (flags & SDIM_FLAG_STAGE_HOST)) return nullptr;
+  if (!p || !(flags & SDIM_FLAG_DIRECT_HOST)) return nullptr;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();

@@ -50,6 +50,15 @@ struct ModU8 {
     else return x - (int)__umulhi((uint32_t)x, mu_ord) * ord;
   }
   __device__ __forceinline__ int neg(int x) const { return x ? d - x : 0; }
+  // dd + f (f - 1) / 2 x z, the term of one generator in the deterministic
+  // outcome's sum_i f_i (f_i - 1) / 2 (x_i . z_i): plain sums for d <= 7
+  // (at most 15 * 36 per term, so rows of thousands of terms stay far inside
+  // an int), reduced mod d otherwise
+  __device__ __forceinline__ int half_xz(int dd, int f, int x, int z) const {
+    const int h = (f * (f - 1)) >> 1;
+    if constexpr (DD > 0 && DD <= 7) return dd + h * x * z;
+    else return md(dd + md(h) * x * z);
+  }
   __device__ __forceinline__ int inv(int x) const {  // d prime, 0 < x < d
     int r = 1, b = x, e = d - 2;
     while (e > 0) {
@@ -267,30 +276,29 @@ struct EngineU8 {
     //         + phi^2 * sum_i (x_i . z_i) f_i (f_i - 1) / 2,   f_i = destab_x[q][i]
     for (int i = lane; i < n; i += 32) CX[i] = xq[n + i];
     __syncwarp();
+    // sum_i f_i ph_i here; the f_i (f_i - 1) / 2 (x_i . z_i) term is summed
+    // row by row in the cross-term pass below (one pass over the tableau)
     int pl = 0, dl = 0;
     for (int i = lane; i < n; i += 32) {
       const int f = CX[i];
-      if (!f) continue;
-      pl += f * PH[i];
-      if (M.d != 2) {
-        int cd = 0;
-        for (int k = 0; k < n; ++k) cd += X[(size_t)k * S + i] * Z[(size_t)k * S + i];
-        dl += M.md(M.md(cd) * ((f * (f - 1)) >> 1));
-      }
+      if (f) pl += f * PH[i];
     }
     int tl = 0;
     for (int k = lane; k < n; k += 32) {
       const uint8_t* xr = X + (size_t)k * S;
       const uint8_t* zr = Z + (size_t)k * S;
-      int pre = 0, acc = 0;
+      int pre = 0, acc = 0, dd = 0;
       for (int i = 0; i < n; ++i) {
         const int f = CX[i];
         if (f) {
-          acc = M.md(acc + f * xr[i] * pre);
-          pre = M.md(pre + f * zr[i]);
+          const int xv = xr[i], zv = zr[i];
+          acc = M.md(acc + f * xv * pre);
+          pre = M.md(pre + f * zv);
+          dd = M.half_xz(dd, f, xv, zv);
         }
       }
       tl += acc;
+      dl += M.md(dd);
     }
     const int P = M.mo(__reduce_add_sync(0xffffffffu, pl));
     const int T = M.md(__reduce_add_sync(0xffffffffu, tl));

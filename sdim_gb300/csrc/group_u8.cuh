@@ -401,16 +401,12 @@ struct TGroupU8 {
     for (int i = t; i < SlotU8::npad(n); i += size) CX[i] = i < n ? xq[n + i] : (uint8_t)0;
     if (ch == 0) shot_acc[s] = 0;
     tm.sync();
+    // sum_i f_i c_i here; the f_i (f_i - 1) / 2 (x_i . z_i) term is summed
+    // row by row in the cross-term pass below (one pass over the tableau)
     int pl = 0, dl = 0;
     for (int i = t; i < n; i += size) {
       const int f = CX[i];
-      if (!f) continue;
-      pl += f * C[i];
-      if (f > 1) {
-        int cd = 0;
-        for (int k = 0; k < n; ++k) cd += X[(size_t)k * S + i] * Z[(size_t)k * S + i];
-        dl += M.md(M.md(cd) * ((f * (f - 1)) >> 1));
-      }
+      if (f) pl += f * C[i];
     }
     // cross term: rows over threads, each row read as 32-bit words
     int tl = 0;
@@ -419,7 +415,7 @@ struct TGroupU8 {
     for (int k = t; k < n; k += size) {
       const uint32_t* xr = reinterpret_cast<const uint32_t*>(X + (size_t)k * S);
       const uint32_t* zr = reinterpret_cast<const uint32_t*>(Z + (size_t)k * S);
-      int pre = 0, acc = 0;
+      int pre = 0, acc = 0, dd = 0;
       for (int w = 0; w < nw; ++w) {
         const uint32_t fw = fq[w];
         if (!fw) continue;
@@ -428,12 +424,15 @@ struct TGroupU8 {
         for (int j = 0; j < 4; ++j) {
           const int f = (fw >> (8 * j)) & 0xff;
           if (f) {
-            acc = M.md(acc + f * (int)((xw >> (8 * j)) & 0xff) * pre);
-            pre = M.md(pre + f * (int)((zw >> (8 * j)) & 0xff));
+            const int xv = (int)((xw >> (8 * j)) & 0xff), zv = (int)((zw >> (8 * j)) & 0xff);
+            acc = M.md(acc + f * xv * pre);
+            pre = M.md(pre + f * zv);
+            dd = M.half_xz(dd, f, xv, zv);
           }
         }
       }
       tl += acc;
+      dl += M.md(dd);
     }
     // per shot: sum_i f_i delta_i over this thread's chunk
     int sacc = 0;

@@ -375,22 +375,18 @@ __device__ void cluster_measure(ClusterU8<DD, K, kStream>& e, const TraceDescU8&
     }
   } else if (e.stab) {
     // deterministic: this slice's partial sums to CTA 0
+    // sum_j f_j c_j here; the f_j (f_j - 1) / 2 (x_j . z_j) term of this
+    // slice is summed row by row in the cross-term pass below
     int pl_sum = 0, dl = 0;
     for (int j = t; j < nc; j += size) {
       const int fj = fb[j];
-      if (!fj) continue;
-      pl_sum += fj * Cp[j];
-      if (fj > 1) {
-        int cd = 0;
-        for (int k = 0; k < n; ++k) cd += X[(size_t)k * SL + j] * Z[(size_t)k * SL + j];
-        dl += M.md(M.md(cd) * ((fj * (fj - 1)) >> 1));
-      }
+      if (fj) pl_sum += fj * Cp[j];
     }
     int al = 0;
     const int nw = (nc + 3) >> 2;
     const uint32_t* fq = reinterpret_cast<const uint32_t*>(fb);
     for (int k = t; k < np; k += size) {  // Z_c[k] staged in CX, X_c[k] in CZ
-      int pre = 0, acc = 0, xs = 0;
+      int pre = 0, acc = 0, xs = 0, dd = 0;
       if (k < n) {
         const uint32_t* xr = reinterpret_cast<const uint32_t*>(X + (size_t)k * SL);
         const uint32_t* zr = reinterpret_cast<const uint32_t*>(Z + (size_t)k * SL);
@@ -402,10 +398,11 @@ __device__ void cluster_measure(ClusterU8<DD, K, kStream>& e, const TraceDescU8&
           for (int j = 0; j < 4; ++j) {
             const int fj = (fw >> (8 * j)) & 0xff;
             if (fj) {
-              const int xv = (int)((xw >> (8 * j)) & 0xff);
+              const int xv = (int)((xw >> (8 * j)) & 0xff), zv = (int)((zw >> (8 * j)) & 0xff);
               acc = M.md(acc + fj * xv * pre);
-              pre = M.md(pre + fj * (int)((zw >> (8 * j)) & 0xff));
+              pre = M.md(pre + fj * zv);
               xs = M.md(xs + fj * xv);
+              dd = M.half_xz(dd, fj, xv, zv);
             }
           }
         }
@@ -413,6 +410,7 @@ __device__ void cluster_measure(ClusterU8<DD, K, kStream>& e, const TraceDescU8&
       e.CX[k] = (uint8_t)pre;
       e.CZ[k] = (uint8_t)xs;
       al += acc;
+      dl += M.md(dd);
     }
     const int P = M.mo(e.tm.add(pl_sum));
     const int A = M.md(e.tm.add(al));

@@ -372,16 +372,12 @@ __device__ void split_measure(SplitU8<DD>& e, const TraceDescU8& td, int q, uint
     // deterministic: f from CTA 1, stabilizer columns here
     for (int i = t; i < np; i += size) e.CX[i] = i < n ? bf[i] : (uint8_t)0;
     e.tm.sync();
+    // sum_i f_i c_i here; the f_i (f_i - 1) / 2 (x_i . z_i) term is summed
+    // row by row in the cross-term pass below (one pass over the tableau)
     int pl = 0, dl = 0;
     for (int i = t; i < n; i += size) {
       const int f = e.CX[i];
-      if (!f) continue;
-      pl += f * C[i];
-      if (f > 1) {
-        int cd = 0;
-        for (int k = 0; k < n; ++k) cd += X[(size_t)k * SL + i] * Z[(size_t)k * SL + i];
-        dl += M.md(M.md(cd) * ((f * (f - 1)) >> 1));
-      }
+      if (f) pl += f * C[i];
     }
     int tl = 0;
     const int nw = (n + 3) >> 2;
@@ -389,7 +385,7 @@ __device__ void split_measure(SplitU8<DD>& e, const TraceDescU8& td, int q, uint
     for (int k = t; k < n; k += size) {
       const uint32_t* xr = reinterpret_cast<const uint32_t*>(X + (size_t)k * SL);
       const uint32_t* zr = reinterpret_cast<const uint32_t*>(Z + (size_t)k * SL);
-      int pre = 0, acc = 0;
+      int pre = 0, acc = 0, dd = 0;
       for (int w = 0; w < nw; ++w) {
         const uint32_t fw = fq[w];
         if (!fw) continue;
@@ -398,12 +394,15 @@ __device__ void split_measure(SplitU8<DD>& e, const TraceDescU8& td, int q, uint
         for (int j = 0; j < 4; ++j) {
           const int f = (fw >> (8 * j)) & 0xff;
           if (f) {
-            acc = M.md(acc + f * (int)((xw >> (8 * j)) & 0xff) * pre);
-            pre = M.md(pre + f * (int)((zw >> (8 * j)) & 0xff));
+            const int xv = (int)((xw >> (8 * j)) & 0xff), zv = (int)((zw >> (8 * j)) & 0xff);
+            acc = M.md(acc + f * xv * pre);
+            pre = M.md(pre + f * zv);
+            dd = M.half_xz(dd, f, xv, zv);
           }
         }
       }
       tl += acc;
+      dl += M.md(dd);
     }
     for (int g = t; g < sw; g += size) row[g] = g < n ? e.CX[g] : (uint8_t)0;
     const int P = M.mo(e.tm.add(pl));

@@ -38,7 +38,7 @@ import numpy as np
 from . import _lib
 from .circuit import Circuit
 from .encode import DeviceProgram, EncodedProgram, encode_program
-from .gatedata import RESET_ID
+from .gatedata import RESET_ID, GateData
 from .tableau import ExtendedTableau, MeasurementResult
 
 
@@ -106,6 +106,7 @@ class Program:
         self._ctx = None
         self._cache = {}
         self._last = None  # (seed, shot, noise) of the last simulated shot
+        self._applied: list = []  # instructions applied by apply_gate since then
 
     # ------------------------------------------------------------------
     @property
@@ -134,8 +135,14 @@ class Program:
         identities play no part, so a new instruction that reuses a freed
         object's address cannot alias an old one."""
         content = self._instruction_content
-        return (tuple((c.num_qudits, tuple([content(o) for o in c.operations])) for c in self.circuits),
+        circuits = self.circuits + ([self._applied_circuit()] if self._applied else [])
+        return (tuple((c.num_qudits, tuple([content(o) for o in c.operations])) for c in circuits),
                 bool(noise))
+
+    def _applied_circuit(self) -> Circuit:
+        c = Circuit(self.num_qudits, self.dimension)
+        c.operations = list(self._applied)
+        return c
 
     def compile(self, noise: bool = True) -> DeviceProgram:
         """Encoded program on the device (cached while the circuits' content
@@ -144,7 +151,9 @@ class Program:
         hit = self._cache.get(key[1])
         if hit is not None and hit[0] == key[0]:
             return hit[1]
-        enc = encode_program(self.circuits, self.num_qudits, self.dimension, noise=noise)
+        # apply_gate's instructions run after the circuits
+        circuits = self.circuits + ([self._applied_circuit()] if self._applied else [])
+        enc = encode_program(circuits, self.num_qudits, self.dimension, noise=noise)
         dp = DeviceProgram(self.context, enc)
         # keep the other noise setting only while it encodes the same circuits
         # (the frame route uses both)
@@ -252,6 +261,9 @@ class Program:
                                         show_gate, exact)
         shots = int(options.shots)
         s = self._seed(seed)
+        if self._applied:
+            self._applied = []
+            self._cache = {}
         frame = shots > 1 and not options.record_tableau and not options.force_tableau and not plain
         if frame:
             # the reference's frame route (sdim/program.py:244-265); verbose and
@@ -308,10 +320,48 @@ class Program:
         print(label, t, "\t", name, q, info)
 
     # ------------------------------------------------------------------
+    def apply_gate(self, instruc) -> Optional[MeasurementResult]:
+        """Applies one instruction to the current stabilizer tableau, as
+        sdim/program.py:367-385 does: the tableau after the last simulated
+        shot (the initial tableau before any), changed by every instruction
+        applied since.  Returns the MeasurementResult of M, M_X and RESET,
+        else None.
+
+        There is no host tableau here: the current state is the last shot
+        replayed on the GPU (same seed and shot index, so the same outcomes)
+        with the applied instructions appended, and its outcome stream
+        continues at the next measurement ordinal.  Each call replays the
+        whole program, so it is meant for stepping, not for throughput.
+        ``simulate`` starts afresh and drops the applied instructions."""
+        gid = getattr(instruc, "gate_id", None)
+        if gid is None or not 0 <= int(gid) <= 17:
+            raise ValueError("Invalid gate value")
+        q = int(instruc.qudit_index)
+        t = instruc.target_index
+        if not 0 <= q < self.num_qudits or (t is not None and not 0 <= int(t) < self.num_qudits):
+            raise IndexError("qudit index out of range")
+        if self._last is None:
+            self._last = (self._seed(None), 0, True)
+        # sdim/tableau/tableau_gates.py:331-346: applied alone, RESET only
+        # measures (the shot loop applies the X corrections), and N1 is the
+        # identity (sdim/program.py:31)
+        if int(gid) in (16, 17):
+            from .circuit import CircuitInstruction
+            instruc = CircuitInstruction(GateData(self.dimension), "M" if int(gid) == 16 else "I", q)
+        self._applied.append(instruc)
+        self._cache = {}
+        if int(gid) not in (14, 15, 16):
+            return None
+        s, shot, noise = self._last
+        dp = self.compile(noise)
+        _, rec = self.snapshot(s, max(shot, 0), _lib.SNAP_FINAL, noise)
+        v = int(rec[dp.num_records - 1])
+        return MeasurementResult(q, bool(v >> 7), v & 0x7F)
+
     @property
     def stabilizer_tableau(self) -> ExtendedTableau:
         """Final tableau of the last simulated shot (initial state before any run)."""
-        if self._last is None:
+        if self._last is None and not self._applied:
             return ExtendedTableau(self.num_qudits, self.dimension)
         s, shot, noise = self._last
         snaps, _ = self.snapshot(s, max(shot, 0), _lib.SNAP_FINAL, noise)

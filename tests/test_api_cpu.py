@@ -320,3 +320,21 @@ def test_header_flags_match_the_bindings():
     assert len(flags) >= 14
     for name, v in flags.items():
         assert getattr(_lib, "FLAG_" + name) == int(v), name
+
+
+def test_apply_gate_validates_before_any_device_call():
+    """Program.apply_gate raises ValueError for an unknown gate id and
+    IndexError for a qudit out of range (sdim/program.py:381-382; NumPy's
+    IndexError in the reference), without touching the device."""
+    from sdim_gb300 import Program
+    from sdim_gb300.circuit import CircuitInstruction
+    c = Circuit(2, 3)
+    c.add_gate("H", 0)
+    prog = Program(c)
+    bad = CircuitInstruction(c.gate_data, "H", 0)
+    bad.gate_id = 42
+    with pytest.raises(ValueError):
+        prog.apply_gate(bad)
+    with pytest.raises(IndexError):
+        prog.apply_gate(CircuitInstruction(c.gate_data, "CNOT", 0, 5))
+    assert prog._applied == [] and prog._ctx is None

@@ -1,10 +1,9 @@
 """GPU: records written straight into page-locked host memory.
 
-With a page-locked host output buffer the kernels store the records into it
-directly (no device buffer, no copy); with pageable memory, or with
-SDIM_FLAG_STAGE_HOST, they go through a device buffer and a copy.  Both
-routes must give the same records, bit for bit, for every engine, and equal
-the oracle."""
+With SDIM_FLAG_DIRECT_HOST and a page-locked host output buffer the kernels
+store the records into it directly (no device buffer, no copy); otherwise
+they go through a device buffer and a copy.  Both routes must give the same
+records, bit for bit, for every engine, and equal the oracle."""
 import numpy as np
 import pytest
 
@@ -34,14 +33,21 @@ def test_pinned_and_pageable_outputs_agree(spec, shots, engine):
     pageable = prog.sample(shots, seed=9, shot0=5, engine=engine)
     pinned = _pinned(pageable.shape)
     pinned.fill(0xEE)
-    prog.sample(shots, seed=9, shot0=5, engine=engine, out=pinned)
+    dp = prog.compile()
+    rc = prog.context.lib.sdim_run(prog.context.ptr, dp.ptr, 9, 5, shots, pinned.ctypes.data,
+                                   _lib.FLAG_DIRECT_HOST | _lib.engine_flags(engine))
+    _lib.check(rc, prog.context.ptr)
+    staged = _pinned(pageable.shape)
+    prog.sample(shots, seed=9, shot0=5, engine=engine, out=staged)
     assert np.array_equal(pageable, ref)
     assert np.array_equal(pinned, ref)
+    assert np.array_equal(staged, ref)
 
 
 def test_batch_mixes_pinned_and_pageable_outputs():
-    """One batch whose outputs are partly page-locked, partly pageable, and
-    the same batch staged through the device (SDIM_FLAG_STAGE_HOST)."""
+    """One batch whose outputs are partly page-locked, partly pageable, run
+    with SDIM_FLAG_DIRECT_HOST (the page-locked ones written directly), and
+    the same batch staged through the device."""
     specs = [workloads.random_hpc(12, 3, 60, seed=1), workloads.surface_memory(3, 2, prob=0.05),
              workloads.random_hpc(170, 5, 400, seed=2), workloads.random_hpc(30, 2, 100, seed=3)]
     shots = [33, 200, 20, 150]
@@ -54,8 +60,8 @@ def test_batch_mixes_pinned_and_pageable_outputs():
     for i, e in enumerate(br.entries):
         shape = (e.shots, e.program.num_records)
         outs.append(_pinned(shape) if i % 2 == 0 else np.empty(shape, dtype=np.uint8))
-    got = br.run(outs=outs)
-    staged = br.run(flags=_lib.FLAG_STAGE_HOST)
+    got = br.run(outs=outs, flags=_lib.FLAG_DIRECT_HOST)
+    staged = br.run()
     for g, st, r in zip(got, staged, refs):
         assert np.array_equal(g, r)
         assert np.array_equal(st, r)

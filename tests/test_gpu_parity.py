@@ -252,3 +252,44 @@ def test_simulate_follows_circuit_mutations_against_oracle():
         res = prog.simulate(shots=4, force_tableau=True, seed=100 + r)
         flat = [[m.measurement_value for m in rounds] for per_q in res for rounds in per_q]
         assert sum(len(f) for f in flat) == 4 * ref.shape[1]
+
+
+def test_apply_gate_continues_the_last_shot_against_oracle():
+    """apply_gate steps the tableau of the last simulated shot
+    (sdim/program.py:367-385): its measurement results and the resulting
+    stabilizer_tableau equal the oracle run of the program with the applied
+    instructions appended (RESET applied alone only measures, N1 is the
+    identity, as the reference's gate functions do)."""
+    from sdim_gb300 import Circuit
+    from sdim_gb300.circuit import CircuitInstruction
+    spec = workloads.random_hpc(5, 3, 40, seed=12)
+    c = spec.build()
+    prog = Program(c)
+    prog.simulate(shots=1, force_tableau=True, seed=77)
+    gd = c.gate_data
+    steps = [("H", 0, None), ("CNOT", 0, 2), ("M", 0, None), ("P", 2, None), ("RESET", 2, None),
+             ("N1", 1, None), ("M", 2, None), ("M_X", 1, None)]
+    extra = Circuit(5, 3)
+    got = []
+    for name, q, t in steps:
+        got.append(prog.apply_gate(CircuitInstruction(gd, name, q, t)))
+        ref_name = {"RESET": "M", "N1": "I"}.get(name, name)
+        if t is None:
+            extra.add_gate(ref_name, q)
+        else:
+            extra.add_gate(ref_name, q, t)
+    ref = oracle.simulate(oracle.OracleProgram([c, extra], 5, 3), 77, 0, 1, final=True)
+    recs = ref["records"][0]
+    meas = [r for r in got if r is not None]
+    assert [r.qudit_index for r in meas] == [0, 2, 2, 1]
+    assert [(int(r.measurement_value) | (int(r.deterministic) << 7)) for r in meas] == [int(v) for v in recs[-4:]]
+    assert [r is None for r in got] == [True, True, False, True, False, True, False, False]
+    snap, _ = prog.snapshot(77, 0, _lib.SNAP_FINAL)
+    assert np.array_equal(snap[0], ref["final"][0])
+    assert prog.stabilizer_tableau.x_block.shape == (5, 5)
+    # simulate starts afresh: the applied instructions are dropped
+    from sdim_gb300.encode import encode_program
+    from sdim_gb300.program import flatten_single_shot, records_to_nested
+    again = prog.simulate(shots=1, force_tableau=True, seed=77)
+    first = oracle.simulate(oracle.OracleProgram([c], 5, 3), 77, 0, 1)["records"]
+    assert again == flatten_single_shot(records_to_nested(first, encode_program([c], 5, 3), 5))
