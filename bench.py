@@ -76,8 +76,10 @@ def parse():
     ap.add_argument("--autotune", action="store_true",
                     help="uneven batch: also time the autotuner's batch-wide routes")
     ap.add_argument("--plain-shots", type=int, default=256)
+    ap.add_argument("--per-shot-leg", action="store_true",
+                    help="uneven batch: also time the per-shot engine on the whole batch (minutes)")
     ap.add_argument("--quick", action="store_true",
-                    help="single-program workloads: time the selected engine only (for profiling runs)")
+                    help="time the selected engine's step only, no other legs (for profiling runs)")
     ap.add_argument("--engine", default="auto", choices=["auto", "trace", "group", "per_shot"],
                     help="batched engine of the timed run (auto: the library's choice)")
     ap.add_argument("--route", default="tableau", choices=["tableau", "frame"],
@@ -985,10 +987,22 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
     value = units_per_step * ws * steps / (total_ms / 1e3)
     ref_out = out.cpu().numpy()
     _leg(f"uneven: {warmup} warm-up + {steps} timed steps", t_leg)
+    if args.quick:
+        # the timed step only (profiling runs): no other legs
+        if rank != 0:
+            return None
+        return {"value": value, "unit": UNIT, "steps": steps, "warmup": warmup, "ms_per_step": total_ms / steps,
+                "config": dict(uneven_config(items, ws), mode="quick: timed step only"),
+                "kernel_ms": statistics.mean(kern_ms),
+                "stages_ms": {"xz_pass_and_coin_pass": stages[0], "phase_pass": stages[1],
+                              "shot_group_engines": stages[2]},
+                "gpu_launches": steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),
+                "clocks": clk}
 
     ps = None
-    if not sub:
-        # the per-shot engine on the same batch
+    if not sub and args.per_shot_leg:
+        # the per-shot engine on the same batch (minutes: one warp walks each
+        # shot's whole tableau, up to 4 MB at n = 1024)
         t_leg = time.perf_counter()
         step(_lib.FLAG_PER_SHOT)
         ctx.sync()
