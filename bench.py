@@ -379,13 +379,30 @@ def _split_stride(c):
     return s if (s >> 2) & 1 else s + 4
 
 
-def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152):
+def p3_single_cta(n, smem_optin):
+    """Whether the d = 3 bit-plane x / z pass of n qudits keeps its tableau in
+    one CTA's shared memory: rows of W = 2 ceil(n / 32) plane pairs (8 bytes)
+    at an odd stride, a hot part of 3 W + 2 W / 2 + 512 pairs and two n-byte
+    columns, and a 4 KB instruction window."""
+    wh = (n + 31) // 32
+    w = 2 * wh
+    r16 = lambda x: (x + 15) & ~15  # noqa: E731
+    hot = r16((3 * w + 2 * wh + 512) * 8 + 2 * ((n + 15) & ~15))
+    xz = r16(2 * n * (w | 1) * 8)
+    return hot + xz + 4096 + 4096 <= smem_optin
+
+
+def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=5):
     """Where the library runs the odd-d x / z pass of n qudits, as (CTAs per
-    program, where its columns live: "smem", "l2" or "hbm").  One CTA when its
-    tableau fits in shared memory.  Else, in a batch of at least num_sms / 2
-    odd-d trace programs, a CTA pair when that fits and one CTA streaming from
-    HBM above; in a smaller batch a cluster of 8 CTAs, columns in shared
-    memory up to n = 636 and streamed from global memory, held in L2, above."""
+    program, where its columns live: "smem", "l2" or "hbm").  For d = 3 one
+    CTA on the bit-plane tableau, in shared memory when it fits, else
+    streamed from HBM.  For other d one CTA when its byte tableau fits in
+    shared memory.  Else, in a batch of at least num_sms / 2 odd-d trace
+    programs, a CTA pair when that fits and one CTA streaming from HBM above;
+    in a smaller batch a cluster of 8 CTAs, columns in shared memory up to
+    n = 636 and streamed from global memory, held in L2, above."""
+    if d == 3:
+        return 1, ("smem" if p3_single_cta(n, smem_optin) else "hbm")
     if u8_single_cta(n, smem_optin):
         return 1, "smem"
     r16 = lambda x: (x + 15) & ~15  # noqa: E731
@@ -406,7 +423,7 @@ def tableau_place(n, d, on_trace, smem_optin, odd_trace_programs=1, num_sms=152)
     planes for d = 2 and the odd-d shot-group engine on one CTA, the odd-d
     trace pass as u8_xz_layout places it."""
     if on_trace and d != 2:
-        return u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms)[1]
+        return u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms, d)[1]
     tab = 2 * n * (-(-2 * n // 8) if d == 2 else 2 * n)
     return "smem" if tab <= smem_optin - 16384 else "hbm"
 
@@ -862,10 +879,11 @@ def run_single(args, torch, dist, ws, rank, local):
             # against the share of the measured shared-memory bandwidth of the
             # SMs it runs on
             xz_ms = stages[0]
-            sms, _ = u8_xz_layout(n, 1, ctx.smem_optin, ctx.num_sms)
+            sms, _ = u8_xz_layout(n, 1, ctx.smem_optin, ctx.num_sms, d)
             share = peak * sms / ctx.num_sms
             xz_ach = per_shot_bytes / (xz_ms / 1e3) / 1e9
-            xz_kernel = {1: "k_trace_pass_u8", 2: "k_trace_pass_split", 8: "k_trace_pass_cluster"}[sms]
+            xz_kernel = {1: "k_trace_pass_p3" if d == 3 else "k_trace_pass_u8", 2: "k_trace_pass_split",
+                         8: "k_trace_pass_cluster"}[sms]
             roofline = {"bound": f"smem (x/z pass, latency-bound on {sms} CTA{'s' if sms > 1 else ''})",
                         "achieved": xz_ach, "peak": share, "unit": "GB/s", "frac": xz_ach / share,
                         "traffic": read_traffic(f"trace_engine_{args.workload}.md"),

@@ -58,6 +58,8 @@ extern "C" {
                                       that do not fit one CTA in batches of fewer than 76 odd-d trace
                                       programs (larger batches use CTA pairs, then single CTAs streaming
                                       from global memory) */
+#define SDIM_FLAG_U8_XZ 16384u /* odd-d trace engine, d = 3: x / z pass on residue bytes (the forms of
+                                 d = 5, 7) instead of the two-bit-plane tableau */
 #define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
                                        into the host buffer directly, with no device buffer and no copy
                                        (by default records go to device memory, then one copy down) */
@@ -185,15 +187,17 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
                     const int64_t* shot0, const int64_t* nshots, uint8_t* const* outs, void* stream,
                     unsigned flags);
 /* The form the odd-d trace engine's x / z pass takes for a program of n
- * qudits in a run with odd_trace_programs odd-d trace programs, on a device
- * with smem_optin bytes of opt-in shared memory per block and num_sms SMs:
- * 0 one CTA, tableau in shared memory; 1 a CTA pair; 2 one CTA, tableau in
- * global memory; 3 a cluster of 8 CTAs, columns in shared memory; 4 the
- * cluster, columns in global memory.  Host-only (no device is touched), so
+ * qudits and odd prime dimension d in a run with odd_trace_programs odd-d
+ * trace programs, on a device with smem_optin bytes of opt-in shared memory
+ * per block and num_sms SMs: 0 one CTA, byte tableau in shared memory; 1 a
+ * CTA pair; 2 one CTA, byte tableau in global memory; 3 a cluster of 8
+ * CTAs, columns in shared memory; 4 the cluster, columns in global memory;
+ * 5 (d = 3) one CTA, bit-plane tableau in shared memory; 6 (d = 3) one CTA,
+ * bit-plane tableau in global memory.  Host-only (no device is touched), so
  * callers such as a roofline model can mirror the library's routing.
- * SDIM_EINVAL for n outside [1, 2048] or non-positive sizes.  No
+ * SDIM_EINVAL for n outside [1, 2048], an even d or non-positive sizes.  No
  * counterpart in the reference. */
-int sdim_trace_xz_mode(int32_t n, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
+int sdim_trace_xz_mode(int32_t n, int32_t d, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
                        int32_t num_sms);
 /* Measured shared-memory read bandwidth of the device in GB/s (all SMs):
  * the roofline denominator for tableaux resident in shared memory.  No

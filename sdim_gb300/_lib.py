@@ -32,6 +32,7 @@ FLAG_NO_COIN_PASS = 1024
 FLAG_SPLIT_XZ = 2048
 FLAG_CLUSTER_XZ = 4096
 FLAG_DIRECT_HOST = 8192
+FLAG_U8_XZ = 16384
 
 
 def engine_flags(engine) -> int:
@@ -76,7 +77,7 @@ SIGNATURES = {
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_probe_l2_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
-    "sdim_trace_xz_mode": (C.c_int, [C.c_int32, C.c_int64, C.c_uint, C.c_int32, C.c_int32]),
+    "sdim_trace_xz_mode": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_uint, C.c_int32, C.c_int32]),
     "sdim_probe_philox_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_graph_create": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, C.c_uint, C.POINTER(_P)]),
     "sdim_graph_launch": (C.c_int, [_P, _P, _P, _P]),

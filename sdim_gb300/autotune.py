@@ -10,9 +10,9 @@ fastest.  Its knobs:
   tableaux per CTA) or one per CTA, or one warp per shot;
 * residency: tableaux in shared memory where they fit, or in global memory
   (``FLAG_FORCE_GMEM``);
-* the odd-d x / z pass form: one CTA, a CTA pair, an eight-CTA cluster
-  (``sdim_trace_xz_mode`` tells which flags change the form, so equal forms
-  are timed once);
+* the odd-d x / z pass form: one CTA, a CTA pair, an eight-CTA cluster, and
+  for d = 3 the bit-plane tableau or residue bytes (``sdim_trace_xz_mode``
+  tells which flags change the form, so equal forms are timed once);
 * for d = 2 the N1 coins in their own pass or inside the phase pass.
 
 Rows in flight per thread are fixed per kernel form at compile time (16 for a
@@ -61,7 +61,7 @@ PER_SHOT_MAX_SHOTS = 64
 TUNE_MAX_SHOTS = 1 << 17
 
 _XZ_FORM = {0: "one CTA", 1: "CTA pair", 2: "one CTA, global memory", 3: "8-CTA cluster",
-            4: "8-CTA cluster, global memory"}
+            4: "8-CTA cluster, global memory", 5: "one CTA, bit planes", 6: "one CTA, bit planes in global memory"}
 
 
 @dataclass(frozen=True)
@@ -87,8 +87,8 @@ class TuneResult:
                    list(obj.get("aborted", [])))
 
 
-def _xz_mode(n: int, programs: int, flags: int, smem_optin: int, num_sms: int) -> int:
-    rc = _lib.load().sdim_trace_xz_mode(int(n), int(programs), int(flags), int(smem_optin), int(num_sms))
+def _xz_mode(n: int, d: int, programs: int, flags: int, smem_optin: int, num_sms: int) -> int:
+    rc = _lib.load().sdim_trace_xz_mode(int(n), int(d), int(programs), int(flags), int(smem_optin), int(num_sms))
     if rc < 0:
         raise ValueError(f"no odd-d x / z pass form for n = {n}")
     return rc
@@ -104,10 +104,11 @@ def program_candidates(d: int, n: int, shots: int, smem_optin: int, num_sms: int
             out.append(Candidate("trace, coins in the phase pass", _lib.FLAG_TRACE | _lib.FLAG_NO_COIN_PASS))
             out.append(Candidate("trace, global memory", _lib.FLAG_TRACE | _lib.FLAG_FORCE_GMEM))
         else:
-            seen = {_xz_mode(n, 1, 0, smem_optin, num_sms)}
+            seen = {_xz_mode(n, d, 1, 0, smem_optin, num_sms)}
             for extra in (_lib.FLAG_SPLIT_XZ, _lib.FLAG_CLUSTER_XZ, _lib.FLAG_FORCE_GMEM,
-                          _lib.FLAG_CLUSTER_XZ | _lib.FLAG_FORCE_GMEM):
-                mode = _xz_mode(n, 1, extra, smem_optin, num_sms)
+                          _lib.FLAG_CLUSTER_XZ | _lib.FLAG_FORCE_GMEM, _lib.FLAG_U8_XZ,
+                          _lib.FLAG_U8_XZ | _lib.FLAG_FORCE_GMEM):
+                mode = _xz_mode(n, d, 1, extra, smem_optin, num_sms)
                 if mode not in seen:
                     seen.add(mode)
                     out.append(Candidate(f"trace, x/z pass on {_XZ_FORM[mode]}", _lib.FLAG_TRACE | extra))
@@ -129,6 +130,7 @@ def batch_candidates() -> List[Candidate]:
             Candidate("shot groups only", _lib.FLAG_NO_TRACE),
             Candidate("odd-d x/z passes on CTA pairs", _lib.FLAG_SPLIT_XZ),
             Candidate("odd-d x/z passes on 8-CTA clusters", _lib.FLAG_CLUSTER_XZ),
+            Candidate("d = 3 x/z passes on residue bytes", _lib.FLAG_U8_XZ),
             Candidate("d=2 coins in the phase pass", _lib.FLAG_NO_COIN_PASS)]
 
 

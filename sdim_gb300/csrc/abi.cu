@@ -402,12 +402,17 @@ constexpr int kTraceU8MaxQudits = 2048;
 // generator columns (trace_split_u8.cuh) when that fits, else 2, one CTA
 // with the tableau in global memory.  In a smaller batch, for latency: a
 // cluster of kTraceClusterCtas CTAs (trace_cluster_u8.cuh) with its columns
-// in shared memory (3) or global memory (4).  A cluster shares each
+// in shared memory (3) or global memory (4).  For d = 3 (unless
+// SDIM_FLAG_U8_XZ, SDIM_FLAG_SPLIT_XZ or SDIM_FLAG_CLUSTER_XZ names a byte
+// form) one CTA on the bit-plane tableau (trace_p3.cuh), in shared memory (5)
+// up to n = 448 on GB300, else in a global-memory slot (6).  A cluster shares each
 // measurement's fixed cost (two cluster barriers, pivot search, broadcast)
 // among 8 SMs, so it finishes one program sooner but a full batch later.
-int odd_xz_mode(int n, long long programs, unsigned flags, size_t optin, int num_sms) {
+int odd_xz_mode(int n, int d, long long programs, unsigned flags, size_t optin, int num_sms) {
   const size_t win = trace_u8_window_bytes();
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
+  if (d == 3 && !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ)))
+    return !force_gmem && trace_p3_hot_bytes(n) + trace_p3_xz_bytes(n) + win + 4096 <= optin ? 5 : 6;
   const bool few = programs * 2 < (long long)num_sms;
   const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
   const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
@@ -450,6 +455,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   if (!ctx->trace_smem_set) {
     cudaError_t e = trace_set_smem(ctx->smem_optin);
     if (e == cudaSuccess) e = trace_u8_set_smem(ctx->smem_optin);
+    if (e == cudaSuccess) e = trace_p3_set_smem(ctx->smem_optin);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFuncSetAttribute");
     ctx->trace_smem_set = true;
   }
@@ -625,7 +631,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   // odd d: the x / z pass form of each program (odd_xz_mode)
   const size_t optin = (size_t)ctx->smem_optin;
   const size_t win = trace_u8_window_bytes();
-  auto xz_mode = [&](int n) { return odd_xz_mode(n, (long long)ku, flags, optin, ctx->num_sms); };
+  auto xz_mode = [&](int n, int d) { return odd_xz_mode(n, d, (long long)ku, flags, optin, ctx->num_sms); };
   // clusters of a mode-4 run: one per kTraceClusterCtas SMs, each CTA alone
   // on its SM, so the programs in flight keep their columns in L2
   auto stream_clusters = [&](size_t programs) {
@@ -638,13 +644,16 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   size_t slot_total = 0;
   for (size_t b = 0; b < ku;) {
     const int v = trace_u8_variant(hu[b].c.d);
-    const int mode = xz_mode(hu[b].c.n);
+    const int mode = xz_mode(hu[b].c.n, hu[b].c.d);
     size_t e = b;
-    while (e < ku && trace_u8_variant(hu[e].c.d) == v && xz_mode(hu[e].c.n) == mode) ++e;
+    while (e < ku && trace_u8_variant(hu[e].c.d) == v && xz_mode(hu[e].c.n, hu[e].c.d) == mode) ++e;
     runs.push_back(Run{b, e, v, mode, slot_total});
     if (mode == 2) {
       const size_t grid = std::min<size_t>(e - b, 2 * (size_t)ctx->num_sms);
       slot_total += trace_u8_xz_bytes(hu[b].c.n) * grid;
+    } else if (mode == 6) {
+      const size_t grid = std::min<size_t>(e - b, 2 * (size_t)ctx->num_sms);
+      slot_total += trace_p3_xz_bytes(hu[b].c.n) * grid;
     } else if (mode == 4) {
       slot_total += trace_u8_cluster_xz(hu[b].c.n) * kTraceClusterCtas * stream_clusters(e - b);
     }
@@ -670,7 +679,16 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       used[si] = true;
     }
     const int nmax = hu[b].c.n;
-    if (mode == 1) {
+    if (mode >= 5) {
+      // d = 3 on bit planes: one CTA per program, largest first
+      const bool in_smem = mode == 5;
+      const size_t hot = trace_p3_hot_bytes(nmax), xz = trace_p3_xz_bytes(nmax);
+      int grid = (int)std::min<size_t>(e - b, 65535);
+      if (!in_smem) grid = std::min(grid, 2 * ctx->num_sms);
+      unsigned* queue = in_smem ? nullptr : static_cast<unsigned*>(ctx->xz_queue.p) + r;
+      launch_trace_p3(grid, hot + (in_smem ? xz : 0) + win, rs, du + b, (int)(e - b),
+                      static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, queue, status);
+    } else if (mode == 1) {
       launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax) + win,
                             trace_u8_split_smem(nmax), rs, du + b, (int)(e - b), status);
     } else if (mode >= 3) {
@@ -1118,11 +1136,12 @@ void append_frame_ops(const int32_t* ops, int64_t nops, const double* noise_prob
 
 extern "C" {
 
-int sdim_trace_xz_mode(int32_t n, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
+int sdim_trace_xz_mode(int32_t n, int32_t d, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
                        int32_t num_sms) {
-  if (n < 1 || n > kTraceU8MaxQudits || odd_trace_programs < 0 || smem_optin <= 0 || num_sms <= 0)
+  if (n < 1 || n > kTraceU8MaxQudits || d < 3 || !(d & 1) || odd_trace_programs < 0 || smem_optin <= 0 ||
+      num_sms <= 0)
     return SDIM_EINVAL;
-  return odd_xz_mode(n, (long long)odd_trace_programs, flags, (size_t)smem_optin, num_sms);
+  return odd_xz_mode(n, d, (long long)odd_trace_programs, flags, (size_t)smem_optin, num_sms);
 }
 
 int sdim_probe_smem_bandwidth(sdim_ctx* ctx, double* gbs) {

@@ -1,0 +1,56 @@
+// x / z pass of the odd-d trace engine for d = 3 on bit planes
+// (trace_p3.cuh): one program per CTA, the tableau in shared memory when it
+// fits (n <= 448 on GB300), else in a global-memory slot per CTA with the
+// CTAs taking programs, largest first, from an atomic counter.
+#include "trace_p3.cuh"
+
+namespace sdim {
+namespace {
+
+__global__ void __launch_bounds__(kP3Threads, 2) k_trace_pass_p3(const TraceDescU8* __restrict__ descs, int ndesc,
+                                                              uint8_t* gxz, size_t xz_bytes, size_t hot_bytes,
+                                                              int xz_in_smem, unsigned* queue, int* status) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int red[40];
+  __shared__ int next;
+  uint8_t* hot = smem;
+  uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
+  uint2* win = reinterpret_cast<uint2*>(smem + hot_bytes + (xz_in_smem ? xz_bytes : 0));
+  int i = blockIdx.x;
+  if (queue) {
+    if (threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
+    __syncthreads();
+    i = next;
+  }
+  while (i < ndesc) {
+    const TraceDescU8 td = descs[i];
+    TabP3 e(xz, hot, td.c.n, CtaTeam(red));
+    trace_program_p3(td, e, win, status);
+    __syncthreads();
+    if (queue) {
+      if (threadIdx.x == 0) next = (int)atomicAdd(queue, 1u);
+      __syncthreads();
+      i = next;
+    } else {
+      i += gridDim.x;
+    }
+  }
+}
+
+size_t round16p(size_t b) { return (b + 15) & ~(size_t)15; }
+
+}  // namespace
+
+size_t trace_p3_hot_bytes(int n) { return round16p(P3Layout(n).hot_bytes()); }
+size_t trace_p3_xz_bytes(int n) { return round16p(P3Layout(n).xz_bytes()); }
+
+cudaError_t trace_p3_set_smem(int optin) {
+  return cudaFuncSetAttribute(k_trace_pass_p3, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
+void launch_trace_p3(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
+                     size_t hot, int in_smem, unsigned* queue, int* status) {
+  k_trace_pass_p3<<<grid, kP3Threads, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, queue, status);
+}
+
+}  // namespace sdim

@@ -197,4 +197,15 @@ void launch_trace_u8_cluster(int variant, int clusters, size_t smem, cudaStream_
 void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
                            int nd, long long total, int* status);
 
+// x / z pass for d = 3 on bit planes (k_trace_p3.cu): one CTA of 512
+// threads per program, x / z in shared memory after the hot part when
+// in_smem, else at gxz + blockIdx.x * xzb with programs taken from queue;
+// the instruction window (trace_u8_window_bytes) follows in shared memory.
+// Writes the same trace as the byte-residue passes.
+size_t trace_p3_hot_bytes(int n);
+size_t trace_p3_xz_bytes(int n);
+cudaError_t trace_p3_set_smem(int optin);
+void launch_trace_p3(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
+                     size_t hot, int in_smem, unsigned* queue, int* status);
+
 }  // namespace sdim

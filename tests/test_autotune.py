@@ -38,8 +38,12 @@ def test_odd_d_xz_forms_are_deduplicated_by_the_library_query():
     assert forms == ["trace, x/z pass on CTA pair", "trace, x/z pass on one CTA, global memory",
                      "trace, x/z pass on 8-CTA cluster, global memory"]
     # n = 100 fits one CTA: every override is a different form
-    small = [x for x in _names(autotune.program_candidates(3, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
+    small = [x for x in _names(autotune.program_candidates(5, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
     assert len(small) == 4
+    # d = 3 runs on bit planes by default; the byte forms are six more
+    d3 = [x for x in _names(autotune.program_candidates(3, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
+    assert len(d3) == 6 and "trace, x/z pass on one CTA" in d3
+    assert "trace, x/z pass on one CTA, bit planes in global memory" in d3
     # past the odd-d trace engine's limit only the group engines remain
     big = _names(autotune.program_candidates(5, 2049, 64, OPTIN, SMS))
     assert not any(x.startswith("trace") for x in big)
