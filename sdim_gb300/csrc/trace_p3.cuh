@@ -224,8 +224,9 @@ __device__ void trace_measure_p3(TabP3& e, const TraceDescU8& td, int q, uint32_
     const int phc = p3_get(C[wp], lp);
     e.tm.sync();
     e.row_bytes(e.FW, 0, 2 * n, row, sw);
-    // rank-1 update of X and Z and the column dots, (word, row group) threads
-    const int W = L.W, R = kP3Threads / W > 0 ? min(size, kP3Threads) / W : 1;
+    // rank-1 update of X and Z and the column dots, (word, row group) threads;
+    // at least four rows per group, so that few partial dots are summed
+    const int W = L.W, R = max(1, min(min(size, kP3Threads) / W, (n + 3) >> 2));
     if (t < R * W) {
       const int w = t % W, r = t / W;
       const P3 f1 = e.FW[w], f2 = p3_neg(f1);
