@@ -496,7 +496,10 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       size_t e = b;
       long long shots = 0;
       while (e < k && trace_words(jobs[e].c->n) == tw) shots += jobs[e++].nshots;
-      for (size_t i = b; i < e; ++i) spl[i] = shots >= kPhasePairMinShots ? 2 : 1;
+      int sp = shots >= kPhasePairMinShots ? (tw <= kPhaseQuadMaxWords ? 4 : 2) : 1;
+      if (flags & SDIM_FLAG_LANE_SHOTS_2) sp = std::min(sp, 2);
+      if (flags & SDIM_FLAG_LANE_SHOTS_1) sp = 1;
+      for (size_t i = b; i < e; ++i) spl[i] = sp;
       b = e;
     }
     long long groups = 0;

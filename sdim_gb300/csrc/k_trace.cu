@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
 // registers.  Up to 16-word rows and one shot per lane, 32 blocks per SM at
 // 64 registers; wider rows or two shots per lane get 128.
 template <int TW, int SPL>
-__global__ void __launch_bounds__(32, (TW >= 16 || SPL == 2) ? 16 : 32)
+__global__ void __launch_bounds__(32, SPL == 4 ? 12 : (TW >= 16 || SPL == 2) ? 16 : 32)
     k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc, long long total_groups, const int* status) {
   __shared__ uint8_t rec[32 * SPL * kRecStride];
   if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
@@ -40,13 +40,13 @@ __global__ void __launch_bounds__(32, (TW >= 16 || SPL == 2) ? 16 : 32)
   if (g >= total_groups) return;
   const int i = find_trace_desc(descs, ndesc, g);
   const long long lg = g - descs[i].c.item_begin;
-  if constexpr (SPL == 2) {
+  if constexpr (SPL >= 2) {
     if (descs[i].masks) {
-      phase_program_pair<TW>(descs + i, lg, threadIdx.x, rec);
-    } else {  // no masks: the two 32-shot halves one after the other
-      phase_program<TW, false>(descs + i, 2 * lg, threadIdx.x, rec);
-      if ((2 * lg + 1) * 32 < (long long)descs[i].c.nshots)
-        phase_program<TW, false>(descs + i, 2 * lg + 1, threadIdx.x, rec);
+      phase_program_multi<TW, SPL>(descs + i, lg, threadIdx.x, rec);
+    } else {  // no masks: the 32-shot parts one after the other
+      for (int h = 0; h < SPL; ++h)
+        if ((SPL * lg + h) * 32 < (long long)descs[i].c.nshots)
+          phase_program<TW, false>(descs + i, SPL * lg + h, threadIdx.x, rec);
     }
   } else {
     if (descs[i].masks)
@@ -129,8 +129,21 @@ bool launch_phase_spl(int tw, int grid, int block, cudaStream_t s, const TraceDe
   }
 }
 
+// Four shots per lane for trace rows of up to 8 words (the deltas of four
+// shots stay in registers).
+bool launch_phase_quad(int tw, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
+                       long long total_groups, int* status) {
+  switch (tw) {
+    case 2: k_phase_pass<2, 4><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    case 4: k_phase_pass<4, 4><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    case 8: k_phase_pass<8, 4><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+    default: return false;
+  }
+}
+
 bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        long long total_groups, int* status) {
+  if (spl == 4) return launch_phase_quad(tw, grid, block, s, descs, ndesc, total_groups, status);
   return spl == 2 ? launch_phase_spl<2>(tw, grid, block, s, descs, ndesc, total_groups, status)
                   : launch_phase_spl<1>(tw, grid, block, s, descs, ndesc, total_groups, status);
 }

@@ -3,6 +3,7 @@
 // fits (n <= 448 on GB300), else in a global-memory slot per CTA with the
 // CTAs taking programs, largest first, from an atomic counter.
 #include "trace_p3.cuh"
+#include "variants.cuh"
 
 namespace sdim {
 namespace {
@@ -37,16 +38,12 @@ __global__ void __launch_bounds__(kP3Threads, 2) k_trace_pass_p3(const TraceDesc
   }
 }
 
-size_t round16p(size_t b) { return (b + 15) & ~(size_t)15; }
-
 }  // namespace
 
-size_t trace_p3_hot_bytes(int n) { return round16p(P3Layout(n).hot_bytes()); }
-size_t trace_p3_xz_bytes(int n) { return round16p(P3Layout(n).xz_bytes()); }
+size_t trace_p3_hot_bytes(int n) { return round16(P3Layout(n).hot_bytes()); }
+size_t trace_p3_xz_bytes(int n) { return round16(P3Layout(n).xz_bytes()); }
 
-cudaError_t trace_p3_set_smem(int optin) {
-  return cudaFuncSetAttribute(k_trace_pass_p3, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-}
+cudaError_t trace_p3_set_smem(int optin) { return set_dynamic_smem(k_trace_pass_p3, optin); }
 
 void launch_trace_p3(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
                      size_t hot, int in_smem, unsigned* queue, int* status) {

@@ -154,15 +154,18 @@ void launch_coin_pass(int grid, int block, size_t smem, cudaStream_t s, const Tr
 // shared memory so that no coin block lands beside them.
 constexpr size_t kCoinFenceSmem = 8192;
 
-// Phase pass: spl (1 or 2) shots per lane, one warp per group of 32 spl
-// shots (item_begin counts those groups); every program of descs has trace
-// rows of tw words.  Returns false for an unsupported tw.
+// Phase pass: spl (1, 2, or 4 for tw <= kPhaseQuadMaxWords) shots per lane,
+// one warp per group of 32 spl shots (item_begin counts those groups); every
+// program of descs has trace rows of tw words.  Returns false for an
+// unsupported (tw, spl).
 bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        long long total_groups, int* status);
 
 // From this many shots in one phase-pass launch, lanes carry two shots each:
 // with 152 SMs that still leaves 8 single-warp blocks per SM.
 constexpr long long kPhasePairMinShots = 152LL * 64 * 8;
+// Largest trace row (words) whose phase pass can carry four shots per lane.
+constexpr int kPhaseQuadMaxWords = 8;
 
 // Odd-d trace engine (k_trace_u8.cu).  variant: 0, 1, 2 for d = 3, 5, 7, 3
 // for any other odd prime.

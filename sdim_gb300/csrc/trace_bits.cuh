@@ -629,30 +629,32 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
   }
 }
 
-// Two shots per lane (coin-pass masks only): lane l of group g carries shots
-// 64 g + l and 64 g + 32 + l, each with its own delta and fire cursor, while
-// the per-measurement work that does not depend on the shot -- header and
-// factor-row loads, the measurement kind, the loop -- is done once for both.
-// Records of the group's 64 rows are staged in rec[64][kRecStride].
-template <int TW>
-__device__ __forceinline__ void phase_program_pair(const TraceDesc* __restrict__ tdp, long long group, int lane,
-                                                   uint8_t* rec) {
+// S shots per lane, S = 2 or 4 (coin-pass masks only): lane l of group g
+// carries shots 32 S g + 32 s + l, s < S, each with its own delta and fire
+// cursor, while the per-measurement work that does not depend on the shot --
+// header and factor-row loads, the measurement kind, the loop -- is done once
+// for all S; the S outcome draws of a random measurement are independent
+// Philox chains the lane interleaves.  Records of the group's 32 S rows are
+// staged in rec[32 S][kRecStride].
+template <int TW, int S>
+__device__ __forceinline__ void phase_program_multi(const TraceDesc* __restrict__ tdp, long long group, int lane,
+                                                    uint8_t* rec) {
   constexpr int FH = TW / 2;
   constexpr bool kAhead = FH <= 8;
   const uint4* __restrict__ mhdr = tdp->mhdr;
   const uint32_t* __restrict__ mrow = tdp->mrow;
   const int nm = tdp->nm, wn = tdp->wn, nmeas = tdp->c.nmeas, nshots = tdp->c.nshots;
   const uint32_t nn1 = (uint32_t)tdp->nn1;
-  const long long first = group * 64;
-  const int rows = (int)min(64LL, (long long)nshots - first);
+  const long long first = group * 32 * S;
+  const int rows = (int)min(32LL * S, (long long)nshots - first);
   uint8_t* __restrict__ gout = tdp->c.out + first * (long long)nmeas;
   const PhiloxKeys K(tdp->c.seed);
-  uint32_t d1[2][TW];
-  bool active[2];
-  uint32_t slo[2], shi[2];
-  FireCursor fc[2];
+  uint32_t d1[S][TW];
+  bool active[S];
+  uint32_t slo[S], shi[S];
+  FireCursor fc[S];
 #pragma unroll
-  for (int s = 0; s < 2; ++s) {
+  for (int s = 0; s < S; ++s) {
 #pragma unroll
     for (int w = 0; w < TW; ++w) d1[s][w] = 0u;
     const long long rel = first + 32 * s + lane;
@@ -692,7 +694,7 @@ __device__ __forceinline__ void phase_program_pair(const TraceDesc* __restrict__
     }
     const uint32_t nend = h.z < nn1 ? h.z : nn1;
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < S; ++s) {
       while (fc[s].next < nend) {
         const uint32_t j = fc[s].next, bit = 1u << (j & 31u);
         const uint32_t mz = (fc[s].ax & bit) ? 0xffffffffu : 0u, mx = (fc[s].bz & bit) ? 0xffffffffu : 0u;
@@ -706,11 +708,11 @@ __device__ __forceinline__ void phase_program_pair(const TraceDesc* __restrict__
     }
     const uint32_t* row = mrow + (size_t)k * 2 * TW;
     const uint32_t det = h.x & 1u;
-    int m[2];
+    int m[S];
     if (!det) {
       const int p = (int)h.y, wp = p >> 5, bp = p & 31;
 #pragma unroll
-      for (int s = 0; s < 2; ++s) {
+      for (int s = 0; s < S; ++s) {
         const uint32_t dp = (word_at<0, TW>(d1[s], wp) >> bp) & 1u;
         if (dp) {
 #pragma unroll
@@ -723,7 +725,7 @@ __device__ __forceinline__ void phase_program_pair(const TraceDesc* __restrict__
     } else {
       if constexpr (!kAhead) load_row<FH>(row, f);
 #pragma unroll
-      for (int s = 0; s < 2; ++s) {
+      for (int s = 0; s < S; ++s) {
         int acc = 0;
 #pragma unroll
         for (int w = 0; w < FH; ++w) acc += __popc(f[w] & d1[s][w]);
@@ -732,14 +734,14 @@ __device__ __forceinline__ void phase_program_pair(const TraceDesc* __restrict__
     }
     if (h.x & 2u) {
 #pragma unroll
-      for (int s = 0; s < 2; ++s)
+      for (int s = 0; s < S; ++s)
         if (m[s] & 1) {
 #pragma unroll
           for (int w = 0; w < TW; ++w) d1[s][w] ^= __ldg(row + TW + w);
         }
     }
 #pragma unroll
-    for (int s = 0; s < 2; ++s) rec[(32 * s + lane) * kRecStride + (k & (kRecWindow - 1))] = (uint8_t)(m[s] | (int)(det << 7));
+    for (int s = 0; s < S; ++s) rec[(32 * s + lane) * kRecStride + (k & (kRecWindow - 1))] = (uint8_t)(m[s] | (int)(det << 7));
     if ((k & (kRecWindow - 1)) == kRecWindow - 1 || k == nm - 1) {
       const int k0 = k & ~(kRecWindow - 1);
       flush_records(rec, gout, nmeas, rows, k0, min(k + 1, nmeas) - k0, lane);
