@@ -725,7 +725,7 @@ def run_single(args, torch, dist, ws, rank, local):
     if d == 2:
         # the shot-group engine on the same inputs, for comparison
         for name, fl in (("group", _lib.FLAG_NO_TRACE), ("trace", _lib.FLAG_TRACE),
-                         ("trace, at most two shots per phase-pass lane", _lib.FLAG_TRACE | _lib.FLAG_LANE_SHOTS_2)):
+                         ("trace, one shot per phase-pass lane", _lib.FLAG_TRACE | _lib.FLAG_LANE_SHOTS_1)):
             step(fl)
             ctx.sync()
             g_ms, g_kern, _ = timer.run(2, lambda: step(fl))

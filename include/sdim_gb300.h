@@ -60,10 +60,8 @@ extern "C" {
                                       from global memory) */
 #define SDIM_FLAG_U8_XZ 16384u /* odd-d trace engine, d = 3: x / z pass on residue bytes (the forms of
                                  d = 5, 7) instead of the two-bit-plane tableau */
-#define SDIM_FLAG_LANE_SHOTS_2 32768u /* d = 2 trace engine: at most two shots per phase-pass lane (by default
-                                         four from 77,824 shots in a launch when trace rows have at most 8
-                                         words, n <= 128; two for wider rows) */
-#define SDIM_FLAG_LANE_SHOTS_1 65536u /* d = 2 trace engine: one shot per phase-pass lane */
+#define SDIM_FLAG_LANE_SHOTS_1 65536u /* d = 2 trace engine: one shot per phase-pass lane (by default two
+                                         from 77,824 shots in one launch) */
 #define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
                                        into the host buffer directly, with no device buffer and no copy
                                        (by default records go to device memory, then one copy down) */

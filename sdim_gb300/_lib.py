@@ -33,7 +33,6 @@ FLAG_SPLIT_XZ = 2048
 FLAG_CLUSTER_XZ = 4096
 FLAG_DIRECT_HOST = 8192
 FLAG_U8_XZ = 16384
-FLAG_LANE_SHOTS_2 = 32768
 FLAG_LANE_SHOTS_1 = 65536
 
 

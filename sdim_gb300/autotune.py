@@ -13,7 +13,8 @@ fastest.  Its knobs:
 * the odd-d x / z pass form: one CTA, a CTA pair, an eight-CTA cluster, and
   for d = 3 the bit-plane tableau or residue bytes (``sdim_trace_xz_mode``
   tells which flags change the form, so equal forms are timed once);
-* for d = 2 the N1 coins in their own pass or inside the phase pass.
+* for d = 2 the N1 coins in their own pass or inside the phase pass, and
+  one or two shots per phase-pass lane.
 
 Rows in flight per thread are fixed per kernel form at compile time (16 for a
 tableau streamed from global memory, 8 for a CTA team, 4 in shared memory)
@@ -102,6 +103,7 @@ def program_candidates(d: int, n: int, shots: int, smem_optin: int, num_sms: int
         out.append(Candidate("trace", _lib.FLAG_TRACE))
         if d == 2:
             out.append(Candidate("trace, coins in the phase pass", _lib.FLAG_TRACE | _lib.FLAG_NO_COIN_PASS))
+            out.append(Candidate("trace, one shot per phase-pass lane", _lib.FLAG_TRACE | _lib.FLAG_LANE_SHOTS_1))
             out.append(Candidate("trace, global memory", _lib.FLAG_TRACE | _lib.FLAG_FORCE_GMEM))
         else:
             seen = {_xz_mode(n, d, 1, 0, smem_optin, num_sms)}
@@ -131,7 +133,8 @@ def batch_candidates() -> List[Candidate]:
             Candidate("odd-d x/z passes on CTA pairs", _lib.FLAG_SPLIT_XZ),
             Candidate("odd-d x/z passes on 8-CTA clusters", _lib.FLAG_CLUSTER_XZ),
             Candidate("d = 3 x/z passes on residue bytes", _lib.FLAG_U8_XZ),
-            Candidate("d=2 coins in the phase pass", _lib.FLAG_NO_COIN_PASS)]
+            Candidate("d=2 coins in the phase pass", _lib.FLAG_NO_COIN_PASS),
+            Candidate("d=2 one shot per phase-pass lane", _lib.FLAG_LANE_SHOTS_1)]
 
 
 def _octave(v: int) -> int:

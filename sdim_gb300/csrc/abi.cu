@@ -496,9 +496,10 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       size_t e = b;
       long long shots = 0;
       while (e < k && trace_words(jobs[e].c->n) == tw) shots += jobs[e++].nshots;
-      int sp = shots >= kPhasePairMinShots ? (tw <= kPhaseQuadMaxWords ? 4 : 2) : 1;
-      if (flags & SDIM_FLAG_LANE_SHOTS_2) sp = std::min(sp, 2);
-      if (flags & SDIM_FLAG_LANE_SHOTS_1) sp = 1;
+      // two shots per lane from kPhasePairMinShots (four measured slower on
+      // the L = 7 surface step: 0.31 against 0.20 ms, the lanes' registers
+      // leave five warps per SM); SDIM_FLAG_LANE_SHOTS_1 keeps one
+      const int sp = shots >= kPhasePairMinShots && !(flags & SDIM_FLAG_LANE_SHOTS_1) ? 2 : 1;
       for (size_t i = b; i < e; ++i) spl[i] = sp;
       b = e;
     }
@@ -689,7 +690,10 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       int grid = (int)std::min<size_t>(e - b, 65535);
       if (!in_smem) grid = std::min(grid, 2 * ctx->num_sms);
       unsigned* queue = in_smem ? nullptr : static_cast<unsigned*>(ctx->xz_queue.p) + r;
-      launch_trace_p3(grid, hot + (in_smem ? xz : 0) + win, rs, du + b, (int)(e - b),
+      // about one thread per qudit (64 to 512): the warps of a larger CTA
+      // would only spend issue slots walking the instruction stream
+      const int block = std::max(64, std::min(kTracePassThreads, (nmax + 31) & ~31));
+      launch_trace_p3(grid, block, hot + (in_smem ? xz : 0) + win, rs, du + b, (int)(e - b),
                       static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, queue, status);
     } else if (mode == 1) {
       launch_trace_u8_split(v, (int)std::min<size_t>(e - b, 32768), trace_u8_split_smem(nmax) + win,

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
 // registers.  Up to 16-word rows and one shot per lane, 32 blocks per SM at
 // 64 registers; wider rows or two shots per lane get 128.
 template <int TW, int SPL>
-__global__ void __launch_bounds__(32, SPL == 4 ? 12 : (TW >= 16 || SPL == 2) ? 16 : 32)
+__global__ void __launch_bounds__(32, (TW >= 16 || SPL == 2) ? 16 : 32)
     k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc, long long total_groups, const int* status) {
   __shared__ uint8_t rec[32 * SPL * kRecStride];
   if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
@@ -129,21 +129,8 @@ bool launch_phase_spl(int tw, int grid, int block, cudaStream_t s, const TraceDe
   }
 }
 
-// Four shots per lane for trace rows of up to 8 words (the deltas of four
-// shots stay in registers).
-bool launch_phase_quad(int tw, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
-                       long long total_groups, int* status) {
-  switch (tw) {
-    case 2: k_phase_pass<2, 4><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    case 4: k_phase_pass<4, 4><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    case 8: k_phase_pass<8, 4><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    default: return false;
-  }
-}
-
 bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        long long total_groups, int* status) {
-  if (spl == 4) return launch_phase_quad(tw, grid, block, s, descs, ndesc, total_groups, status);
   return spl == 2 ? launch_phase_spl<2>(tw, grid, block, s, descs, ndesc, total_groups, status)
                   : launch_phase_spl<1>(tw, grid, block, s, descs, ndesc, total_groups, status);
 }

@@ -1,5 +1,5 @@
 // x / z pass of the odd-d trace engine for d = 3 on bit planes
-// (trace_p3.cuh): one program per CTA, the tableau in shared memory when it
+// (trace_p3.cuh): one program per CTA of 64 to 512 threads, the tableau in shared memory when it
 // fits (n <= 448 on GB300), else in a global-memory slot per CTA with the
 // CTAs taking programs, largest first, from an atomic counter.
 #include "trace_p3.cuh"
@@ -45,9 +45,9 @@ size_t trace_p3_xz_bytes(int n) { return round16(P3Layout(n).xz_bytes()); }
 
 cudaError_t trace_p3_set_smem(int optin) { return set_dynamic_smem(k_trace_pass_p3, optin); }
 
-void launch_trace_p3(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
-                     size_t hot, int in_smem, unsigned* queue, int* status) {
-  k_trace_pass_p3<<<grid, kP3Threads, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, queue, status);
+void launch_trace_p3(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
+                     size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status) {
+  k_trace_pass_p3<<<grid, block, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, queue, status);
 }
 
 }  // namespace sdim

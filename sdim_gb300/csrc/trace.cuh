@@ -154,18 +154,16 @@ void launch_coin_pass(int grid, int block, size_t smem, cudaStream_t s, const Tr
 // shared memory so that no coin block lands beside them.
 constexpr size_t kCoinFenceSmem = 8192;
 
-// Phase pass: spl (1, 2, or 4 for tw <= kPhaseQuadMaxWords) shots per lane,
-// one warp per group of 32 spl shots (item_begin counts those groups); every
-// program of descs has trace rows of tw words.  Returns false for an
-// unsupported (tw, spl).
+// Phase pass: spl (1 or 2) shots per lane, one warp per group of 32 spl
+// shots (item_begin counts those groups); every program of descs has trace
+// rows of tw words.  Returns false for an unsupported tw.
 bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,
                        long long total_groups, int* status);
 
 // From this many shots in one phase-pass launch, lanes carry two shots each:
 // with 152 SMs that still leaves 8 single-warp blocks per SM.
 constexpr long long kPhasePairMinShots = 152LL * 64 * 8;
-// Largest trace row (words) whose phase pass can carry four shots per lane.
-constexpr int kPhaseQuadMaxWords = 8;
+
 
 // Odd-d trace engine (k_trace_u8.cu).  variant: 0, 1, 2 for d = 3, 5, 7, 3
 // for any other odd prime.
@@ -200,15 +198,15 @@ void launch_trace_u8_cluster(int variant, int clusters, size_t smem, cudaStream_
 void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
                            int nd, long long total, int* status);
 
-// x / z pass for d = 3 on bit planes (k_trace_p3.cu): one CTA of 512
-// threads per program, x / z in shared memory after the hot part when
+// x / z pass for d = 3 on bit planes (k_trace_p3.cu): one CTA of block (64
+// to 512) threads per program, x / z in shared memory after the hot part when
 // in_smem, else at gxz + blockIdx.x * xzb with programs taken from queue;
 // the instruction window (trace_u8_window_bytes) follows in shared memory.
 // Writes the same trace as the byte-residue passes.
 size_t trace_p3_hot_bytes(int n);
 size_t trace_p3_xz_bytes(int n);
 cudaError_t trace_p3_set_smem(int optin);
-void launch_trace_p3(int grid, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz, size_t xzb,
-                     size_t hot, int in_smem, unsigned* queue, int* status);
+void launch_trace_p3(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
+                     size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status);
 
 }  // namespace sdim

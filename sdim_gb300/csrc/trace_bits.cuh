@@ -629,7 +629,7 @@ __device__ __forceinline__ void phase_program(const TraceDesc* __restrict__ tdp,
   }
 }
 
-// S shots per lane, S = 2 or 4 (coin-pass masks only): lane l of group g
+// S shots per lane (coin-pass masks only; the kernels use S = 2): lane l of group g
 // carries shots 32 S g + 32 s + l, s < S, each with its own delta and fire
 // cursor, while the per-measurement work that does not depend on the shot --
 // header and factor-row loads, the measurement kind, the loop -- is done once
