@@ -394,18 +394,39 @@ def p3_single_cta(n, smem_optin):
     return hot + xz + 4096 + 4096 <= smem_optin
 
 
-def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=5):
+def n4_single_cta(n, d, smem_optin):
+    """Whether the d = 5 / 7 4-bit-lane x / z pass of n qudits keeps its
+    tableau in one CTA's shared memory: rows of W = 2 ceil(n / 8) words at an
+    odd stride, a hot part of 3 W + W / 2 * 2 + (d - 1) (W + 512) words and two
+    n-byte columns, and a 4 KB instruction window."""
+    wh = (n + 7) // 8
+    w = 2 * wh
+    r16 = lambda x: (x + 15) & ~15  # noqa: E731
+    hot = r16((3 * w + 2 * wh + (d - 1) * w + (d - 1) * 512) * 4 + 2 * ((n + 15) & ~15))
+    xz = r16(2 * n * (w | 1) * 4)
+    return hot + xz + 4096 + 4096 <= smem_optin
+
+
+def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=11):
     """Where the library runs the odd-d x / z pass of n qudits, as (CTAs per
     program, where its columns live: "smem", "l2" or "hbm").  For d = 3 one
     CTA on the bit-plane tableau, in shared memory when it fits, else
-    streamed from HBM.  For other d one CTA when its byte tableau fits in
-    shared memory.  Else, in a batch of at least num_sms / 2 odd-d trace
-    programs, a CTA pair when that fits and one CTA streaming from HBM above;
-    in a smaller batch a cluster of 8 CTAs, columns in shared memory up to
-    n = 636 and streamed from global memory, held in L2, above."""
+    streamed from HBM.  For d = 5, 7 one CTA on the 4-bit-lane tableau when it
+    fits in shared memory, else streamed from HBM in a batch of at least
+    num_sms / 2 odd-d trace programs and the byte cluster below in a smaller
+    one.  For other d one CTA when its byte tableau fits in shared memory.
+    Else, in a batch of at least num_sms / 2 odd-d trace programs, a CTA pair
+    when that fits and one CTA streaming from HBM above; in a smaller batch a
+    cluster of 8 CTAs, columns in shared memory up to n = 636 and streamed
+    from global memory, held in L2, above."""
     if d == 3:
         return 1, ("smem" if p3_single_cta(n, smem_optin) else "hbm")
-    if u8_single_cta(n, smem_optin):
+    if d in (5, 7):
+        if n4_single_cta(n, d, smem_optin):
+            return 1, "smem"
+        if 2 * odd_trace_programs >= num_sms:
+            return 1, "hbm"
+    elif u8_single_cta(n, smem_optin):
         return 1, "smem"
     r16 = lambda x: (x + 15) & ~15  # noqa: E731
     npad, win = (n + 15) & ~15, 4096
@@ -885,7 +906,8 @@ def run_single(args, torch, dist, ws, rank, local):
             sms, _ = u8_xz_layout(n, 1, ctx.smem_optin, ctx.num_sms, d)
             share = peak * sms / ctx.num_sms
             xz_ach = per_shot_bytes / (xz_ms / 1e3) / 1e9
-            xz_kernel = {1: "k_trace_pass_p3" if d == 3 else "k_trace_pass_u8", 2: "k_trace_pass_split",
+            xz_kernel = {1: {3: "k_trace_pass_p3", 5: "k_trace_pass_n4", 7: "k_trace_pass_n4"}.get(d, "k_trace_pass_u8"),
+                         2: "k_trace_pass_split",
                          8: "k_trace_pass_cluster"}[sms]
             roofline = {"bound": f"smem (x/z pass, latency-bound on {sms} CTA{'s' if sms > 1 else ''})",
                         "achieved": xz_ach, "peak": share, "unit": "GB/s", "frac": xz_ach / share,

@@ -58,8 +58,8 @@ extern "C" {
                                       that do not fit one CTA in batches of fewer than 76 odd-d trace
                                       programs (larger batches use CTA pairs, then single CTAs streaming
                                       from global memory) */
-#define SDIM_FLAG_U8_XZ 16384u /* odd-d trace engine, d = 3: x / z pass on residue bytes (the forms of
-                                 d = 5, 7) instead of the two-bit-plane tableau */
+#define SDIM_FLAG_U8_XZ 16384u /* odd-d trace engine: x / z pass on residue bytes (the forms of d >= 11)
+                                 instead of the two-bit-plane tableau (d = 3) or 4-bit lanes (d = 5, 7) */
 #define SDIM_FLAG_LANE_SHOTS_1 65536u /* d = 2 trace engine: one shot per phase-pass lane (by default two
                                          from 77,824 shots in one launch) */
 #define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
@@ -195,7 +195,9 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
  * CTA pair; 2 one CTA, byte tableau in global memory; 3 a cluster of 8
  * CTAs, columns in shared memory; 4 the cluster, columns in global memory;
  * 5 (d = 3) one CTA, bit-plane tableau in shared memory; 6 (d = 3) one CTA,
- * bit-plane tableau in global memory.  Host-only (no device is touched), so
+ * bit-plane tableau in global memory; 7 (d = 5, 7) one CTA, 4-bit-lane
+ * tableau in shared memory; 8 (d = 5, 7) one CTA, 4-bit-lane tableau in
+ * global memory.  Host-only (no device is touched), so
  * callers such as a roofline model can mirror the library's routing.
  * SDIM_EINVAL for n outside [1, 2048], an even d or non-positive sizes.  No
  * counterpart in the reference. */

@@ -11,7 +11,8 @@ fastest.  Its knobs:
 * residency: tableaux in shared memory where they fit, or in global memory
   (``FLAG_FORCE_GMEM``);
 * the odd-d x / z pass form: one CTA, a CTA pair, an eight-CTA cluster, and
-  for d = 3 the bit-plane tableau or residue bytes (``sdim_trace_xz_mode``
+  the packed tableau (bit planes for d = 3, 4-bit lanes for d = 5, 7) or
+  residue bytes (``sdim_trace_xz_mode``
   tells which flags change the form, so equal forms are timed once);
 * for d = 2 the N1 coins in their own pass or inside the phase pass, and
   one or two shots per phase-pass lane.
@@ -62,7 +63,8 @@ PER_SHOT_MAX_SHOTS = 64
 TUNE_MAX_SHOTS = 1 << 17
 
 _XZ_FORM = {0: "one CTA", 1: "CTA pair", 2: "one CTA, global memory", 3: "8-CTA cluster",
-            4: "8-CTA cluster, global memory", 5: "one CTA, bit planes", 6: "one CTA, bit planes in global memory"}
+            4: "8-CTA cluster, global memory", 5: "one CTA, bit planes", 6: "one CTA, bit planes in global memory",
+            7: "one CTA, 4-bit lanes", 8: "one CTA, 4-bit lanes in global memory"}
 
 
 @dataclass(frozen=True)
@@ -132,7 +134,7 @@ def batch_candidates() -> List[Candidate]:
             Candidate("shot groups only", _lib.FLAG_NO_TRACE),
             Candidate("odd-d x/z passes on CTA pairs", _lib.FLAG_SPLIT_XZ),
             Candidate("odd-d x/z passes on 8-CTA clusters", _lib.FLAG_CLUSTER_XZ),
-            Candidate("d = 3 x/z passes on residue bytes", _lib.FLAG_U8_XZ),
+            Candidate("odd-d x/z passes on residue bytes", _lib.FLAG_U8_XZ),
             Candidate("d=2 coins in the phase pass", _lib.FLAG_NO_COIN_PASS),
             Candidate("d=2 one shot per phase-pass lane", _lib.FLAG_LANE_SHOTS_1)]
 

@@ -20,7 +20,8 @@ INCLUDE = ROOT / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-diag-suppress", "177"]
-UNITS = ["abi.cu", "k_pershot.cu", "k_group.cu", "k_trace.cu", "k_trace_u8.cu", "k_trace_p3.cu", "k_frame.cu",
+UNITS = ["abi.cu", "k_pershot.cu", "k_group.cu", "k_trace.cu", "k_trace_u8.cu", "k_trace_p3.cu", "k_trace_n4.cu",
+         "k_frame.cu",
          "noalloc.cu", "chp.cu"]
 
 

@@ -405,15 +405,27 @@ constexpr int kTraceU8MaxQudits = 2048;
 // in shared memory (3) or global memory (4).  For d = 3 (unless
 // SDIM_FLAG_U8_XZ, SDIM_FLAG_SPLIT_XZ or SDIM_FLAG_CLUSTER_XZ names a byte
 // form) one CTA on the bit-plane tableau (trace_p3.cuh), in shared memory (5)
-// up to n = 448 on GB300, else in a global-memory slot (6).  A cluster shares each
+// up to n = 448 on GB300, else in a global-memory slot (6).  For d = 5 and 7
+// (same flags) one CTA on the 4-bit-lane tableau (trace_n4.cuh) in shared
+// memory (7) up to n = 320 on GB300, else in a global-memory slot (8) in a batch
+// of num_sms / 2 or more odd-d trace programs, the byte cluster in a smaller
+// one.  A cluster shares each
 // measurement's fixed cost (two cluster barriers, pivot search, broadcast)
 // among 8 SMs, so it finishes one program sooner but a full batch later.
 int odd_xz_mode(int n, int d, long long programs, unsigned flags, size_t optin, int num_sms) {
   const size_t win = trace_u8_window_bytes();
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
-  if (d == 3 && !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ)))
-    return !force_gmem && trace_p3_hot_bytes(n) + trace_p3_xz_bytes(n) + win + 4096 <= optin ? 5 : 6;
+  const bool packed = !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ));
   const bool few = programs * 2 < (long long)num_sms;
+  if (d == 3 && packed)
+    return !force_gmem && trace_p3_hot_bytes(n) + trace_p3_xz_bytes(n) + win + 4096 <= optin ? 5 : 6;
+  if ((d == 5 || d == 7) && packed) {
+    if (force_gmem) return 8;
+    if (trace_n4_hot_bytes(n, d) + trace_n4_xz_bytes(n) + win + 4096 <= optin) return 7;
+    if (!few) return 8;
+    // a lone large program: the byte cluster below shares its measurements
+    // among 8 SMs
+  }
   const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
   const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
   const bool cl_smem = trace_u8_cluster_hot(n) + trace_u8_cluster_xz(n) + win + 4096 <= optin;
@@ -456,6 +468,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     cudaError_t e = trace_set_smem(ctx->smem_optin);
     if (e == cudaSuccess) e = trace_u8_set_smem(ctx->smem_optin);
     if (e == cudaSuccess) e = trace_p3_set_smem(ctx->smem_optin);
+    if (e == cudaSuccess) e = trace_n4_set_smem(ctx->smem_optin);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFuncSetAttribute");
     ctx->trace_smem_set = true;
   }
@@ -658,6 +671,9 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     } else if (mode == 6) {
       const size_t grid = std::min<size_t>(e - b, 2 * (size_t)ctx->num_sms);
       slot_total += trace_p3_xz_bytes(hu[b].c.n) * grid;
+    } else if (mode == 8) {
+      const size_t grid = std::min<size_t>(e - b, 2 * (size_t)ctx->num_sms);
+      slot_total += trace_n4_xz_bytes(hu[b].c.n) * grid;
     } else if (mode == 4) {
       slot_total += trace_u8_cluster_xz(hu[b].c.n) * kTraceClusterCtas * stream_clusters(e - b);
     }
@@ -683,7 +699,18 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       used[si] = true;
     }
     const int nmax = hu[b].c.n;
-    if (mode >= 5) {
+    if (mode >= 7) {
+      // d = 5, 7 on 4-bit lanes: one CTA per program, largest first
+      const bool in_smem = mode == 7;
+      const int dd = hu[b].c.d;
+      const size_t hot = trace_n4_hot_bytes(nmax, dd), xz = trace_n4_xz_bytes(nmax);
+      int grid = (int)std::min<size_t>(e - b, 65535);
+      if (!in_smem) grid = std::min(grid, 2 * ctx->num_sms);
+      unsigned* queue = in_smem ? nullptr : static_cast<unsigned*>(ctx->xz_queue.p) + r;
+      const int block = std::max(64, std::min(kTracePassThreads, (nmax + 31) & ~31));
+      launch_trace_n4(dd, grid, block, hot + (in_smem ? xz : 0) + win, rs, du + b, (int)(e - b),
+                      static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, queue, status);
+    } else if (mode >= 5) {
       // d = 3 on bit planes: one CTA per program, largest first
       const bool in_smem = mode == 5;
       const size_t hot = trace_p3_hot_bytes(nmax), xz = trace_p3_xz_bytes(nmax);

@@ -209,4 +209,12 @@ cudaError_t trace_p3_set_smem(int optin);
 void launch_trace_p3(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
                      size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status);
 
+// x / z pass for d = 5 and 7 on 4-bit residue lanes (k_trace_n4.cu), in the
+// same form as the d = 3 bit-plane pass.
+size_t trace_n4_hot_bytes(int n, int d);
+size_t trace_n4_xz_bytes(int n);
+cudaError_t trace_n4_set_smem(int optin);
+void launch_trace_n4(int d, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* dsc, int nd,
+                     uint8_t* gxz, size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status);
+
 }  // namespace sdim

@@ -162,18 +162,20 @@ def test_library_without_device_reports_error_not_fallback():
 
 
 def test_odd_d_xz_routing_and_its_bench_mirror():
-    """sdim_trace_xz_mode (host-only) on GB300's limits.  d = 5, 7: one CTA
-    to n = 226; for batches of 76+ programs a CTA pair to n = 330, then one
-    streaming CTA; for smaller batches an eight-CTA cluster, in shared memory
-    to n = 636.  d = 3: one CTA on the bit-plane tableau, in shared memory to
-    n = 448, then streamed; SDIM_FLAG_U8_XZ (or a pair / cluster flag) gives
-    the byte forms.  The bench's roofline model (bench.u8_xz_layout) agrees
-    with it at every n."""
+    """sdim_trace_xz_mode (host-only) on GB300's limits.  Residue bytes
+    (d >= 11, or SDIM_FLAG_U8_XZ): one CTA to n = 226; for batches of 76+
+    programs a CTA pair to n = 330, then one streaming CTA; for smaller
+    batches an eight-CTA cluster, in shared memory to n = 636.  d = 3: one
+    CTA on the bit-plane tableau, in shared memory to n = 448, then
+    streamed.  d = 5, 7: one CTA on 4-bit lanes, in shared memory to n = 320,
+    then streamed in batches of 76+ and the byte cluster in smaller ones.
+    The bench's roofline model (bench.u8_xz_layout) agrees with it at every
+    n."""
     import bench
     from sdim_gb300 import _lib
     lib = _lib.load()
     optin, sms = 232448, 152
-    mode = lambda n, progs, flags=0, d=5: lib.sdim_trace_xz_mode(n, d, progs, flags, optin, sms)  # noqa: E731
+    mode = lambda n, progs, flags=0, d=11: lib.sdim_trace_xz_mode(n, d, progs, flags, optin, sms)  # noqa: E731
     assert [mode(n, 1000) for n in (1, 226, 227, 330, 331, 2048)] == [0, 0, 1, 1, 2, 2]
     assert [mode(n, 75) for n in (226, 227, 636, 637, 2048)] == [0, 3, 3, 4, 4]
     assert mode(100, 1000, _lib.FLAG_CLUSTER_XZ) == 3
@@ -185,11 +187,15 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     assert [mode(n, 1000, 0, 3) for n in (1, 448, 449, 2048)] == [5, 5, 6, 6]
     assert [mode(n, 75, 0, 3) for n in (1, 448, 449, 2048)] == [5, 5, 6, 6]
     assert mode(100, 1, _lib.FLAG_FORCE_GMEM, 3) == 6
-    assert mode(300, 1000, _lib.FLAG_U8_XZ, 3) == mode(300, 1000, 0, 5) == 1
+    assert mode(300, 1000, _lib.FLAG_U8_XZ, 3) == mode(300, 1000, _lib.FLAG_U8_XZ, 5) == mode(300, 1000) == 1
     assert mode(300, 1, _lib.FLAG_CLUSTER_XZ, 3) == 3
+    for d in (5, 7):
+        assert [mode(n, 1000, 0, d) for n in (1, 256, 320, 321, 2048)] == [7, 7, 7, 8, 8]
+        assert [mode(n, 75, 0, d) for n in (320, 321, 636, 637)] == [7, 3, 3, 4]
+        assert mode(100, 1, _lib.FLAG_FORCE_GMEM, d) == 8
     forms = {0: (1, "smem"), 1: (2, "smem"), 2: (1, "hbm"), 3: (8, "smem"), 4: (8, "l2"), 5: (1, "smem"),
-             6: (1, "hbm")}
-    for d in (3, 5):
+             6: (1, "hbm"), 7: (1, "smem"), 8: (1, "hbm")}
+    for d in (3, 5, 7, 11):
         for progs in (1, 75, 76, 5000):
             for n in range(1, 2049):
                 assert bench.u8_xz_layout(n, progs, optin, sms, d) == forms[mode(n, progs, 0, d)], (n, progs, d)

@@ -30,16 +30,21 @@ def test_candidates_past_the_d2_trace_limit_and_large_n_teams():
 
 
 def test_odd_d_xz_forms_are_deduplicated_by_the_library_query():
-    # n = 256 does not fit one CTA: a lone program's default x / z pass is the
-    # 8-CTA cluster in shared memory; the pair, the streamed single CTA and the
-    # streamed cluster are the other forms, each timed once
-    c = _names(autotune.program_candidates(5, 256, 4096, OPTIN, SMS))
+    # d = 11, n = 256 does not fit one CTA in bytes: a lone program's default
+    # x / z pass is the 8-CTA cluster in shared memory; the pair, the streamed
+    # single CTA and the streamed cluster are the other forms, each timed once
+    c = _names(autotune.program_candidates(11, 256, 4096, OPTIN, SMS))
     forms = [x for x in c if x.startswith("trace, x/z")]
     assert forms == ["trace, x/z pass on CTA pair", "trace, x/z pass on one CTA, global memory",
                      "trace, x/z pass on 8-CTA cluster, global memory"]
     # n = 100 fits one CTA: every override is a different form
-    small = [x for x in _names(autotune.program_candidates(5, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
+    small = [x for x in _names(autotune.program_candidates(11, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
     assert len(small) == 4
+    # d = 5, n = 256 runs on 4-bit lanes in one CTA; the byte forms follow
+    d5 = [x for x in _names(autotune.program_candidates(5, 256, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
+    assert d5 == ["trace, x/z pass on CTA pair", "trace, x/z pass on 8-CTA cluster",
+                  "trace, x/z pass on one CTA, 4-bit lanes in global memory",
+                  "trace, x/z pass on 8-CTA cluster, global memory", "trace, x/z pass on one CTA, global memory"]
     # d = 3 runs on bit planes by default; the byte forms are six more
     d3 = [x for x in _names(autotune.program_candidates(3, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
     assert len(d3) == 6 and "trace, x/z pass on one CTA" in d3
