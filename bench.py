@@ -409,24 +409,18 @@ def n4_single_cta(n, d, smem_optin):
 
 def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=11):
     """Where the library runs the odd-d x / z pass of n qudits, as (CTAs per
-    program, where its columns live: "smem", "l2" or "hbm").  For d = 3 one
-    CTA on the bit-plane tableau, in shared memory when it fits, else
-    streamed from HBM.  For d = 5, 7 one CTA on the 4-bit-lane tableau when it
-    fits in shared memory, else streamed from HBM in a batch of at least
-    num_sms / 2 odd-d trace programs and the byte cluster below in a smaller
-    one.  For other d one CTA when its byte tableau fits in shared memory.
-    Else, in a batch of at least num_sms / 2 odd-d trace programs, a CTA pair
-    when that fits and one CTA streaming from HBM above; in a smaller batch a
-    cluster of 8 CTAs, columns in shared memory up to n = 636 and streamed
-    from global memory, held in L2, above."""
-    if d == 3:
-        return 1, ("smem" if p3_single_cta(n, smem_optin) else "hbm")
-    if d in (5, 7):
-        if n4_single_cta(n, d, smem_optin):
-            return 1, "smem"
-        if 2 * odd_trace_programs >= num_sms:
-            return 1, "hbm"
-    elif u8_single_cta(n, smem_optin):
+    program, where its columns live: "smem", "l2" or "hbm").  In a batch of
+    at least num_sms / 2 odd-d trace programs, d = 3, 5, 7 run on one CTA with
+    the packed tableau (bit planes, 4-bit lanes), in shared memory when it
+    fits, else streamed from HBM.  Otherwise (other d, smaller batches) one
+    CTA when the byte tableau fits in shared memory; else, in a batch of at
+    least num_sms / 2, a CTA pair when that fits and one CTA streaming from
+    HBM above; in a smaller batch a cluster of 8 CTAs, columns in shared
+    memory up to n = 636 and streamed from global memory, held in L2, above."""
+    if d in (3, 5, 7) and 2 * odd_trace_programs >= num_sms:
+        fits = p3_single_cta(n, smem_optin) if d == 3 else n4_single_cta(n, d, smem_optin)
+        return 1, ("smem" if fits else "hbm")
+    if u8_single_cta(n, smem_optin):
         return 1, "smem"
     r16 = lambda x: (x + 15) & ~15  # noqa: E731
     npad, win = (n + 15) & ~15, 4096

@@ -59,7 +59,10 @@ extern "C" {
                                       programs (larger batches use CTA pairs, then single CTAs streaming
                                       from global memory) */
 #define SDIM_FLAG_U8_XZ 16384u /* odd-d trace engine: x / z pass on residue bytes (the forms of d >= 11)
-                                 instead of the two-bit-plane tableau (d = 3) or 4-bit lanes (d = 5, 7) */
+                                 instead of the two-bit-plane tableau (d = 3) or 4-bit lanes (d = 5, 7),
+                                 which batches of 76+ odd-d trace programs use by default */
+#define SDIM_FLAG_PACKED_XZ 131072u /* odd-d trace engine, d = 3, 5, 7: the packed x / z pass (bit planes,
+                                       4-bit lanes) also for runs of fewer than 76 odd-d trace programs */
 #define SDIM_FLAG_LANE_SHOTS_1 65536u /* d = 2 trace engine: one shot per phase-pass lane (by default two
                                          from 77,824 shots in one launch) */
 #define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
@@ -197,7 +200,8 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
  * 5 (d = 3) one CTA, bit-plane tableau in shared memory; 6 (d = 3) one CTA,
  * bit-plane tableau in global memory; 7 (d = 5, 7) one CTA, 4-bit-lane
  * tableau in shared memory; 8 (d = 5, 7) one CTA, 4-bit-lane tableau in
- * global memory.  Host-only (no device is touched), so
+ * global memory (5-8 for runs of 76+ odd-d trace programs on GB300, or with
+ * SDIM_FLAG_PACKED_XZ).  Host-only (no device is touched), so
  * callers such as a roofline model can mirror the library's routing.
  * SDIM_EINVAL for n outside [1, 2048], an even d or non-positive sizes.  No
  * counterpart in the reference. */

@@ -33,6 +33,7 @@ FLAG_SPLIT_XZ = 2048
 FLAG_CLUSTER_XZ = 4096
 FLAG_DIRECT_HOST = 8192
 FLAG_U8_XZ = 16384
+FLAG_PACKED_XZ = 131072
 FLAG_LANE_SHOTS_1 = 65536
 
 

@@ -111,7 +111,8 @@ def program_candidates(d: int, n: int, shots: int, smem_optin: int, num_sms: int
             seen = {_xz_mode(n, d, 1, 0, smem_optin, num_sms)}
             for extra in (_lib.FLAG_SPLIT_XZ, _lib.FLAG_CLUSTER_XZ, _lib.FLAG_FORCE_GMEM,
                           _lib.FLAG_CLUSTER_XZ | _lib.FLAG_FORCE_GMEM, _lib.FLAG_U8_XZ,
-                          _lib.FLAG_U8_XZ | _lib.FLAG_FORCE_GMEM):
+                          _lib.FLAG_U8_XZ | _lib.FLAG_FORCE_GMEM, _lib.FLAG_PACKED_XZ,
+                          _lib.FLAG_PACKED_XZ | _lib.FLAG_FORCE_GMEM):
                 mode = _xz_mode(n, d, 1, extra, smem_optin, num_sms)
                 if mode not in seen:
                     seen.add(mode)
@@ -135,6 +136,7 @@ def batch_candidates() -> List[Candidate]:
             Candidate("odd-d x/z passes on CTA pairs", _lib.FLAG_SPLIT_XZ),
             Candidate("odd-d x/z passes on 8-CTA clusters", _lib.FLAG_CLUSTER_XZ),
             Candidate("odd-d x/z passes on residue bytes", _lib.FLAG_U8_XZ),
+            Candidate("odd-d packed x/z passes whatever the batch size", _lib.FLAG_PACKED_XZ),
             Candidate("d=2 coins in the phase pass", _lib.FLAG_NO_COIN_PASS),
             Candidate("d=2 one shot per phase-pass lane", _lib.FLAG_LANE_SHOTS_1)]
 

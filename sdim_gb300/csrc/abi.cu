@@ -404,28 +404,28 @@ constexpr int kTraceU8MaxQudits = 2048;
 // cluster of kTraceClusterCtas CTAs (trace_cluster_u8.cuh) with its columns
 // in shared memory (3) or global memory (4).  For d = 3 (unless
 // SDIM_FLAG_U8_XZ, SDIM_FLAG_SPLIT_XZ or SDIM_FLAG_CLUSTER_XZ names a byte
-// form) one CTA on the bit-plane tableau (trace_p3.cuh), in shared memory (5)
-// up to n = 448 on GB300, else in a global-memory slot (6).  For d = 5 and 7
-// (same flags) one CTA on the 4-bit-lane tableau (trace_n4.cuh) in shared
-// memory (7) up to n = 320 on GB300, else in a global-memory slot (8) in a batch
-// of num_sms / 2 or more odd-d trace programs, the byte cluster in a smaller
-// one.  A cluster shares each
+// form) in a batch of num_sms / 2 or more odd-d trace programs (or with
+// SDIM_FLAG_PACKED_XZ) one CTA on the bit-plane tableau (trace_p3.cuh), in
+// shared memory (5) up to n = 448 on GB300, else in a global-memory slot (6).
+// For d = 5 and 7 likewise on the 4-bit-lane tableau (trace_n4.cuh): shared
+// memory (7) up to n = 320, else a global-memory slot (8).  A cluster shares each
 // measurement's fixed cost (two cluster barriers, pivot search, broadcast)
 // among 8 SMs, so it finishes one program sooner but a full batch later.
 int odd_xz_mode(int n, int d, long long programs, unsigned flags, size_t optin, int num_sms) {
   const size_t win = trace_u8_window_bytes();
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
-  const bool packed = !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ));
   const bool few = programs * 2 < (long long)num_sms;
-  if (d == 3 && packed)
+  // packed tableaux for batches (throughput: a quarter or half of the bytes),
+  // the byte forms for a few programs (latency: on GB300 a lone d = 5,
+  // n = 256 program's x / z pass took 4.38 ms on 4-bit lanes in one CTA and
+  // 3.17 ms on the byte cluster; PR1's 0.31 ms on bit planes, 0.26 on bytes)
+  const bool packed = (d == 3 || d == 5 || d == 7) &&
+                      !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ)) &&
+                      (!few || (flags & SDIM_FLAG_PACKED_XZ));
+  if (packed && d == 3)
     return !force_gmem && trace_p3_hot_bytes(n) + trace_p3_xz_bytes(n) + win + 4096 <= optin ? 5 : 6;
-  if ((d == 5 || d == 7) && packed) {
-    if (force_gmem) return 8;
-    if (trace_n4_hot_bytes(n, d) + trace_n4_xz_bytes(n) + win + 4096 <= optin) return 7;
-    if (!few) return 8;
-    // a lone large program: the byte cluster below shares its measurements
-    // among 8 SMs
-  }
+  if (packed)
+    return !force_gmem && trace_n4_hot_bytes(n, d) + trace_n4_xz_bytes(n) + win + 4096 <= optin ? 7 : 8;
   const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
   const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
   const bool cl_smem = trace_u8_cluster_hot(n) + trace_u8_cluster_xz(n) + win + 4096 <= optin;

@@ -40,14 +40,16 @@ def test_odd_d_xz_forms_are_deduplicated_by_the_library_query():
     # n = 100 fits one CTA: every override is a different form
     small = [x for x in _names(autotune.program_candidates(11, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
     assert len(small) == 4
-    # d = 5, n = 256 runs on 4-bit lanes in one CTA; the byte forms follow
+    # a lone d = 5, n = 256 program runs on the byte cluster; the 4-bit-lane
+    # forms are timed beside the byte ones
     d5 = [x for x in _names(autotune.program_candidates(5, 256, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
-    assert d5 == ["trace, x/z pass on CTA pair", "trace, x/z pass on 8-CTA cluster",
-                  "trace, x/z pass on one CTA, 4-bit lanes in global memory",
-                  "trace, x/z pass on 8-CTA cluster, global memory", "trace, x/z pass on one CTA, global memory"]
-    # d = 3 runs on bit planes by default; the byte forms are six more
+    assert d5 == ["trace, x/z pass on CTA pair", "trace, x/z pass on one CTA, global memory",
+                  "trace, x/z pass on 8-CTA cluster, global memory", "trace, x/z pass on one CTA, 4-bit lanes",
+                  "trace, x/z pass on one CTA, 4-bit lanes in global memory"]
+    # a lone d = 3 program runs on bytes by default; the bit-plane forms are
+    # two of the six others
     d3 = [x for x in _names(autotune.program_candidates(3, 100, 4096, OPTIN, SMS)) if x.startswith("trace, x/z")]
-    assert len(d3) == 6 and "trace, x/z pass on one CTA" in d3
+    assert len(d3) == 6 and "trace, x/z pass on one CTA, bit planes" in d3
     assert "trace, x/z pass on one CTA, bit planes in global memory" in d3
     # past the odd-d trace engine's limit only the group engines remain
     big = _names(autotune.program_candidates(5, 2049, 64, OPTIN, SMS))

@@ -14,8 +14,8 @@ from tests.conftest import oracle_run
 
 pytestmark = pytest.mark.gpu
 
-LANES = _lib.FLAG_TRACE
-LANES_GMEM = _lib.FLAG_TRACE | _lib.FLAG_FORCE_GMEM
+LANES = _lib.FLAG_TRACE | _lib.FLAG_PACKED_XZ
+LANES_GMEM = _lib.FLAG_TRACE | _lib.FLAG_PACKED_XZ | _lib.FLAG_FORCE_GMEM
 BYTES = _lib.FLAG_TRACE | _lib.FLAG_U8_XZ
 
 
@@ -98,7 +98,7 @@ def test_uneven_batch_forms_agree():
     br = BatchRunner()
     for it in items:
         br.add_spec(it.spec, it.shots, it.seed)
-    lanes = br.run(flags=_lib.FLAG_TRACE)
+    lanes = br.run(flags=_lib.FLAG_TRACE | _lib.FLAG_PACKED_XZ)
     bytes_ = br.run(flags=_lib.FLAG_TRACE | _lib.FLAG_U8_XZ)
     for it, a, b in zip(items, lanes, bytes_):
         assert np.array_equal(a, b), it.spec.name

@@ -14,8 +14,8 @@ from tests.conftest import oracle_run
 
 pytestmark = pytest.mark.gpu
 
-PLANES = _lib.FLAG_TRACE
-PLANES_GMEM = _lib.FLAG_TRACE | _lib.FLAG_FORCE_GMEM
+PLANES = _lib.FLAG_TRACE | _lib.FLAG_PACKED_XZ
+PLANES_GMEM = _lib.FLAG_TRACE | _lib.FLAG_PACKED_XZ | _lib.FLAG_FORCE_GMEM
 BYTES = _lib.FLAG_TRACE | _lib.FLAG_U8_XZ
 
 
@@ -84,7 +84,7 @@ def test_uneven_batch_d3_forms_agree():
     br = BatchRunner()
     for it in items:
         br.add_spec(it.spec, it.shots, it.seed)
-    planes = br.run(flags=_lib.FLAG_TRACE)
+    planes = br.run(flags=_lib.FLAG_TRACE | _lib.FLAG_PACKED_XZ)
     bytes_ = br.run(flags=_lib.FLAG_TRACE | _lib.FLAG_U8_XZ)
     for it, a, b in zip(items, planes, bytes_):
         assert np.array_equal(a, b), it.spec.name
