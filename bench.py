@@ -345,7 +345,7 @@ def trace_words(n):
     tw = 2
     while tw < w2:
         tw *= 2
-    return tw if tw <= 32 else 0
+    return tw if tw <= 128 else 0
 
 
 def philox_peak(ctx):

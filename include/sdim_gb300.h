@@ -48,7 +48,7 @@ extern "C" {
 #define SDIM_FLAG_TEAM_CTA 128u  /* shot groups on one CTA each, whatever n */
 #define SDIM_FLAG_TRACE 256u     /* trace engines (one x / z pass per program, then a per-shot phase
                                     replay) whatever the shot count; by default they run from 128
-                                    shots or 160 qudits (d = 2 up to n = 512, odd d up to 2048) */
+                                    shots or 160 qudits (n up to 2048) */
 #define SDIM_FLAG_NO_TRACE 512u  /* no trace engine: shot-group engines only */
 #define SDIM_FLAG_NO_COIN_PASS 1024u /* trace engine: draw N1 coins inside the phase pass, no coin pass */
 #define SDIM_FLAG_SPLIT_XZ 2048u /* odd-d trace engine: x / z pass on a CTA pair whenever it fits */

@@ -53,7 +53,7 @@ from . import _lib
 
 # limits of the library's routes (abi.cu: trace_words, kTraceU8MaxQudits,
 # kCtaTeamQudits); candidates outside them would fall back to another route
-TRACE_BITS_MAX_QUDITS = 512
+TRACE_BITS_MAX_QUDITS = 2048
 TRACE_U8_MAX_QUDITS = 2048
 CTA_TEAM_QUDITS = 160
 # the per-shot engine is a candidate for runs of fewer shots than this: a

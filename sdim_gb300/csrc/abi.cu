@@ -114,7 +114,7 @@ struct sdim_circuit {
   uint2* h_ops = nullptr;  // pinned host copy of the blob: instruction words, then the trace schedule
   uint2* d_ops = nullptr;  // device copy of the same blob
   int64_t blob_words = 0;  // uint2 words of the blob
-  const uint4* d_steps = nullptr;  // trace schedule (d = 2, n <= 512), inside the blob
+  const uint4* d_steps = nullptr;  // trace schedule (d = 2, n <= 2048), inside the blob
   const uint4* d_lops = nullptr;
   const uint4* d_wins = nullptr;
   const uint32_t* d_nthr = nullptr;  // N1 coin thresholds, padded to a multiple of 64 with 0xffffffff
@@ -379,7 +379,7 @@ constexpr int64_t kTraceMinShots = 128;
 constexpr int kTraceMinQudits = 160;
 
 // Jobs for the trace engine: d = 2, batched form, trace rows of at most
-// kTraceMaxWords words (n <= 512) and kTraceMinShots shots or
+// kTraceMaxWords words (n <= 2048) and kTraceMinShots shots or
 // kTraceMinQudits qudits, unless SDIM_FLAG_TRACE (any shot count) or a flag
 // that names another engine.
 bool use_trace(const Job& j, unsigned flags) {
@@ -512,7 +512,8 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       // two shots per lane from kPhasePairMinShots (four measured slower on
       // the L = 7 surface step: 0.31 against 0.20 ms, the lanes' registers
       // leave five warps per SM); SDIM_FLAG_LANE_SHOTS_1 keeps one
-      const int sp = shots >= kPhasePairMinShots && !(flags & SDIM_FLAG_LANE_SHOTS_1) ? 2 : 1;
+      const int sp = shots >= kPhasePairMinShots && tw <= kPhasePairMaxWords && !(flags & SDIM_FLAG_LANE_SHOTS_1)
+                         ? 2 : 1;
       for (size_t i = b; i < e; ++i) spl[i] = sp;
       b = e;
     }

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
 // registers.  Up to 16-word rows and one shot per lane, 32 blocks per SM at
 // 64 registers; wider rows or two shots per lane get 128.
 template <int TW, int SPL>
-__global__ void __launch_bounds__(32, (TW >= 16 || SPL == 2) ? 16 : 32)
+__global__ void __launch_bounds__(32, TW >= 64 ? 8 : (TW >= 16 || SPL == 2) ? 16 : 32)
     k_phase_pass(const TraceDesc* __restrict__ descs, int ndesc, long long total_groups, const int* status) {
   __shared__ uint8_t rec[32 * SPL * kRecStride];
   if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
@@ -125,8 +125,16 @@ bool launch_phase_spl(int tw, int grid, int block, cudaStream_t s, const TraceDe
     case 8: k_phase_pass<8, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
     case 16: k_phase_pass<16, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
     case 32: k_phase_pass<32, SPL><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
-    default: return false;
+    default: break;
   }
+  if constexpr (SPL == 1) {  // wider rows: one shot per lane (n <= 2048)
+    switch (tw) {
+      case 64: k_phase_pass<64, 1><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+      case 128: k_phase_pass<128, 1><<<grid, block, 0, s>>>(descs, ndesc, total_groups, status); return true;
+      default: break;
+    }
+  }
+  return false;
 }
 
 bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,

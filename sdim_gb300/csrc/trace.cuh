@@ -107,8 +107,11 @@ __host__ __device__ inline void trace_offsets_u8(int nm, int nn1, int sw, size_t
   o[4] = o[3] + round_up((size_t)nn1 * 8, 256);
 }
 
-// Widest trace row the phase pass has an instance for (n <= 512).
-constexpr int kTraceMaxWords = 32;
+// Widest trace row the phase pass has an instance for (n <= 2048).  Rows of
+// up to 32 words (n <= 512) keep two shots per lane from kPhasePairMinShots
+// shots on; wider rows keep one.
+constexpr int kTraceMaxWords = 128;
+constexpr int kPhasePairMaxWords = 32;
 
 // Words per trace row for n qudits, 0 when n is too large for the phase pass.
 __host__ __device__ inline int trace_words(int n) {

@@ -24,7 +24,7 @@ def test_candidates_d2_within_the_trace_limit():
 
 
 def test_candidates_past_the_d2_trace_limit_and_large_n_teams():
-    c = _names(autotune.program_candidates(2, 600, 20, OPTIN, SMS))
+    c = _names(autotune.program_candidates(2, 2100, 20, OPTIN, SMS))
     assert not any(name.startswith("trace") for name in c)
     assert "shot groups, one per warp" in c and "one warp per shot" in c
 

@@ -207,3 +207,24 @@ def test_odd_d_cta_pair_against_oracle(d, n):
     rc = ctx.lib.sdim_run(ctx.ptr, dp.ptr, d, 2, 70, out.ctypes.data, _lib.FLAG_TRACE | _lib.FLAG_SPLIT_XZ)
     _lib.check(rc, ctx.ptr, "odd-d trace on a CTA pair")
     assert np.array_equal(out, oracle_run([spec], d, 2, 70)["records"]), (d, n)
+
+
+@pytest.mark.parametrize("n", [513, 700, 1024, 1025, 1500, 2048])
+def test_wide_rows_past_512_qudits(n):
+    """Trace rows of 64 and 128 words (n up to 2048, x / z tableau in global
+    memory, one shot per phase-pass lane) with MEASURE+RESET rounds and
+    depolarizing noise: all 70 shots against the shot-group engine, and up
+    to n = 1025 the first two against the oracle (about 20 core-seconds a
+    shot at n = 1024)."""
+    base = workloads.random_hpc(n, 2, 3 * n, seed=950 + n, mr_every=n, mr_fraction=0.1)
+    ops = []
+    for op in base.ops:
+        ops.append(op)
+        if op[0] in ("H", "CNOT"):
+            ops.append(("N1", op[1], None, {"noise_channel": "d", "prob": 0.01}))
+    spec = workloads.CircuitSpec(n, 2, ops, f"wide_n{n}")
+    prog = Program(spec.build())
+    rec = prog.sample(70, seed=n, engine="trace")
+    assert np.array_equal(rec, prog.sample(70, seed=n, engine="group")), n
+    if n <= 1025:
+        assert np.array_equal(rec[:2], oracle_run([spec], n, 0, 2)["records"]), n
