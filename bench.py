@@ -1078,7 +1078,12 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
     l2 = l2_peak(ctx)
     odd_trace = sum(1 for e in entries if e.program.enc.d != 2 and e.program.enc.n <= TRACE_U8_MAX_QUDITS
                     and trace_routed(e.program.enc.n, e.program.enc.d, e.shots))
-    gb, t_min, streamed, in_l2 = 0.0, 0.0, 0.0, 0.0
+    # t_packed: the same bound with the x / z bytes of d = 5, 7 trace programs
+    # at the 4-bit lanes their batched x / z pass stores (half of the byte
+    # figure the survey's model charges; its d = 3 figure is already two bit
+    # planes)
+    packed_run = 2 * odd_trace >= ctx.num_sms
+    gb, t_min, t_packed, streamed, in_l2 = 0.0, 0.0, 0.0, 0.0, 0.0
     for e, o in zip(entries, offs[:-1]):
         enc = e.program.enc
         nr = e.program.num_records
@@ -1087,8 +1092,11 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
         xz = algorithmic_bytes_per_shot(enc, det_row, enc.n, enc.d) * (1 if on_trace else -(-e.shots // 32))
         delta = e.shots * group_delta_bytes_per_shot(enc, det_row, 0.0, enc.n, enc.d)
         place = tableau_place(enc.n, enc.d, on_trace, ctx.smem_optin, odd_trace, ctx.num_sms)
+        bw = {"smem": peak, "l2": l2, "hbm": hbm}[place]
         gb += xz + delta
-        t_min += (xz / {"smem": peak, "l2": l2, "hbm": hbm}[place] + delta / peak) / 1e9
+        t_min += (xz / bw + delta / peak) / 1e9
+        xz_p = xz / 2 if (on_trace and packed_run and enc.d in (5, 7)) else xz
+        t_packed += (xz_p / bw + delta / peak) / 1e9
         streamed += xz if place == "hbm" else 0.0
         in_l2 += xz if place == "l2" else 0.0
     mean_kern = statistics.mean(kern_ms)
@@ -1151,7 +1159,10 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
                                     "sdim_probe_smem_bandwidth / sdim_probe_l2_bandwidth; HBM from "
                                     "MEASURED_PEAKS.json",
                      "bytes_model": "x/z tableau updates once per program (trace engines) or per 32-shot group, "
-                                    "plus per-shot phase-delta bytes; frac = bound_ms / kernel_ms"},
+                                    "plus per-shot phase-delta bytes; frac = bound_ms / kernel_ms",
+                     "packed": {"bound_ms": t_packed * 1e3, "frac": t_packed * 1e3 / mean_kern,
+                                "model": "the same bound with d = 5, 7 trace x/z bytes at 4-bit lanes (half), as "
+                                         "the batched packed x/z pass stores them"}},
         "cpu_baseline": cpu,
         # one persistent launch per (dimension, team kind) present in the batch
         "gpu_launches": steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),
