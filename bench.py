@@ -381,7 +381,12 @@ def _split_stride(c):
     return s if (s >> 2) & 1 else s + 4
 
 
-def p3_single_cta(n, smem_optin):
+def packed_threads(n, few):
+    """Threads of a packed x / z pass CTA (the library's packed_threads)."""
+    return 1024 if few and n >= 128 else max(64, min(512, (n + 31) & ~31))
+
+
+def p3_single_cta(n, smem_optin, threads=512):
     """Whether the d = 3 bit-plane x / z pass of n qudits keeps its tableau in
     one CTA's shared memory: rows of W = 2 ceil(n / 32) plane pairs (8 bytes)
     at an odd stride, a hot part of 3 W + 2 W / 2 + 512 pairs and two n-byte
@@ -389,12 +394,12 @@ def p3_single_cta(n, smem_optin):
     wh = (n + 31) // 32
     w = 2 * wh
     r16 = lambda x: (x + 15) & ~15  # noqa: E731
-    hot = r16((3 * w + 2 * wh + 512) * 8 + 2 * ((n + 15) & ~15))
+    hot = r16((3 * w + 2 * wh + threads) * 8 + 2 * ((n + 15) & ~15))
     xz = r16(2 * n * (w | 1) * 8)
     return hot + xz + 4096 + 4096 <= smem_optin
 
 
-def n4_single_cta(n, d, smem_optin):
+def n4_single_cta(n, d, smem_optin, threads=512):
     """Whether the d = 5 / 7 4-bit-lane x / z pass of n qudits keeps its
     tableau in one CTA's shared memory: rows of W = 2 ceil(n / 8) words at an
     odd stride, a hot part of 3 W + W / 2 * 2 + (d - 1) (W + 512) words and two
@@ -402,7 +407,7 @@ def n4_single_cta(n, d, smem_optin):
     wh = (n + 7) // 8
     w = 2 * wh
     r16 = lambda x: (x + 15) & ~15  # noqa: E731
-    hot = r16((3 * w + 2 * wh + (d - 1) * w + (d - 1) * 512) * 4 + 2 * ((n + 15) & ~15))
+    hot = r16((3 * w + 2 * wh + (d - 1) * w + (d - 1) * threads) * 4 + 2 * ((n + 15) & ~15))
     xz = r16(2 * n * (w | 1) * 4)
     return hot + xz + 4096 + 4096 <= smem_optin
 
@@ -418,7 +423,8 @@ def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=11):
     HBM above; in a smaller batch a cluster of 8 CTAs, columns in shared
     memory up to n = 636 and streamed from global memory, held in L2, above."""
     if d in (3, 5, 7) and 2 * odd_trace_programs >= num_sms:
-        fits = p3_single_cta(n, smem_optin) if d == 3 else n4_single_cta(n, d, smem_optin)
+        th = packed_threads(n, False)
+        fits = p3_single_cta(n, smem_optin, th) if d == 3 else n4_single_cta(n, d, smem_optin, th)
         return 1, ("smem" if fits else "hbm")
     if u8_single_cta(n, smem_optin):
         return 1, "smem"

@@ -411,6 +411,15 @@ constexpr int kTraceU8MaxQudits = 2048;
 // memory (7) up to n = 320, else a global-memory slot (8).  A cluster shares each
 // measurement's fixed cost (two cluster barriers, pivot search, broadcast)
 // among 8 SMs, so it finishes one program sooner but a full batch later.
+// Threads of a packed odd-d x / z pass CTA for programs of up to n qudits:
+// about one per qudit (64 to 512) in a batch, where more warps would only
+// spend issue slots walking the instruction stream; 1024 for a few programs
+// of 128+ qudits, whose rank-1 updates then spread over more row groups.
+int packed_threads(int n, bool few) {
+  if (few && n >= 128) return 1024;
+  return std::max(64, std::min(kTracePassThreads, (n + 31) & ~31));
+}
+
 int odd_xz_mode(int n, int d, long long programs, unsigned flags, size_t optin, int num_sms) {
   const size_t win = trace_u8_window_bytes();
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
@@ -422,10 +431,11 @@ int odd_xz_mode(int n, int d, long long programs, unsigned flags, size_t optin, 
   const bool packed = (d == 3 || d == 5 || d == 7) &&
                       !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ)) &&
                       (!few || (flags & SDIM_FLAG_PACKED_XZ));
+  const int th = packed_threads(n, few);
   if (packed && d == 3)
-    return !force_gmem && trace_p3_hot_bytes(n) + trace_p3_xz_bytes(n) + win + 4096 <= optin ? 5 : 6;
+    return !force_gmem && trace_p3_hot_bytes(n, th) + trace_p3_xz_bytes(n) + win + 4096 <= optin ? 5 : 6;
   if (packed)
-    return !force_gmem && trace_n4_hot_bytes(n, d) + trace_n4_xz_bytes(n) + win + 4096 <= optin ? 7 : 8;
+    return !force_gmem && trace_n4_hot_bytes(n, d, th) + trace_n4_xz_bytes(n) + win + 4096 <= optin ? 7 : 8;
   const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
   const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
   const bool cl_smem = trace_u8_cluster_hot(n) + trace_u8_cluster_xz(n) + win + 4096 <= optin;
@@ -704,23 +714,21 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       // d = 5, 7 on 4-bit lanes: one CTA per program, largest first
       const bool in_smem = mode == 7;
       const int dd = hu[b].c.d;
-      const size_t hot = trace_n4_hot_bytes(nmax, dd), xz = trace_n4_xz_bytes(nmax);
+      const int block = packed_threads(nmax, 2 * (long long)ku < ctx->num_sms);
+      const size_t hot = trace_n4_hot_bytes(nmax, dd, block), xz = trace_n4_xz_bytes(nmax);
       int grid = (int)std::min<size_t>(e - b, 65535);
       if (!in_smem) grid = std::min(grid, 2 * ctx->num_sms);
       unsigned* queue = in_smem ? nullptr : static_cast<unsigned*>(ctx->xz_queue.p) + r;
-      const int block = std::max(64, std::min(kTracePassThreads, (nmax + 31) & ~31));
       launch_trace_n4(dd, grid, block, hot + (in_smem ? xz : 0) + win, rs, du + b, (int)(e - b),
                       static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, queue, status);
     } else if (mode >= 5) {
       // d = 3 on bit planes: one CTA per program, largest first
       const bool in_smem = mode == 5;
-      const size_t hot = trace_p3_hot_bytes(nmax), xz = trace_p3_xz_bytes(nmax);
+      const int block = packed_threads(nmax, 2 * (long long)ku < ctx->num_sms);
+      const size_t hot = trace_p3_hot_bytes(nmax, block), xz = trace_p3_xz_bytes(nmax);
       int grid = (int)std::min<size_t>(e - b, 65535);
       if (!in_smem) grid = std::min(grid, 2 * ctx->num_sms);
       unsigned* queue = in_smem ? nullptr : static_cast<unsigned*>(ctx->xz_queue.p) + r;
-      // about one thread per qudit (64 to 512): the warps of a larger CTA
-      // would only spend issue slots walking the instruction stream
-      const int block = std::max(64, std::min(kTracePassThreads, (nmax + 31) & ~31));
       launch_trace_p3(grid, block, hot + (in_smem ? xz : 0) + win, rs, du + b, (int)(e - b),
                       static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, queue, status);
     } else if (mode == 1) {

@@ -202,11 +202,11 @@ void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaSt
                            int nd, long long total, int* status);
 
 // x / z pass for d = 3 on bit planes (k_trace_p3.cu): one CTA of block (64
-// to 512) threads per program, x / z in shared memory after the hot part when
+// to 512, or 1024) threads per program, x / z in shared memory after the hot part when
 // in_smem, else at gxz + blockIdx.x * xzb with programs taken from queue;
 // the instruction window (trace_u8_window_bytes) follows in shared memory.
 // Writes the same trace as the byte-residue passes.
-size_t trace_p3_hot_bytes(int n);
+size_t trace_p3_hot_bytes(int n, int threads);
 size_t trace_p3_xz_bytes(int n);
 cudaError_t trace_p3_set_smem(int optin);
 void launch_trace_p3(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
@@ -214,7 +214,7 @@ void launch_trace_p3(int grid, int block, size_t smem, cudaStream_t s, const Tra
 
 // x / z pass for d = 5 and 7 on 4-bit residue lanes (k_trace_n4.cu), in the
 // same form as the d = 3 bit-plane pass.
-size_t trace_n4_hot_bytes(int n, int d);
+size_t trace_n4_hot_bytes(int n, int d, int threads);
 size_t trace_n4_xz_bytes(int n);
 cudaError_t trace_n4_set_smem(int optin);
 void launch_trace_n4(int d, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* dsc, int nd,

@@ -25,8 +25,10 @@
 
 namespace sdim {
 
-// (word, row group) threads of the rank-1 update, at most.
+// Threads of a CTA of the pass: up to 512 in batches (two CTAs per SM), 1024
+// for a lone program (its rank-1 update spread over more row groups).
 constexpr int kN4Threads = 512;
+constexpr int kN4WideThreads = 1024;
 
 template <int DD>
 struct N4Layout {
@@ -39,10 +41,10 @@ struct N4Layout {
   }
   __host__ __device__ size_t xz_bytes() const { return (size_t)2 * n * RS * 4; }
   // C, FW, DOT (W words each), F, H (Wh each), the multiples c * FW
-  // (d - 1 rows of W words), the row-group partial sums ((d - 1) x
-  // kN4Threads words), CX and CZ (np bytes each)
-  __host__ __device__ size_t hot_bytes() const {
-    return (size_t)(3 * W + 2 * Wh + (DD - 1) * W + (DD - 1) * kN4Threads) * 4 + 2 * (size_t)np;
+  // (d - 1 rows of W words), the row-group partial sums ((d - 1) x threads
+  // words for a CTA of `threads`), CX and CZ (np bytes each)
+  __host__ __device__ size_t hot_bytes(int threads) const {
+    return (size_t)(3 * W + 2 * Wh + (DD - 1) * W + (DD - 1) * threads) * 4 + 2 * (size_t)np;
   }
 };
 
@@ -53,8 +55,10 @@ struct TabN4 {
   N4Layout<DD> L;
   uint32_t *X, *Z, *C, *FW, *DOT, *F, *H, *FWC, *part;
   uint8_t *CX, *CZ;
+  int pcap;  // row-group partial sums per pivot value: the CTA's threads
 
-  __device__ TabN4(uint8_t* xz, uint8_t* hot, int n, CtaTeam team) : tm(team), L(n) {
+  __device__ TabN4(uint8_t* xz, uint8_t* hot, int n, CtaTeam team, int threads)
+      : tm(team), L(n), pcap(threads) {
     X = reinterpret_cast<uint32_t*>(xz);
     Z = X + (size_t)n * L.RS;
     C = reinterpret_cast<uint32_t*>(hot);
@@ -63,8 +67,8 @@ struct TabN4 {
     F = DOT + L.W;
     H = F + L.Wh;
     FWC = H + L.Wh;              // FWC[(c - 1) W + w] = c * FW[w]
-    part = FWC + (DD - 1) * L.W;  // part[(c - 1) kN4Threads + r W + w]
-    CX = reinterpret_cast<uint8_t*>(part + (DD - 1) * kN4Threads);
+    part = FWC + (DD - 1) * L.W;  // part[(c - 1) pcap + r W + w]
+    CX = reinterpret_cast<uint8_t*>(part + (DD - 1) * pcap);
     CZ = CX + L.np;
   }
 
@@ -242,7 +246,7 @@ __device__ void trace_measure_n4(TabN4<DD>& e, const TraceDescU8& td, int q, uin
     e.row_bytes(e.FW, 0, 2 * n, row, sw);
     // rank-1 update of X and Z, (word, row group) threads; row-group sums of
     // the old Z rows per pivot value c for the column dots
-    const int W = L.W, R = max(1, min(min(size, kN4Threads) / W, (n + 3) >> 2));
+    const int W = L.W, R = max(1, min(min(size, e.pcap) / W, (n + 3) >> 2));
     if (t < R * W) {
       const int w = t % W, r = t / W;
       uint32_t acc[DD - 1];
@@ -284,7 +288,7 @@ __device__ void trace_measure_n4(TabN4<DD>& e, const TraceDescU8& td, int q, uin
         }
       }
 #pragma unroll
-      for (int c = 0; c < DD - 1; ++c) e.part[c * kN4Threads + r * W + w] = acc[c];
+      for (int c = 0; c < DD - 1; ++c) e.part[c * e.pcap + r * W + w] = acc[c];
     }
     e.tm.sync();
     // phases of the absorbing generators: c += phc f + f DOT + s1 f (f - 1) / 2
@@ -295,7 +299,7 @@ __device__ void trace_measure_n4(TabN4<DD>& e, const TraceDescU8& td, int q, uin
 #pragma unroll
       for (int c = 1; c < DD; ++c) {
         uint32_t sc = 0u;
-        for (int r = 0; r < R; ++r) sc = M::add(sc, e.part[(c - 1) * kN4Threads + r * W + w]);
+        for (int r = 0; r < R; ++r) sc = M::add(sc, e.part[(c - 1) * e.pcap + r * W + w]);
         dot = M::add(dot, M::mulc(sc, c));
       }
       C[w] = M::add(C[w], M::add(M::mulc(f, phc), M::add(M::mul(f, dot), M::mulc(M::half(f), s1))));

@@ -31,8 +31,10 @@
 
 namespace sdim {
 
-// Row-group partial dots: at most this many (word, row group) threads.
+// Threads of a CTA of the pass: up to 512 in batches (two CTAs per SM), 1024
+// for a lone program (its rank-1 update spread over more row groups).
 constexpr int kP3Threads = 512;
+constexpr int kP3WideThreads = 1024;
 
 struct P3Layout {
   int n, Wh, W, RS, np;
@@ -45,9 +47,9 @@ struct P3Layout {
   // bytes of X and Z
   __host__ __device__ size_t xz_bytes() const { return (size_t)2 * n * RS * sizeof(P3); }
   // bytes of C, FW, DOT (W pairs each), F, H (Wh each), the row-group partial
-  // dots, CX and CZ (np bytes each)
-  __host__ __device__ size_t hot_bytes() const {
-    return (size_t)(3 * W + 2 * Wh + kP3Threads) * sizeof(P3) + 2 * (size_t)np;
+  // dots (one pair per thread of a CTA of `threads`), CX and CZ (np bytes each)
+  __host__ __device__ size_t hot_bytes(int threads) const {
+    return (size_t)(3 * W + 2 * Wh + threads) * sizeof(P3) + 2 * (size_t)np;
   }
 };
 
@@ -56,8 +58,10 @@ struct TabP3 {
   P3Layout L;
   P3 *X, *Z, *C, *FW, *DOT, *F, *H, *part;
   uint8_t *CX, *CZ;
+  int pcap;  // row-group partial dots: the CTA's threads
 
-  __device__ TabP3(uint8_t* xz, uint8_t* hot, int n, CtaTeam team) : tm(team), L(n) {
+  __device__ TabP3(uint8_t* xz, uint8_t* hot, int n, CtaTeam team, int threads)
+      : tm(team), L(n), pcap(threads) {
     X = reinterpret_cast<P3*>(xz);
     Z = X + (size_t)n * L.RS;
     C = reinterpret_cast<P3*>(hot);
@@ -66,7 +70,7 @@ struct TabP3 {
     F = DOT + L.W;
     H = F + L.Wh;
     part = H + L.Wh;
-    CX = reinterpret_cast<uint8_t*>(part + kP3Threads);
+    CX = reinterpret_cast<uint8_t*>(part + pcap);
     CZ = CX + L.np;
   }
 
@@ -226,7 +230,7 @@ __device__ void trace_measure_p3(TabP3& e, const TraceDescU8& td, int q, uint32_
     e.row_bytes(e.FW, 0, 2 * n, row, sw);
     // rank-1 update of X and Z and the column dots, (word, row group) threads;
     // at least four rows per group, so that few partial dots are summed
-    const int W = L.W, R = max(1, min(min(size, kP3Threads) / W, (n + 3) >> 2));
+    const int W = L.W, R = max(1, min(min(size, e.pcap) / W, (n + 3) >> 2));
     if (t < R * W) {
       const int w = t % W, r = t / W;
       const P3 f1 = e.FW[w], f2 = p3_neg(f1);
