@@ -415,15 +415,17 @@ def n4_single_cta(n, d, smem_optin, threads=512):
 def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=11):
     """Where the library runs the odd-d x / z pass of n qudits, as (CTAs per
     program, where its columns live: "smem", "l2" or "hbm").  In a batch of
-    at least num_sms / 2 odd-d trace programs, d = 3, 5, 7 run on one CTA with
-    the packed tableau (bit planes, 4-bit lanes), in shared memory when it
-    fits, else streamed from HBM.  Otherwise (other d, smaller batches) one
+    at least num_sms / 2 odd-d trace programs, and in smaller ones for
+    128 <= n while the byte tableau would fit one CTA, d = 3, 5, 7 run on one
+    CTA with the packed tableau (bit planes, 4-bit lanes), in shared memory
+    when it fits, else streamed from HBM.  Otherwise (other d, smaller batches) one
     CTA when the byte tableau fits in shared memory; else, in a batch of at
     least num_sms / 2, a CTA pair when that fits and one CTA streaming from
     HBM above; in a smaller batch a cluster of 8 CTAs, columns in shared
     memory up to n = 636 and streamed from global memory, held in L2, above."""
-    if d in (3, 5, 7) and 2 * odd_trace_programs >= num_sms:
-        th = packed_threads(n, False)
+    few = 2 * odd_trace_programs < num_sms
+    if d in (3, 5, 7) and (not few or (n >= 128 and u8_single_cta(n, smem_optin))):
+        th = packed_threads(n, few)
         fits = p3_single_cta(n, smem_optin, th) if d == 3 else n4_single_cta(n, d, smem_optin, th)
         return 1, ("smem" if fits else "hbm")
     if u8_single_cta(n, smem_optin):

@@ -424,19 +424,21 @@ int odd_xz_mode(int n, int d, long long programs, unsigned flags, size_t optin, 
   const size_t win = trace_u8_window_bytes();
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
   const bool few = programs * 2 < (long long)num_sms;
-  // packed tableaux for batches (throughput: a quarter or half of the bytes),
-  // the byte forms for a few programs (latency: on GB300 a lone d = 5,
-  // n = 256 program's x / z pass took 4.38 ms on 4-bit lanes in one CTA and
-  // 3.17 ms on the byte cluster; PR1's 0.31 ms on bit planes, 0.26 on bytes)
+  const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
+  // packed tableaux for batches (throughput: a quarter or half of the bytes);
+  // for a few programs (latency) only where the byte tableau would sit in one
+  // CTA and n >= 128.  On GB300, lone programs: d = 5, n = 180 1.27 ms packed
+  // against 1.46 on one byte CTA, d = 3, n = 200 1.32 against 1.66; but
+  // d = 5, n = 256 4.32 against 3.16 on the byte cluster, d = 7, n = 600
+  // 11.5 against 5.6 on the streamed cluster, PR1 (n = 32) 0.31 against 0.26
   const bool packed = (d == 3 || d == 5 || d == 7) &&
                       !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ)) &&
-                      (!few || (flags & SDIM_FLAG_PACKED_XZ));
+                      (!few || (flags & SDIM_FLAG_PACKED_XZ) || (single && n >= 128));
   const int th = packed_threads(n, few);
   if (packed && d == 3)
     return !force_gmem && trace_p3_hot_bytes(n, th) + trace_p3_xz_bytes(n) + win + 4096 <= optin ? 5 : 6;
   if (packed)
     return !force_gmem && trace_n4_hot_bytes(n, d, th) + trace_n4_xz_bytes(n) + win + 4096 <= optin ? 7 : 8;
-  const bool single = trace_u8_hot_bytes(n) + trace_u8_xz_bytes(n) + win + 4096 <= optin;
   const bool pair = trace_u8_split_smem(n) + win + 4096 <= optin;
   const bool cl_smem = trace_u8_cluster_hot(n) + trace_u8_cluster_xz(n) + win + 4096 <= optin;
   if (flags & SDIM_FLAG_CLUSTER_XZ) return cl_smem && !force_gmem ? 3 : 4;

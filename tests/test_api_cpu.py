@@ -186,7 +186,7 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     assert mode(10, 1, 0, 4) == _lib.SDIM_EINVAL
     packed = _lib.FLAG_PACKED_XZ
     assert [mode(n, 1000, 0, 3) for n in (1, 448, 449, 2048)] == [5, 5, 6, 6]
-    assert [mode(n, 75, 0, 3) for n in (1, 226, 227, 2048)] == [0, 0, 3, 4]
+    assert [mode(n, 75, 0, 3) for n in (1, 127, 128, 226, 227, 2048)] == [0, 0, 5, 5, 3, 4]
     assert [mode(n, 75, packed, 3) for n in (1, 448, 449, 2048)] == [5, 5, 6, 6]
     assert mode(100, 1000, _lib.FLAG_FORCE_GMEM, 3) == mode(100, 1, packed | _lib.FLAG_FORCE_GMEM, 3) == 6
     assert mode(300, 1000, _lib.FLAG_U8_XZ, 3) == mode(300, 1000, _lib.FLAG_U8_XZ, 5) == mode(300, 1000) == 1
@@ -195,7 +195,7 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     # (more room for its row-group sums), so the shared-memory limits differ
     for d, batch_max, lone_max in ((5, 324, 315), (7, 320, 310)):
         assert [mode(n, 1000, 0, d) for n in (1, 256, batch_max, batch_max + 1, 2048)] == [7, 7, 7, 8, 8]
-        assert [mode(n, 75, 0, d) for n in (226, 227, 636, 637)] == [0, 3, 3, 4]
+        assert [mode(n, 75, 0, d) for n in (127, 128, 226, 227, 636, 637)] == [0, 7, 7, 3, 3, 4]
         assert [mode(n, 1, packed, d) for n in (256, lone_max, lone_max + 1)] == [7, 7, 8]
         assert mode(100, 1, packed | _lib.FLAG_FORCE_GMEM, d) == 8
     forms = {0: (1, "smem"), 1: (2, "smem"), 2: (1, "hbm"), 3: (8, "smem"), 4: (8, "l2"), 5: (1, "smem"),
