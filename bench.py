@@ -84,6 +84,9 @@ def parse():
                     help="time the selected engine's step only, no other legs (for profiling runs)")
     ap.add_argument("--engine", default="auto", choices=["auto", "trace", "group", "per_shot"],
                     help="batched engine of the timed run (auto: the library's choice)")
+    ap.add_argument("--xz", default="auto", choices=["auto", "packed", "bytes"],
+                    help="odd-d trace engine: x/z pass on the packed tableau (bit planes / 4-bit lanes) or on "
+                         "residue bytes whatever the batch size (auto: the library's choice)")
     ap.add_argument("--route", default="tableau", choices=["tableau", "frame"],
                     help="with --quick: time the tableau route or the frame route (sdim_frame_run)")
     return ap.parse_args()
@@ -681,6 +684,7 @@ def run_single(args, torch, dist, ws, rank, local):
     timer = Timer(torch, stream, ctx, ws, dist)
 
     engine_flags = _lib.engine_flags(None if args.engine == "auto" else args.engine)
+    engine_flags |= {"auto": 0, "packed": _lib.FLAG_PACKED_XZ, "bytes": _lib.FLAG_U8_XZ}[args.xz]
     trace_used = (d == 2 and trace_words(n) > 0 and
                   (args.engine == "trace" or (args.engine == "auto" and trace_routed(n, d, shots))))
     odd_trace_used = (d != 2 and n <= TRACE_U8_MAX_QUDITS and
