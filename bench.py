@@ -1067,7 +1067,7 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
         graph = graph_replay(args, torch, ctx, timer, stream, entries, units_per_step, lambda: ref_out[:-1])
         _leg("uneven: graph replay", t_leg)
     tuned = None
-    if rank == 0 and args.autotune:
+    if rank == 0 and (args.autotune or sub):
         # the autotuner over the batch-wide routes (records checked equal to
         # the default route's; kernel time by the library's CUDA events)
         t_leg = time.perf_counter()
@@ -1075,7 +1075,11 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
         res = Autotuner(ctx, reps=2).tune_batch(br)
         tuned = {"best": res.best.name, "flags": res.best.flags, "kernel_ms": res.times_ms,
                  "aborted_after_one_run": res.aborted,
-                 "value": units_per_step / (res.times_ms[res.best.name] / 1e3), "unit": UNIT}
+                 "value": units_per_step / (res.times_ms[res.best.name] / 1e3), "unit": UNIT,
+                 "form": "Autotuner.tune_batch: every batch-wide route (trace engines at any shot count, shot groups "
+                         "only, CTA-pair / cluster / byte / packed odd-d x/z passes, d = 2 coins in the phase pass, "
+                         "one shot per phase-pass lane) timed by the library's CUDA events, median of 2 runs after "
+                         "a warm-up, records checked equal to the default route's"}
         _leg("uneven: autotuner", t_leg)
 
     # algorithmic bytes: det flags per program from its first shot.  The x / z
