@@ -65,6 +65,14 @@ extern "C" {
                                        4-bit lanes) also for runs of fewer than 76 odd-d trace programs */
 #define SDIM_FLAG_LANE_SHOTS_1 65536u /* d = 2 trace engine: one shot per phase-pass lane (by default two
                                          from 77,824 shots in one launch) */
+#define SDIM_FLAG_REUSE_XZ 262144u /* d = 2 trace engine, one program per call: keep the program's x / z
+                                      trace on the device (with the sdim_circuit) and, once a synchronous
+                                      call with this flag has written it and ended without an error,
+                                      replay it in later calls with this flag without running the x / z
+                                      pass (the trace depends on the program alone, not on the seed or
+                                      the shots).  Calls that use the kept trace must be ordered on the
+                                      device after the call that wrote it (one stream, or synchronous
+                                      calls); asynchronous calls and graph capture never make it valid */
 #define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
                                        into the host buffer directly, with no device buffer and no copy
                                        (by default records go to device memory, then one copy down) */
@@ -236,8 +244,10 @@ int sdim_host_free(void* p);
 /* Milliseconds of the kernels of the last call made with SDIM_FLAG_TIME. */
 double sdim_last_kernel_ms(const sdim_ctx* ctx);
 /* The same span split by stage: out[0] the trace engine's x / z passes,
- * out[1] its phase passes, out[2] every other engine's kernels.  No
- * counterpart in the reference (its shot loop is not staged). */
+ * out[1] its phase passes, out[2] every other engine's kernels.  In a batch
+ * that has both, the shot-group engines run on their own stream beside the
+ * trace engines: out[2] is then their own span, which overlaps out[0] and
+ * out[1].  No counterpart in the reference (its shot loop is not staged). */
 int sdim_last_stage_ms(const sdim_ctx* ctx, double out[3]);
 /* Two passes of that span timed by themselves: out[0] from the start of the
  * kernels to the end of the last x / z pass (the coin pass runs alongside on

@@ -35,6 +35,7 @@ FLAG_DIRECT_HOST = 8192
 FLAG_U8_XZ = 16384
 FLAG_PACKED_XZ = 131072
 FLAG_LANE_SHOTS_1 = 65536
+FLAG_REUSE_XZ = 262144
 
 
 def engine_flags(engine) -> int:

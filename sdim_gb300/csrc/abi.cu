@@ -57,7 +57,11 @@ struct sdim_ctx {
   size_t gmem_slot_budget = (size_t)8 << 30;
   std::string err;
   DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace, masks, tdescs_u8, trace_u8, xz_u8;
+  DevBuf gslots_xz;  // d = 2 x / z pass tableaux in global memory (gslots: the shot-group engines')
   cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
+  cudaStream_t grp = nullptr;                      // shot-group engines of a batch with trace programs
+  cudaEvent_t ev_gf = nullptr, ev_gj = nullptr;    // fork to and join from grp
+  cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr;    // shot-group engines' span on grp (SDIM_FLAG_TIME)
   static constexpr int kXzStreams = 3;
   cudaStream_t xzs[kXzStreams] = {};               // odd-d x / z passes of different runs, concurrently
   cudaEvent_t ev_xzf = nullptr, ev_xzj[kXzStreams] = {};
@@ -72,6 +76,7 @@ struct sdim_ctx {
   bool timing_pending = false;
   bool stages_recorded = false;  // ev_xz / ev_phase belong to the pending span
   bool coin_recorded = false;    // ev_c0 / ev_c1 belong to the pending span
+  bool group_recorded = false;   // ev_g0 / ev_g1 belong to the pending span
   double last_ms = 0.0;
   double stage_ms[3] = {0.0, 0.0, 0.0};  // x / z passes, phase passes, other engines
   double pass_ms[2] = {0.0, 0.0};        // x / z passes alone, coin pass alone
@@ -80,6 +85,7 @@ struct sdim_ctx {
   bool frame_smem_set = false;
   int trace_threads = kTracePassThreads;  // x / z pass CTA size (SDIM_TRACE_PASS_THREADS: 256 or 512)
   GraphCapture* capture = nullptr;  // set while sdim_graph_create runs on its private context
+  sdim_circuit* xz_pending = nullptr;  // circuit whose kept trace the current call writes (SDIM_FLAG_REUSE_XZ)
   unsigned long long reallocs = 0;  // device buffers moved by ensure()
 };
 
@@ -122,6 +128,12 @@ struct sdim_circuit {
   int nsteps = 0, nwins = 0, nn1_used = 0;
   int64_t fops_off = 0;  // frame instruction stream (frame.cuh), inside the blob
   int nfops = 0;
+  // d = 2 x / z trace kept on the device for SDIM_FLAG_REUSE_XZ: written by a
+  // run with the flag, valid once that synchronous run has ended without a
+  // device error, then read by the later runs with the flag instead of
+  // running the x / z pass again (it depends only on the program)
+  DevBuf xz_trace;
+  bool xz_trace_valid = false;
 };
 
 namespace {
@@ -279,16 +291,26 @@ int collect_times(sdim_ctx* ctx) {
     c = all;
   }
   if (ctx->coin_recorded) CK(cudaEventElapsedTime(&co, ctx->ev_c0, ctx->ev_c1));
+  if (ctx->group_recorded) CK(cudaEventElapsedTime(&c, ctx->ev_g0, ctx->ev_g1));  // on their own stream
   ctx->pass_ms[0] = xo;
   ctx->pass_ms[1] = co;
   ctx->stages_recorded = false;
   ctx->coin_recorded = false;
+  ctx->group_recorded = false;
   ctx->last_ms = all;
   ctx->stage_ms[0] = a;
   ctx->stage_ms[1] = b;
   ctx->stage_ms[2] = c;
   ctx->timing_pending = false;
   return SDIM_OK;
+}
+
+// The end of a synchronous call: a kept x / z trace that it wrote
+// (SDIM_FLAG_REUSE_XZ) becomes valid when the call ended without an error.
+int settle_xz(sdim_ctx* ctx, int rc) {
+  if (ctx->xz_pending && rc == SDIM_OK) ctx->xz_pending->xz_trace_valid = true;
+  ctx->xz_pending = nullptr;
+  return rc;
 }
 
 int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
@@ -298,13 +320,16 @@ int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
   }
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch");
-  if (flags & SDIM_FLAG_ASYNC) return SDIM_OK;
+  if (flags & SDIM_FLAG_ASYNC) {
+    ctx->xz_pending = nullptr;  // not checked, so a trace written now is not kept valid
+    return SDIM_OK;
+  }
   CK(cudaStreamSynchronize(s));
   if (ctx->timing_pending) {
     const int trc = collect_times(ctx);
     if (trc != SDIM_OK) return trc;
   }
-  return read_status(ctx);
+  return settle_xz(ctx, read_status(ctx));
 }
 
 // With SDIM_FLAG_DIRECT_HOST: the device address through which the kernels
@@ -491,6 +516,16 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   std::vector<TraceDesc> hd(k);
   long long coins = 0;
   TraceDesc* dd = nullptr;
+  // SDIM_FLAG_REUSE_XZ, one d = 2 program: its trace lives in the circuit's
+  // own buffer, and a valid one is replayed without the x / z pass
+  sdim_circuit* keep = (flags & SDIM_FLAG_REUSE_XZ) && k == 1 && !ctx->capture
+                           ? const_cast<sdim_circuit*>(jobs[0].c) : nullptr;
+  const bool skip_xz = keep && keep->xz_trace_valid;
+  if (keep && !skip_xz) {
+    rc = ensure(ctx, keep->xz_trace, trace_bytes(keep->nmeas, keep->nn1, trace_words(keep->n)));
+    if (rc != SDIM_OK) return rc;
+    ctx->xz_pending = keep;
+  }
   if (k) {
     std::vector<size_t> off(k);
     size_t total = 0;
@@ -498,7 +533,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       off[i] = total;
       total += trace_bytes(jobs[i].c->nmeas, jobs[i].c->nn1, trace_words(jobs[i].c->n));
     }
-    if ((rc = ensure(ctx, ctx->trace, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
+    if (!keep && (rc = ensure(ctx, ctx->trace, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
     if ((rc = ensure(ctx, ctx->tdescs, sizeof(TraceDesc) * k)) != SDIM_OK) return rc;
     // fire masks: a word pair per 32 N1 ordinals per shot and the chunk map,
     // within a budget
@@ -548,7 +583,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.c.nshots = (int)j.nshots;
       groups += (j.nshots + 32 * spl[i] - 1) / (32 * spl[i]);
       td.spl = spl[i];
-      uint8_t* b = static_cast<uint8_t*>(ctx->trace.p) + off[i];
+      uint8_t* b = keep ? static_cast<uint8_t*>(keep->xz_trace.p) : static_cast<uint8_t*>(ctx->trace.p) + off[i];
       size_t o[4];
       trace_offsets(j.c->nmeas, j.c->nn1, tw, o);
       td.steps = j.c->d_steps;
@@ -632,32 +667,6 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       return rc;
   }
   if (coins) CK(cudaEventRecord(ctx->ev_fork, s));
-  // ---- x / z passes: one CTA per program
-  if (k) {
-    const int nmax = jobs[0].c->n;
-    const size_t hot = trace_pass_hot_bytes(nmax), xz = trace_pass_xz_bytes(nmax);
-    // after the tableau: the schedule window; about 3.2 KB of static shared memory besides
-    const size_t win = trace_pass_window_bytes();
-    const bool in_smem = !force_gmem && hot + xz + win + 4096 <= (size_t)ctx->smem_optin;
-    int grid = (int)std::min<size_t>(k, 65535);
-    if (!in_smem) {
-      grid = std::min(grid, 2 * ctx->num_sms);
-      if ((rc = ensure(ctx, ctx->gslots, xz * (size_t)grid)) != SDIM_OK) return rc;
-    }
-    size_t smem = hot + (in_smem ? xz : 0) + win;
-    if (coins && grid <= ctx->num_sms / 8) {
-      // shared-memory fence: a few x / z CTAs claim enough shared memory that
-      // no coin-pass block fits beside them, so the coin warps do not take
-      // the issue slots of the latency-bound x / z pass on its SM
-      const long long fence = (long long)ctx->smem_per_sm - 2LL * ctx->smem_reserved - (long long)kCoinFenceSmem + 16;
-      const long long cap = (long long)ctx->smem_optin - 4096;  // room for the kernel's static arrays
-      smem = std::max<size_t>(smem, (size_t)std::max(0LL, std::min(fence, cap)));
-    }
-    launch_trace_pass(ctx->trace_threads, grid, smem, s, dd, (int)k, static_cast<uint8_t*>(ctx->gslots.p), xz, hot,
-                      in_smem ? 1 : 0, status);
-    const cudaError_t le = cudaGetLastError();
-    if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
-  }
   // odd d: the x / z pass form of each program (odd_xz_mode)
   const size_t optin = (size_t)ctx->smem_optin;
   const size_t win = trace_u8_window_bytes();
@@ -693,11 +702,41 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     b = e;
   }
   if (slot_total && (rc = ensure(ctx, ctx->xz_u8, slot_total)) != SDIM_OK) return rc;
-  const bool fan = runs.size() > 1;
   if (!runs.empty()) {
     if ((rc = ensure(ctx, ctx->xz_queue, sizeof(unsigned) * runs.size())) != SDIM_OK) return rc;
     CK(cudaMemsetAsync(ctx->xz_queue.p, 0, sizeof(unsigned) * runs.size(), s));
-    if (fan) CK(cudaEventRecord(ctx->ev_xzf, s));
+  }
+  // the odd-d runs go on streams of their own when there are several, or when
+  // the d = 2 x / z passes run on s: all x / z passes of the batch start
+  // together (the uneven batch: x / z stage 295 -> 229 ms)
+  const bool d2_xz = k && !skip_xz;
+  const bool fan = runs.size() > 1 || (d2_xz && !runs.empty());
+  if (fan) CK(cudaEventRecord(ctx->ev_xzf, s));
+  // ---- x / z passes: one CTA per program (none when a kept trace is valid)
+  if (d2_xz) {
+    const int nmax = jobs[0].c->n;
+    const size_t hot = trace_pass_hot_bytes(nmax), xz = trace_pass_xz_bytes(nmax);
+    // after the tableau: the schedule window; about 3.2 KB of static shared memory besides
+    const size_t win = trace_pass_window_bytes();
+    const bool in_smem = !force_gmem && hot + xz + win + 4096 <= (size_t)ctx->smem_optin;
+    int grid = (int)std::min<size_t>(k, 65535);
+    if (!in_smem) {
+      grid = std::min(grid, 2 * ctx->num_sms);
+      if ((rc = ensure(ctx, ctx->gslots_xz, xz * (size_t)grid)) != SDIM_OK) return rc;
+    }
+    size_t smem = hot + (in_smem ? xz : 0) + win;
+    if (coins && grid <= ctx->num_sms / 8) {
+      // shared-memory fence: a few x / z CTAs claim enough shared memory that
+      // no coin-pass block fits beside them, so the coin warps do not take
+      // the issue slots of the latency-bound x / z pass on its SM
+      const long long fence = (long long)ctx->smem_per_sm - 2LL * ctx->smem_reserved - (long long)kCoinFenceSmem + 16;
+      const long long cap = (long long)ctx->smem_optin - 4096;  // room for the kernel's static arrays
+      smem = std::max<size_t>(smem, (size_t)std::max(0LL, std::min(fence, cap)));
+    }
+    launch_trace_pass(ctx->trace_threads, grid, smem, s, dd, (int)k, static_cast<uint8_t*>(ctx->gslots_xz.p), xz, hot,
+                      in_smem ? 1 : 0, status);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "trace pass launch");
   }
   bool used[sdim_ctx::kXzStreams] = {};
   for (size_t r = 0; r < runs.size(); ++r) {
@@ -835,6 +874,7 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsig
   const bool plain = flags & SDIM_FLAG_PLAIN;
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
   ctx->last_stream = s;
+  ctx->xz_pending = nullptr;
   std::vector<Job> jobs, tjobs, ujobs;
   for (const Job& j : all_jobs) (use_trace(j, flags) ? tjobs : use_trace_u8(j, flags) ? ujobs : jobs).push_back(j);
   int rc;
@@ -886,7 +926,20 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsig
   CK(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * V_COUNT, s));
   if (flags & SDIM_FLAG_TIME) CK(cudaEventRecord(ctx->ev0, s));
   int* status = static_cast<int*>(ctx->status.p);
+  // with trace programs in the batch the shot-group engines run on a stream
+  // of their own, beside the trace engines (the uneven batch: their 23 ms
+  // overlap the x / z passes); they are launched after them, so the x / z
+  // CTAs are dispatched first
+  bool side = false;
+  for (const Group& g : groups) side |= !plain && g.items > 0 && (!tjobs.empty() || !ujobs.empty());
+  cudaStream_t gs = s;
+  if (side) {
+    CK(cudaEventRecord(ctx->ev_gf, s));
+    CK(cudaStreamWaitEvent(ctx->grp, ctx->ev_gf, 0));
+    gs = ctx->grp;
+  }
   if ((rc = launch_trace_jobs(ctx, tjobs, ujobs, s, flags, status)) != SDIM_OK) return rc;
+  if (side && (flags & SDIM_FLAG_TIME)) CK(cudaEventRecord(ctx->ev_g0, gs));
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const Group& g = groups[gi];
     if (g.items == 0) continue;
@@ -903,12 +956,20 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsig
       if (!p.in_smem && (rc = ensure(ctx, ctx->gslots, p.big * p.slots_per_block * (size_t)p.blocks)) != SDIM_OK)
         return rc;
       unsigned long long* counter = static_cast<unsigned long long*>(ctx->counters.p) + g.variant;
-      ops.persistent(dim3(p.blocks), dim3(p.team_threads * p.slots_per_block), p.smem_per_block, s,
+      ops.persistent(dim3(p.blocks), dim3(p.team_threads * p.slots_per_block), p.smem_per_block, gs,
                      ddesc + g.begin, g.end - g.begin, g.items, counter, static_cast<uint8_t*>(ctx->gslots.p),
                      p.big, p.hot, p.in_smem ? 1 : 0, status);
     }
     cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch");
+  }
+  if (side) {
+    if (flags & SDIM_FLAG_TIME) {
+      CK(cudaEventRecord(ctx->ev_g1, gs));
+      ctx->group_recorded = true;
+    }
+    CK(cudaEventRecord(ctx->ev_gj, gs));
+    CK(cudaStreamWaitEvent(s, ctx->ev_gj, 0));
   }
   return SDIM_OK;
 }
@@ -1276,7 +1337,11 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
       cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->ev_xzf, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&ctx->ev_xzf, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->grp, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_gf, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_gj, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev_g0) != cudaSuccess || cudaEventCreate(&ctx->ev_g1) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return SDIM_ECUDA;
@@ -1305,10 +1370,11 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   cudaStreamSynchronize(ctx->aux);
+  cudaStreamSynchronize(ctx->grp);
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) cudaStreamSynchronize(ctx->xzs[i]);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
                     &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8,
-                    &ctx->xz_queue};
+                    &ctx->xz_queue, &ctx->gslots_xz};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);
@@ -1322,6 +1388,11 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaEventDestroy(ctx->ev_fork);
   cudaEventDestroy(ctx->ev_join);
   cudaEventDestroy(ctx->ev_xzf);
+  cudaEventDestroy(ctx->ev_gf);
+  cudaEventDestroy(ctx->ev_gj);
+  cudaEventDestroy(ctx->ev_g0);
+  cudaEventDestroy(ctx->ev_g1);
+  cudaStreamDestroy(ctx->grp);
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) {
     cudaEventDestroy(ctx->ev_xzj[i]);
     cudaStreamDestroy(ctx->xzs[i]);
@@ -1350,8 +1421,12 @@ int sdim_memory_info(sdim_ctx* ctx, int64_t info[3]) {
   CK(cudaMemGetInfo(&free_b, &total_b));
   info[0] = (int64_t)free_b;
   info[1] = (int64_t)total_b;
-  info[2] = (int64_t)(ctx->descs.cap + ctx->counters.cap + ctx->status.cap + ctx->gslots.cap + ctx->out.cap +
-                      ctx->snap.cap);
+  const DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap,
+                          &ctx->arena, &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8,
+                          &ctx->xz_u8, &ctx->xz_queue, &ctx->gslots_xz};
+  int64_t held = 0;
+  for (const DevBuf* b : bufs) held += (int64_t)b->cap;
+  info[2] = held;
   return SDIM_OK;
 }
 
@@ -1430,6 +1505,7 @@ int sdim_circuit_destroy(sdim_circuit* c) {
   cudaSetDevice(c->device);
   if (c->d_ops) cudaFree(c->d_ops);
   if (c->h_ops) cudaFreeHost(c->h_ops);
+  if (c->xz_trace.p) cudaFree(c->xz_trace.p);
   delete c;
   return SDIM_OK;
 }
@@ -1557,7 +1633,7 @@ int sdim_frame_run(sdim_ctx* ctx, const sdim_circuit* c, const sdim_circuit* ref
     const int trc = collect_times(ctx);
     if (trc != SDIM_OK) return trc;
   }
-  return read_status(ctx);
+  return settle_xz(ctx, read_status(ctx));
 }
 
 int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, const uint64_t* seeds,

@@ -171,7 +171,7 @@ class Program:
     # ------------------------------------------------------------------
     def sample(self, shots: int, seed: Optional[int] = None, shot0: int = 0, noise: bool = True,
                plain: bool = False, out: Optional[np.ndarray] = None, per_shot: bool = False,
-               engine: Optional[str] = None) -> np.ndarray:
+               engine: Optional[str] = None, keep_xz: bool = False) -> np.ndarray:
         """Records of shots [shot0, shot0 + shots) as a (shots, records) uint8
         array, value | deterministic << 7 -- the fast path without Python objects.
 
@@ -179,12 +179,19 @@ class Program:
         "trace" (d = 2: one x / z pass, one lane per shot), "group" (32-shot
         groups), "per_shot" (one warp per shot; same as ``per_shot=True``),
         "tuned" (the route the autotuner timed fastest for this program's
-        class of d, n and shots; the first call of a class times them)."""
+        class of d, n and shots; the first call of a class times them).
+
+        ``keep_xz`` (d = 2 trace engine): the first call keeps the program's
+        x / z trace on the device and later calls with ``keep_xz=True`` replay
+        it without the x / z pass; it depends on the program alone, so a
+        sampling loop over fresh seeds or shot ranges gets the same records
+        as without it."""
         dp = self.compile(noise)
         s = self._seed(seed)
         if out is None:
             out = np.empty((int(shots), dp.num_records), dtype=np.uint8)
         flags = (_lib.FLAG_PLAIN if plain else 0) | (_lib.FLAG_PER_SHOT if per_shot else 0)
+        flags |= _lib.FLAG_REUSE_XZ if keep_xz else 0
         if engine == "tuned":
             from .autotune import default_tuner
             if shots > 0:

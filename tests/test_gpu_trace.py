@@ -228,3 +228,39 @@ def test_wide_rows_past_512_qudits(n):
     assert np.array_equal(rec, prog.sample(70, seed=n, engine="group")), n
     if n <= 1025:
         assert np.array_equal(rec[:2], oracle_run([spec], n, 0, 2)["records"]), n
+
+
+def test_kept_xz_trace_replays_for_fresh_seeds_and_shot_ranges():
+    """keep_xz: the first call writes the program's x / z trace, later calls
+    replay it without the x / z pass; every call matches a cold run, and a
+    second program (and an edited one) keeps a trace of its own."""
+    spec = workloads.surface_memory(5, 3, prob=0.02)
+    prog = Program(spec.build())
+    other = Program(workloads.surface_memory(3, 4, prob=0.05).build())
+    for seed, shot0, shots in [(1, 0, 300), (2, 300, 129), (3, 7, 1000), (1, 0, 300)]:
+        warm = prog.sample(shots, seed=seed, shot0=shot0, engine="trace", keep_xz=True)
+        assert np.array_equal(warm, prog.sample(shots, seed=seed, shot0=shot0, engine="trace")), (seed, shot0)
+        w2 = other.sample(shots, seed=seed, shot0=shot0, engine="trace", keep_xz=True)
+        assert np.array_equal(w2, other.sample(shots, seed=seed, shot0=shot0, engine="trace")), (seed, shot0)
+    assert np.array_equal(prog.sample(200, seed=9, shot0=3, engine="trace", keep_xz=True),
+                          oracle_run([spec], 9, 3, 200)["records"])
+    # an edited program is a new encoded program: its trace is written afresh
+    prog.circuits[-1].add_gate("H", 0)
+    prog.circuits[-1].add_gate("MEASURE", 0)
+    cold = prog.sample(200, seed=5, engine="trace")
+    assert np.array_equal(prog.sample(200, seed=5, engine="trace", keep_xz=True), cold)
+    assert np.array_equal(prog.sample(200, seed=5, engine="trace", keep_xz=True), cold)
+
+
+def test_kept_xz_trace_with_coins_in_the_phase_pass():
+    spec = workloads.surface_memory(5, 2, prob=0.03)
+    prog = Program(spec.build())
+    dp = prog.compile()
+    ctx = prog.context
+    cold = prog.sample(500, seed=4, engine="trace")
+    out = np.empty_like(cold)
+    for flags in (_lib.FLAG_TRACE | _lib.FLAG_REUSE_XZ,
+                  _lib.FLAG_TRACE | _lib.FLAG_REUSE_XZ | _lib.FLAG_NO_COIN_PASS):
+        out[:] = 0
+        _lib.check(ctx.lib.sdim_run(ctx.ptr, dp.ptr, 4, 0, 500, out.ctypes.data, flags), ctx.ptr, "run")
+        assert np.array_equal(out, cold)
