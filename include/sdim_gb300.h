@@ -73,6 +73,15 @@ extern "C" {
                                       the shots).  Calls that use the kept trace must be ordered on the
                                       device after the call that wrote it (one stream, or synchronous
                                       calls); asynchronous calls and graph capture never make it valid */
+#define SDIM_FLAG_COLUMNS 524288u /* d = 2 trace engine, one program: record columns whatever the shot
+                                     count -- the records as an affine map over GF(2) of each shot's
+                                     outcome draws and N1 fires, a column per input computed once from
+                                     the trace, then one lane per shot XORing its columns in.  By
+                                     default a single program takes them from max(columns, 19,456)
+                                     shots, with rows of up to 32 words (n <= 512) and up to 1,024
+                                     measurements */
+#define SDIM_FLAG_PHASE_REPLAY 1048576u /* d = 2 trace engine: never the record columns (every shot
+                                           replays its phase deltas) */
 #define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
                                        into the host buffer directly, with no device buffer and no copy
                                        (by default records go to device memory, then one copy down) */
@@ -120,6 +129,10 @@ int sdim_circuit_destroy(sdim_circuit* circ);
  * [4] device ops, [5] backend (0 residue bytes, 1 bit planes), [6] per-shot
  * tableau slot bytes, [7] shot-group slot bytes (0: no group engine for d). */
 int sdim_circuit_info(const sdim_circuit* circ, int64_t info[8]);
+/* What a d = 2 program keeps on the device for SDIM_FLAG_REUSE_XZ:
+ * out[0] 1 when its x / z trace is valid, out[1] 1 when its record columns
+ * are.  Host-only. */
+int sdim_circuit_kept(const sdim_circuit* circ, int32_t out[2]);
 
 /* Runs shots [shot0, shot0 + nshots) of one program; out holds
  * nshots x records bytes (host memory unless SDIM_FLAG_OUT_DEVICE).  The
@@ -254,6 +267,12 @@ int sdim_last_stage_ms(const sdim_ctx* ctx, double out[3]);
  * another stream), out[1] the d = 2 coin pass alone (0 when none ran).  No
  * counterpart in the reference. */
 int sdim_last_pass_ms(const sdim_ctx* ctx, double out[2]);
+/* The passes of that span timed by themselves, first n of: [0] from the
+ * start of the kernels to the end of the last x / z pass, [1] the d = 2 coin
+ * pass, [2] the d = 2 column pass, [3] the shot-group engines when they ran
+ * on their own stream beside the trace engines (0 for a pass that did not
+ * run).  No counterpart in the reference. */
+int sdim_last_passes_ms(const sdim_ctx* ctx, double* out, int n);
 
 /* Tableau export of one shot in the reference's int8 block order
  * x[n][n], z[n][n], phase[n], destab_x[n][n], destab_z[n][n], destab_phase[n]

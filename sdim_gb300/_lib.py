@@ -36,6 +36,8 @@ FLAG_U8_XZ = 16384
 FLAG_PACKED_XZ = 131072
 FLAG_LANE_SHOTS_1 = 65536
 FLAG_REUSE_XZ = 262144
+FLAG_COLUMNS = 524288
+FLAG_PHASE_REPLAY = 1048576
 
 
 def engine_flags(engine) -> int:
@@ -63,6 +65,7 @@ SIGNATURES = {
     "sdim_encode_circuit": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int, C.c_int, C.POINTER(_P)]),
     "sdim_circuit_destroy": (C.c_int, [_P]),
     "sdim_circuit_info": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sdim_circuit_kept": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "sdim_run": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, C.c_uint]),
     "sdim_run_device": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int64, _P, _P, C.c_uint]),
     "sdim_frame_run": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_int64, _P, C.c_uint]),
@@ -77,6 +80,7 @@ SIGNATURES = {
     "sdim_last_kernel_ms": (C.c_double, [_P]),
     "sdim_last_stage_ms": (C.c_int, [_P, _P]),
     "sdim_last_pass_ms": (C.c_int, [_P, _P]),
+    "sdim_last_passes_ms": (C.c_int, [_P, _P, C.c_int]),
     "sdim_snapshot": (C.c_int, [_P, _P, C.c_uint64, C.c_int64, C.c_int, _P, _P, C.c_uint]),
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_probe_l2_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
@@ -187,6 +191,13 @@ class Context:
         """(x / z passes alone, d = 2 coin pass alone) of the last timed call."""
         buf = (C.c_double * 2)()
         check(self.lib.sdim_last_pass_ms(self.ptr, buf), self.ptr, "sdim_last_pass_ms")
+        return tuple(float(v) for v in buf)
+
+    def last_passes_ms(self):
+        """(x / z passes alone, d = 2 coin pass, d = 2 column pass, shot-group
+        engines beside the trace engines) of the last timed call."""
+        buf = (C.c_double * 4)()
+        check(self.lib.sdim_last_passes_ms(self.ptr, buf, 4), self.ptr, "sdim_last_passes_ms")
         return tuple(float(v) for v in buf)
 
     def sync(self):

@@ -58,6 +58,7 @@ struct sdim_ctx {
   std::string err;
   DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace, masks, tdescs_u8, trace_u8, xz_u8;
   DevBuf gslots_xz;  // d = 2 x / z pass tableaux in global memory (gslots: the shot-group engines')
+  DevBuf cols;       // record columns of a d = 2 trace program (trace_cols.cuh)
   cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
   cudaStream_t grp = nullptr;                      // shot-group engines of a batch with trace programs
   cudaEvent_t ev_gf = nullptr, ev_gj = nullptr;    // fork to and join from grp
@@ -77,6 +78,7 @@ struct sdim_ctx {
   bool stages_recorded = false;  // ev_xz / ev_phase belong to the pending span
   bool coin_recorded = false;    // ev_c0 / ev_c1 belong to the pending span
   bool group_recorded = false;   // ev_g0 / ev_g1 belong to the pending span
+  double group_ms = 0.0;         // shot-group engines on their own stream
   double last_ms = 0.0;
   double stage_ms[3] = {0.0, 0.0, 0.0};  // x / z passes, phase passes, other engines
   double pass_ms[2] = {0.0, 0.0};        // x / z passes alone, coin pass alone
@@ -86,6 +88,10 @@ struct sdim_ctx {
   int trace_threads = kTracePassThreads;  // x / z pass CTA size (SDIM_TRACE_PASS_THREADS: 256 or 512)
   GraphCapture* capture = nullptr;  // set while sdim_graph_create runs on its private context
   sdim_circuit* xz_pending = nullptr;  // circuit whose kept trace the current call writes (SDIM_FLAG_REUSE_XZ)
+  bool pend_trace = false, pend_cols = false;  // what of it the call writes: the trace, the columns
+  cudaEvent_t ev_cols = nullptr;               // end of the column pass (SDIM_FLAG_TIME)
+  bool cols_recorded = false;
+  double col_ms = 0.0;                         // column pass alone
   unsigned long long reallocs = 0;  // device buffers moved by ensure()
 };
 
@@ -134,6 +140,8 @@ struct sdim_circuit {
   // running the x / z pass again (it depends only on the program)
   DevBuf xz_trace;
   bool xz_trace_valid = false;
+  DevBuf xz_cols;  // its record columns (trace_cols.cuh), kept the same way
+  bool xz_cols_valid = false;
 };
 
 namespace {
@@ -292,6 +300,11 @@ int collect_times(sdim_ctx* ctx) {
   }
   if (ctx->coin_recorded) CK(cudaEventElapsedTime(&co, ctx->ev_c0, ctx->ev_c1));
   if (ctx->group_recorded) CK(cudaEventElapsedTime(&c, ctx->ev_g0, ctx->ev_g1));  // on their own stream
+  float cm = 0.f;
+  if (ctx->cols_recorded) CK(cudaEventElapsedTime(&cm, ctx->ev_xzo, ctx->ev_cols));
+  ctx->col_ms = cm;
+  ctx->group_ms = ctx->group_recorded ? c : 0.0;
+  ctx->cols_recorded = false;
   ctx->pass_ms[0] = xo;
   ctx->pass_ms[1] = co;
   ctx->stages_recorded = false;
@@ -308,8 +321,12 @@ int collect_times(sdim_ctx* ctx) {
 // The end of a synchronous call: a kept x / z trace that it wrote
 // (SDIM_FLAG_REUSE_XZ) becomes valid when the call ended without an error.
 int settle_xz(sdim_ctx* ctx, int rc) {
-  if (ctx->xz_pending && rc == SDIM_OK) ctx->xz_pending->xz_trace_valid = true;
+  if (ctx->xz_pending && rc == SDIM_OK) {
+    if (ctx->pend_trace) ctx->xz_pending->xz_trace_valid = true;
+    if (ctx->pend_cols) ctx->xz_pending->xz_cols_valid = true;
+  }
   ctx->xz_pending = nullptr;
+  ctx->pend_trace = ctx->pend_cols = false;
   return rc;
 }
 
@@ -322,6 +339,7 @@ int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
   if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch");
   if (flags & SDIM_FLAG_ASYNC) {
     ctx->xz_pending = nullptr;  // not checked, so a trace written now is not kept valid
+    ctx->pend_trace = ctx->pend_cols = false;
     return SDIM_OK;
   }
   CK(cudaStreamSynchronize(s));
@@ -524,7 +542,24 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   if (keep && !skip_xz) {
     rc = ensure(ctx, keep->xz_trace, trace_bytes(keep->nmeas, keep->nn1, trace_words(keep->n)));
     if (rc != SDIM_OK) return rc;
+    keep->xz_cols_valid = false;  // columns of the trace about to be rewritten
     ctx->xz_pending = keep;
+    ctx->pend_trace = true;
+  }
+  // record columns instead of the phase replay (trace_cols.cuh): one program,
+  // fires known from the coin pass, enough shots to pay for the column pass
+  // (or SDIM_FLAG_COLUMNS); SDIM_FLAG_PHASE_REPLAY keeps the replay
+  bool colform = false, skip_cols = false;
+  int cnw = 0;
+  long long ncols = 0;
+  if (k == 1 && !(flags & SDIM_FLAG_PHASE_REPLAY)) {
+    const sdim_circuit* c0 = jobs[0].c;
+    ncols = column_count(c0->nmeas, c0->nn1_used);
+    cnw = column_words(c0->nmeas);
+    const bool masked = c0->nn1_used == 0 || !(flags & SDIM_FLAG_NO_COIN_PASS);
+    const bool fits = trace_words(c0->n) <= kColumnMaxWords && c0->nmeas >= 1 && cnw <= kColumnMaxRecordWords;
+    const bool pays = (flags & SDIM_FLAG_COLUMNS) || jobs[0].nshots >= std::max<long long>(ncols, kColumnMinShots);
+    colform = fits && masked && pays;
   }
   if (k) {
     std::vector<size_t> off(k);
@@ -564,6 +599,7 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       for (size_t i = b; i < e; ++i) spl[i] = sp;
       b = e;
     }
+    if (colform) spl[0] = 1;  // the record pass: one shot per lane
     long long groups = 0;
     for (size_t i = 0; i < k; ++i) {
       const Job& j = jobs[i];
@@ -608,6 +644,26 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.nn1 = j.c->nn1;
       td.tw = tw;
       td.wn = (j.c->n + 31) >> 5;
+      td.nused = j.c->nn1_used;
+    }
+    if (colform) {
+      // the fire masks must be there unless the program has no N1 before its
+      // last measurement (a mask budget overflow falls back to the replay)
+      if (hd[0].nused > 0 && !hd[0].masks) colform = false;
+    }
+    if (colform) {
+      const size_t cbytes = std::max<size_t>((size_t)ncols * (size_t)cnw * 4, 256);
+      DevBuf& cb = keep ? keep->xz_cols : ctx->cols;
+      skip_cols = keep && skip_xz && keep->xz_cols_valid;
+      if (!skip_cols) {
+        if ((rc = ensure(ctx, cb, cbytes)) != SDIM_OK) return rc;
+        if (keep) {
+          ctx->xz_pending = keep;
+          ctx->pend_cols = true;
+        }
+      }
+      hd[0].cols = static_cast<uint32_t*>(cb.p);
+      hd[0].nw = cnw;
     }
     dd = static_cast<TraceDesc*>(ctx->tdescs.p);
     if ((rc = upload_descs(ctx, dd, hd.data(), sizeof(TraceDesc), k, offsetof(TraceDesc, c),
@@ -804,6 +860,17 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       CK(cudaStreamWaitEvent(s, ctx->ev_xzj[i], 0));
     }
   if (timed) CK(cudaEventRecord(ctx->ev_xzo, s));
+  // ---- column pass: after the x / z pass, beside the rest of the coin pass
+  if (colform && !skip_cols) {
+    if (!launch_column_pass(hd[0].tw, (int)((ncols + 32 * kColumnWarps - 1) / (32 * kColumnWarps)), s, dd, status))
+      return fail(ctx, SDIM_EINVAL, "no column pass for trace rows of " + std::to_string(hd[0].tw) + " words");
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "column pass launch");
+    if (timed) {
+      CK(cudaEventRecord(ctx->ev_cols, s));
+      ctx->cols_recorded = true;
+    }
+  }
   // ---- coin pass on the second stream, alongside the x / z passes (independent work)
   if (coins) {
     CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
@@ -822,8 +889,16 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
     CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
   }
   if (timed) CK(cudaEventRecord(ctx->ev_xz, s));
-  // ---- phase passes
-  for (size_t b = 0; b < k;) {
+  // ---- phase passes (the record pass for record columns)
+  if (colform) {
+    const long long groups = (jobs[0].nshots + 31) / 32;
+    if (groups > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one record pass");
+    if (groups > 0 && !launch_record_pass(cnw, (int)groups, s, dd, groups, status))
+      return fail(ctx, SDIM_EINVAL, "no record pass for columns of " + std::to_string(cnw) + " words");
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "record pass launch");
+  }
+  for (size_t b = colform ? k : 0; b < k;) {
     const int tw = hd[b].tw, sp = hd[b].spl;
     size_t e = b;
     long long items = 0;
@@ -875,6 +950,7 @@ int launch_jobs(sdim_ctx* ctx, std::vector<Job>& all_jobs, cudaStream_t s, unsig
   const bool force_gmem = flags & SDIM_FLAG_FORCE_GMEM;
   ctx->last_stream = s;
   ctx->xz_pending = nullptr;
+  ctx->pend_trace = ctx->pend_cols = false;
   std::vector<Job> jobs, tjobs, ujobs;
   for (const Job& j : all_jobs) (use_trace(j, flags) ? tjobs : use_trace_u8(j, flags) ? ujobs : jobs).push_back(j);
   int rc;
@@ -1341,7 +1417,8 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
       cudaStreamCreateWithFlags(&ctx->grp, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_gf, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_gj, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreate(&ctx->ev_g0) != cudaSuccess || cudaEventCreate(&ctx->ev_g1) != cudaSuccess) {
+      cudaEventCreate(&ctx->ev_g0) != cudaSuccess || cudaEventCreate(&ctx->ev_g1) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev_cols) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return SDIM_ECUDA;
@@ -1374,7 +1451,7 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) cudaStreamSynchronize(ctx->xzs[i]);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
                     &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8,
-                    &ctx->xz_queue, &ctx->gslots_xz};
+                    &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);
@@ -1392,6 +1469,7 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaEventDestroy(ctx->ev_gj);
   cudaEventDestroy(ctx->ev_g0);
   cudaEventDestroy(ctx->ev_g1);
+  cudaEventDestroy(ctx->ev_cols);
   cudaStreamDestroy(ctx->grp);
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) {
     cudaEventDestroy(ctx->ev_xzj[i]);
@@ -1423,7 +1501,7 @@ int sdim_memory_info(sdim_ctx* ctx, int64_t info[3]) {
   info[1] = (int64_t)total_b;
   const DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap,
                           &ctx->arena, &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8,
-                          &ctx->xz_u8, &ctx->xz_queue, &ctx->gslots_xz};
+                          &ctx->xz_u8, &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols};
   int64_t held = 0;
   for (const DevBuf* b : bufs) held += (int64_t)b->cap;
   info[2] = held;
@@ -1506,6 +1584,7 @@ int sdim_circuit_destroy(sdim_circuit* c) {
   if (c->d_ops) cudaFree(c->d_ops);
   if (c->h_ops) cudaFreeHost(c->h_ops);
   if (c->xz_trace.p) cudaFree(c->xz_trace.p);
+  if (c->xz_cols.p) cudaFree(c->xz_cols.p);
   delete c;
   return SDIM_OK;
 }
@@ -1521,6 +1600,13 @@ int sdim_circuit_info(const sdim_circuit* c, int64_t info[8]) {
   info[5] = c->d == 2 ? 1 : 0;
   info[6] = (int64_t)variant_ops(c->variant).big_bytes(c->n);
   info[7] = (int64_t)(g.hot_bytes(c->n) + g.big_bytes(c->n));
+  return SDIM_OK;
+}
+
+int sdim_circuit_kept(const sdim_circuit* c, int32_t out[2]) {
+  if (!c || !out) return SDIM_EINVAL;
+  out[0] = c->xz_trace_valid ? 1 : 0;
+  out[1] = c->xz_cols_valid ? 1 : 0;
   return SDIM_OK;
 }
 
@@ -1565,7 +1651,7 @@ int sdim_run(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot0,
     const int trc = collect_times(ctx);
     if (trc != SDIM_OK) return trc;
   }
-  return read_status(ctx);
+  return settle_xz(ctx, read_status(ctx));
 }
 
 int sdim_frame_run(sdim_ctx* ctx, const sdim_circuit* c, const sdim_circuit* ref, uint64_t seed, int64_t nshots,
@@ -1692,7 +1778,7 @@ int sdim_run_batch(sdim_ctx* ctx, int ncirc, const sdim_circuit* const* circs, c
     const int trc = collect_times(ctx);
     if (trc != SDIM_OK) return trc;
   }
-  return read_status(ctx);
+  return settle_xz(ctx, read_status(ctx));
 }
 
 int sdim_graph_create(sdim_ctx* parent, int ncirc, const sdim_circuit* const* circs, const uint64_t* seeds,
@@ -1993,6 +2079,14 @@ int sdim_last_pass_ms(const sdim_ctx* ctx, double out[2]) {
   if (!ctx || !out) return SDIM_EINVAL;
   out[0] = ctx->pass_ms[0];
   out[1] = ctx->pass_ms[1];
+  return SDIM_OK;
+}
+
+int sdim_last_passes_ms(const sdim_ctx* ctx, double* out, int n) {
+  if (!ctx || (!out && n > 0) || n < 0) return SDIM_EINVAL;
+  const double v[4] = {ctx->pass_ms[0], ctx->pass_ms[1], ctx->col_ms, ctx->group_ms};
+  for (int i = 0; i < n && i < 4; ++i) out[i] = v[i];
+  for (int i = 4; i < n; ++i) out[i] = 0.0;
   return SDIM_OK;
 }
 

@@ -1,6 +1,8 @@
 // Trace engine kernels (d = 2): the x / z pass, one CTA per program over its
-// layered schedule, and the phase pass, one lane per shot.
+// layered schedule, the phase pass, one lane per shot, and the column and
+// record passes that replace the phase pass for a single program.
 #include "trace_bits.cuh"
+#include "trace_cols.cuh"
 #include "variants.cuh"
 
 namespace sdim {
@@ -54,6 +56,29 @@ __global__ void __launch_bounds__(32, TW >= 64 ? 8 : (TW >= 16 || SPL == 2) ? 16
     else
       phase_program<TW, false>(descs + i, lg, threadIdx.x, rec);
   }
+}
+
+// One block of kColumnWarps warps per 32 kColumnWarps record columns of
+// descs[0], the trace staged in shared memory a window at a time.
+template <int TW>
+__global__ void __launch_bounds__(32 * kColumnWarps) k_column_pass(const TraceDesc* __restrict__ descs,
+                                                                   const int* status) {
+  __shared__ uint4 shdr[column_window<TW>()];
+  __shared__ __align__(16) uint32_t srow[column_window<TW>() * 2 * TW];
+  __shared__ int smin;
+  if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete (uniform over the block)
+  column_block<TW, kColumnWarps>(descs, blockIdx.x, shdr, srow, &smin);
+}
+
+// One single-warp block per 32-shot group of descs[0], from its record
+// columns: up to 16 column words, 32 blocks per SM at 64 registers.
+template <int NW>
+__global__ void __launch_bounds__(32, NW >= 32 ? 16 : 32)
+    k_record_pass(const TraceDesc* __restrict__ descs, long long groups, const int* status) {
+  __shared__ __align__(16) uint8_t rec[32 * kRecStride];
+  if (*(volatile const int*)status != DEV_OK) return;
+  if ((long long)blockIdx.x >= groups) return;
+  record_group<NW>(descs, blockIdx.x, threadIdx.x, rec);
 }
 
 // One thread per (chunk group, shot) item of the coin pass; descs with
@@ -135,6 +160,29 @@ bool launch_phase_spl(int tw, int grid, int block, cudaStream_t s, const TraceDe
     }
   }
   return false;
+}
+
+bool launch_column_pass(int tw, int grid, cudaStream_t s, const TraceDesc* descs, const int* status) {
+  switch (tw) {
+    case 2: k_column_pass<2><<<grid, 32 * kColumnWarps, 0, s>>>(descs, status); return true;
+    case 4: k_column_pass<4><<<grid, 32 * kColumnWarps, 0, s>>>(descs, status); return true;
+    case 8: k_column_pass<8><<<grid, 32 * kColumnWarps, 0, s>>>(descs, status); return true;
+    case 16: k_column_pass<16><<<grid, 32 * kColumnWarps, 0, s>>>(descs, status); return true;
+    case 32: k_column_pass<32><<<grid, 32 * kColumnWarps, 0, s>>>(descs, status); return true;
+    default: return false;
+  }
+}
+
+bool launch_record_pass(int nw, int grid, cudaStream_t s, const TraceDesc* descs, long long groups,
+                        const int* status) {
+  switch (nw) {
+    case 2: k_record_pass<2><<<grid, 32, 0, s>>>(descs, groups, status); return true;
+    case 4: k_record_pass<4><<<grid, 32, 0, s>>>(descs, groups, status); return true;
+    case 8: k_record_pass<8><<<grid, 32, 0, s>>>(descs, groups, status); return true;
+    case 16: k_record_pass<16><<<grid, 32, 0, s>>>(descs, groups, status); return true;
+    case 32: k_record_pass<32><<<grid, 32, 0, s>>>(descs, groups, status); return true;
+    default: return false;
+  }
 }
 
 bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, const TraceDesc* descs, int ndesc,

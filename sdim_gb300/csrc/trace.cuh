@@ -43,6 +43,7 @@ struct TraceDesc {
   uint32_t* nrow;
   uint32_t* masks;
   uint32_t* cmap;
+  uint32_t* cols;        // record columns (trace_cols.cuh), null when the phase pass replays
   long long coin_begin;  // first coin-pass item of this program
   int nsteps;
   int nwins;
@@ -52,6 +53,8 @@ struct TraceDesc {
   int tw;      // words per trace row
   int wn;      // words per generator half
   int spl;     // shots per lane of the phase pass (item_begin counts groups of 32 spl)
+  int nw;      // words per record column (a power of two >= 2)
+  int nused;   // N1 ordinals before the last measurement
 };
 
 __host__ __device__ inline size_t round_up(size_t b, size_t a) { return (b + a - 1) / a * a; }
@@ -166,6 +169,30 @@ bool launch_phase_pass(int tw, int spl, int grid, int block, cudaStream_t s, con
 // From this many shots in one phase-pass launch, lanes carry two shots each:
 // with 152 SMs that still leaves 8 single-warp blocks per SM.
 constexpr long long kPhasePairMinShots = 152LL * 64 * 8;
+
+// Record columns (trace_cols.cuh): one program per run, trace rows of up to
+// kColumnMaxWords words (n <= 512) and up to 32 x kColumnMaxRecordWords
+// measurements; column_count(nm, nused) columns of nw words each.
+constexpr int kColumnMaxWords = 32;
+constexpr int kColumnMaxRecordWords = 32;
+__host__ __device__ inline long long column_count(int nm, int nused) { return 1LL + nm + 2LL * nused; }
+// Words per record column for nm measurements: a power of two >= 2.
+inline int column_words(int nm) {
+  int w = 2;
+  while (32 * w < nm) w <<= 1;
+  return w;
+}
+// Fewest shots for which a run takes the record columns by default (one
+// 32-shot group per SM and scheduler); SDIM_FLAG_COLUMNS takes them at any
+// shot count.
+constexpr long long kColumnMinShots = 152LL * 32 * 4;
+// Warps of a column-pass block (32 columns each).
+constexpr int kColumnWarps = 4;
+// Column pass: one block per 32 kColumnWarps columns of descs[0].
+bool launch_column_pass(int tw, int grid, cudaStream_t s, const TraceDesc* descs, const int* status);
+// Record pass: one single-warp block per 32-shot group of descs[0].
+bool launch_record_pass(int nw, int grid, cudaStream_t s, const TraceDesc* descs, long long groups,
+                        const int* status);
 
 
 // Odd-d trace engine (k_trace_u8.cu).  variant: 0, 1, 2 for d = 3, 5, 7, 3

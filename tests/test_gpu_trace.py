@@ -3,6 +3,8 @@ replaying its phase deltas) against the oracle and the other engines, for
 every trace-row width, both x / z pass teams, partial shot groups, every
 noise channel (including p = 0 and p = 1), mixed batches and global-memory
 x / z slots."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -264,3 +266,6 @@ def test_kept_xz_trace_with_coins_in_the_phase_pass():
         out[:] = 0
         _lib.check(ctx.lib.sdim_run(ctx.ptr, dp.ptr, 4, 0, 500, out.ctypes.data, flags), ctx.ptr, "run")
         assert np.array_equal(out, cold)
+        state = (ctypes.c_int32 * 2)()
+        _lib.check(ctx.lib.sdim_circuit_kept(dp.ptr, state), ctx.ptr, "kept")
+        assert state[0] == 1, "the x / z trace was not kept"
