@@ -555,7 +555,7 @@ class Timer:
             step_ms.append(e0.elapsed_time(e1))
             kern_ms.append(self.ctx.last_kernel_ms())
             self.stage_ms.append(self.ctx.last_stage_ms())
-            self.pass_ms.append(self.ctx.last_pass_ms())
+            self.pass_ms.append(self.ctx.last_passes_ms())
         torch.cuda.synchronize()
         return step_ms, kern_ms, (clocks.stop() if clocks else None)
 
@@ -735,6 +735,7 @@ def run_single(args, torch, dist, ws, rank, local):
             "config": {"workload": desc, "shots_per_gpu": shots, "mode": "quick: timed engine only"},
             "engine": args.engine, "kernel_ms": statistics.mean(kern_ms),
             "stages_ms": {"xz_pass": stages[0], "phase_pass": stages[1], "other_engines": stages[2]},
+            "passes_ms": {"xz_pass": passes[0], "coin_pass": passes[1], "column_pass": passes[2]},
             "gpu_launches": args.steps, "clocks": clk}
 
     # per-shot engine (one warp, one full tableau per shot) on the same inputs
@@ -752,7 +753,9 @@ def run_single(args, torch, dist, ws, rank, local):
     if d == 2:
         # the shot-group engine on the same inputs, for comparison
         for name, fl in (("group", _lib.FLAG_NO_TRACE), ("trace", _lib.FLAG_TRACE),
-                         ("trace, one shot per phase-pass lane", _lib.FLAG_TRACE | _lib.FLAG_LANE_SHOTS_1)):
+                         ("trace, phase replay instead of record columns", _lib.FLAG_TRACE | _lib.FLAG_PHASE_REPLAY),
+                         ("trace, phase replay, one shot per lane",
+                          _lib.FLAG_TRACE | _lib.FLAG_PHASE_REPLAY | _lib.FLAG_LANE_SHOTS_1)):
             step(fl)
             ctx.sync()
             g_ms, g_kern, _ = timer.run(2, lambda: step(fl))
@@ -877,20 +880,28 @@ def run_single(args, torch, dist, ws, rank, local):
         sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
         model = philox_model_peak(ctx.num_sms, sm_mhz)
         issue_rate = ctx.num_sms * 4 * sm_mhz * 1e6  # warp instructions per second (4 schedulers per SM)
-        phase_instr = read_profile_value("trace_engine_surface_L7.md", "phase_pass_warp_instructions") \
+        columns = len(passes) > 2 and passes[2] > 0.0  # record columns ran instead of the phase replay
+        last_name = "record_pass" if columns else "phase_pass"
+        phase_instr = read_profile_value("trace_engine_surface_L7.md", f"{last_name}_warp_instructions") \
             if args.workload == "surface" else None
         n_meas = int(np.isin(gids, (14, 15, 16)).sum())
+        ncols = 1 + n_meas + 2 * nn1_used
+        nw = 2
+        while 32 * nw < n_meas:
+            nw *= 2
         roofline = {"bound": "int-multiply (Philox4x32-10 blocks)", "achieved": ach / 1e9, "peak": prate / 1e9,
                     "unit": "Gblock/s", "frac": ach / prate,
                     "traffic": read_traffic("trace_engine_surface_L7.md") if args.workload == "surface" else None,
-                    "kernel": "trace engine step: k_trace_pass (x/z, 1 CTA) alongside k_coin_pass, then "
-                              f"k_phase_pass<{trace_words(n)}>",
+                    "kernel": "trace engine step: k_trace_pass (x/z, 1 CTA) alongside k_coin_pass, then " +
+                              (f"k_column_pass<{trace_words(n)}> and k_record_pass<{nw}>" if columns else
+                               f"k_phase_pass<{trace_words(n)}>"),
                     "peak_source": "Philox throughput measured live by sdim_probe_philox_rate",
                     "algorithmic_blocks_per_launch": blocks,
                     "blocks_model": f"per shot ceil({nn1_used} N1 ordinals / 4) coin blocks + {n_random} "
                                     "random-outcome blocks",
                     "kernel_ms": mean_kern,
-                    "stages_ms": {"xz_pass_and_coin_pass": stages[0], "phase_pass": stages[1]},
+                    "stages_ms": {"xz_and_column_passes_beside_coin_pass" if columns else "xz_pass_and_coin_pass":
+                                  stages[0], last_name: stages[1]},
                     "peak_cross_check": {
                         "value": model / 1e9, "unit": "Gblock/s", "probe_over_model": prate / model,
                         "model": f"{ctx.num_sms} SMs x 64 32-bit multiplies per clock / (2 per wide multiply x "
@@ -910,7 +921,13 @@ def run_single(args, torch, dist, ws, rank, local):
                             "bound": "latency: one CTA walks the layered schedule; barriers and dependent "
                                      "shared-memory chains per measurement block",
                             "timed": "CUDA events from the step's first kernel to the end of k_trace_pass"},
-                        "phase_pass": {
+                        "column_pass": {
+                            "ms": passes[2] if columns else None, "columns": ncols, "column_words": nw,
+                            "us_per_measurement": 1e3 * passes[2] / max(n_meas, 1) if columns else None,
+                            "bound": "latency: each warp walks the measurements from its columns' inputs on, the "
+                                     "trace staged in shared memory",
+                            "timed": "CUDA events around k_column_pass on the launching stream"} if columns else None,
+                        last_name: {
                             "ms": stages[1], "warp_instructions": phase_instr,
                             "issue_bound_ms": (1e3 * phase_instr / issue_rate) if phase_instr else None,
                             "frac": (1e3 * phase_instr / issue_rate / stages[1]) if phase_instr else None,
@@ -1122,7 +1139,7 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
     # figure the survey's model charges; its d = 3 figure is already two bit
     # planes)
     packed_run = 2 * odd_trace >= ctx.num_sms
-    gb, t_min, t_packed, streamed, in_l2 = 0.0, 0.0, 0.0, 0.0, 0.0
+    gb, gb_packed, t_min, t_packed, streamed, in_l2 = 0.0, 0.0, 0.0, 0.0, 0.0, 0.0
     for e, o in zip(entries, offs[:-1]):
         enc = e.program.enc
         nr = e.program.num_records
@@ -1136,6 +1153,7 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
         t_min += (xz / bw + delta / peak) / 1e9
         xz_p = xz / 2 if (on_trace and packed_run and enc.d in (5, 7)) else xz
         t_packed += (xz_p / bw + delta / peak) / 1e9
+        gb_packed += xz_p + delta
         streamed += xz if place == "hbm" else 0.0
         in_l2 += xz if place == "l2" else 0.0
     mean_kern = statistics.mean(kern_ms)
@@ -1190,21 +1208,24 @@ def uneven_measure(args, torch, dist, ws, rank, local, sub=False):
         "per_shot_engine": ps,
         "roofline": {"bound": "smem for resident tableaux, L2 for columns streamed by CTA clusters, HBM for "
                               "other streamed tableaux",
-                     "achieved": gb / (mean_kern / 1e3) / 1e9, "peak": gb / t_min / 1e9, "unit": "GB/s",
-                     "frac": t_min * 1e3 / mean_kern, "traffic": None,
+                     "achieved": gb_packed / (mean_kern / 1e3) / 1e9, "peak": gb_packed / t_packed / 1e9,
+                     "unit": "GB/s", "frac": t_packed * 1e3 / mean_kern, "traffic": None,
                      "kernel": "trace engines (k_trace_pass*, k_phase_pass*) for n >= 160 or 128+ shots, "
                                "k_group_warp / k_group_cta for the rest",
-                     "algorithmic_bytes_per_launch": gb, "streamed_bytes": streamed, "l2_bytes": in_l2,
-                     "kernel_ms": mean_kern, "bound_ms": t_min * 1e3, "smem_peak_gbs": peak, "l2_peak_gbs": l2,
+                     "algorithmic_bytes_per_launch": gb_packed, "streamed_bytes": streamed, "l2_bytes": in_l2,
+                     "kernel_ms": mean_kern, "bound_ms": t_packed * 1e3, "smem_peak_gbs": peak, "l2_peak_gbs": l2,
                      "hbm_peak_gbs": hbm,
                      "peak_source": "shared-memory read and L2 read+write bandwidth measured live by "
                                     "sdim_probe_smem_bandwidth / sdim_probe_l2_bandwidth; HBM from "
                                     "MEASURED_PEAKS.json",
                      "bytes_model": "x/z tableau updates once per program (trace engines) or per 32-shot group, "
-                                    "plus per-shot phase-delta bytes; frac = bound_ms / kernel_ms",
-                     "packed": {"bound_ms": t_packed * 1e3, "frac": t_packed * 1e3 / mean_kern,
-                                "model": "the same bound with d = 5, 7 trace x/z bytes at 4-bit lanes (half), as "
-                                         "the batched packed x/z pass stores them"}},
+                                    "at the residue width the library stores (bit planes for d = 2, 3; 4-bit lanes "
+                                    "for d = 5, 7 in the batched packed x/z pass; bytes otherwise), plus per-shot "
+                                    "phase-delta bytes; frac = bound_ms / kernel_ms",
+                     "byte_residues": {"bound_ms": t_min * 1e3, "frac": t_min * 1e3 / mean_kern,
+                                       "algorithmic_bytes": gb,
+                                       "model": "the same bound with d = 5, 7 x/z rows at one byte per residue "
+                                                "(the per-gate byte table's figure for d >= 5)"}},
         "cpu_baseline": cpu,
         # one persistent launch per (dimension, team kind) present in the batch
         "gpu_launches": steps * len({(e.program.enc.d, e.program.enc.n >= 160) for e in entries}),

@@ -109,9 +109,18 @@ __device__ __forceinline__ void column_block(const TraceDesc* __restrict__ tdp, 
       for (int t = threadIdx.x; t < n4; t += 32 * WARPS) dst[t] = __ldg(src + t);
     }
     __syncthreads();
-    for (int k = max(wb, k0); k < we; ++k) {
-      const uint4 h = shdr[k - wb];
+    // the header one measurement ahead and the factor row at the top of
+    // each step (neither depends on the delta), so the shared-memory loads
+    // overlap the dependent bit arithmetic
+    int k = max(wb, k0);
+    uint4 hn = k < we ? shdr[k - wb] : make_uint4(0u, 0u, 0u, 0u);
+    for (; k < we; ++k) {
+      const uint4 h = hn;
+      if (k + 1 < we) hn = shdr[k + 1 - wb];
       const uint32_t* row = srow + (size_t)(k - wb) * 2 * TW;
+      uint32_t r[TW];
+#pragma unroll
+      for (int w = 0; w < TW; ++w) r[w] = row[w];
       if (kind == 3 && start == k) {
 #pragma unroll
         for (int w = 0; w < TW; ++w) d1[w] ^= __ldg(inj + w);
@@ -122,14 +131,14 @@ __device__ __forceinline__ void column_block(const TraceDesc* __restrict__ tdp, 
         const uint32_t dp = (word_at<0, TW>(d1, wp) >> bp) & 1u;
         const uint32_t mk = 0u - dp;
 #pragma unroll
-        for (int w = 0; w < TW; ++w) d1[w] ^= row[w] & mk;
+        for (int w = 0; w < TW; ++w) d1[w] ^= r[w] & mk;
         bit = (kind == 2 && start == k) ? 1u : 0u;  // the outcome itself
         put_bit<0, TW>(d1, wn + wp, bp, dp);
         put_bit<0, TW>(d1, wp, bp, bit);
       } else {
         int s = 0;
 #pragma unroll
-        for (int w = 0; w < FH; ++w) s += __popc(row[w] & d1[w]);
+        for (int w = 0; w < FH; ++w) s += __popc(r[w] & d1[w]);
         bit = ((uint32_t)s & 1u) ^ (kind == 1 ? det_constant(h.w) : 0u);
       }
       if (h.x & 2u) {
