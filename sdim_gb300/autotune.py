@@ -52,9 +52,11 @@ import numpy as np
 from . import _lib
 
 # limits of the library's routes (abi.cu: trace_words, kTraceU8MaxQudits,
-# kCtaTeamQudits); candidates outside them would fall back to another route
+# kCtaTeamQudits, kColumnMaxWords); candidates outside them would fall back to
+# another route
 TRACE_BITS_MAX_QUDITS = 2048
 TRACE_U8_MAX_QUDITS = 2048
+COLUMN_MAX_QUDITS = 512
 CTA_TEAM_QUDITS = 160
 # the per-shot engine is a candidate for runs of fewer shots than this: a
 # partial 32-shot group leaves lanes of the shot-group engine idle
@@ -104,8 +106,12 @@ def program_candidates(d: int, n: int, shots: int, smem_optin: int, num_sms: int
     if trace_ok:
         out.append(Candidate("trace", _lib.FLAG_TRACE))
         if d == 2:
+            if n <= COLUMN_MAX_QUDITS:
+                out.append(Candidate("trace, record columns", _lib.FLAG_TRACE | _lib.FLAG_COLUMNS))
+            replay = _lib.FLAG_TRACE | _lib.FLAG_PHASE_REPLAY
+            out.append(Candidate("trace, phase replay", replay))
             out.append(Candidate("trace, coins in the phase pass", _lib.FLAG_TRACE | _lib.FLAG_NO_COIN_PASS))
-            out.append(Candidate("trace, one shot per phase-pass lane", _lib.FLAG_TRACE | _lib.FLAG_LANE_SHOTS_1))
+            out.append(Candidate("trace, phase replay, one shot per lane", replay | _lib.FLAG_LANE_SHOTS_1))
             out.append(Candidate("trace, global memory", _lib.FLAG_TRACE | _lib.FLAG_FORCE_GMEM))
         else:
             seen = {_xz_mode(n, d, 1, 0, smem_optin, num_sms)}

@@ -18,9 +18,19 @@ def test_candidates_d2_within_the_trace_limit():
     assert flags["default"] == 0
     assert flags["trace"] == _lib.FLAG_TRACE
     assert flags["trace, coins in the phase pass"] == _lib.FLAG_TRACE | _lib.FLAG_NO_COIN_PASS
+    assert flags["trace, record columns"] == _lib.FLAG_TRACE | _lib.FLAG_COLUMNS
+    assert flags["trace, phase replay"] == _lib.FLAG_TRACE | _lib.FLAG_PHASE_REPLAY
+    assert flags["trace, phase replay, one shot per lane"] == (_lib.FLAG_TRACE | _lib.FLAG_PHASE_REPLAY
+                                                                | _lib.FLAG_LANE_SHOTS_1)
     assert flags["shot groups, one per CTA"] == _lib.FLAG_TEAM_CTA
     assert "one warp per shot" not in flags
     assert len(set(flags.values())) == len(flags)
+
+
+def test_record_columns_only_within_their_row_limit():
+    assert "trace, record columns" in _names(autotune.program_candidates(2, 512, 4096, OPTIN, SMS))
+    c = _names(autotune.program_candidates(2, 513, 4096, OPTIN, SMS))
+    assert "trace, record columns" not in c and "trace, phase replay" in c
 
 
 def test_candidates_past_the_d2_trace_limit_and_large_n_teams():
