@@ -1184,6 +1184,12 @@ void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int 
   std::vector<uint4> steps, lops, wins;
   std::vector<std::vector<uint4>> layers;
   std::vector<int> last(n, -1), gen(n, -1);
+  // where the last op on each qudit sits when it is a gate (layer, position,
+  // slot 2 or 3 of its entry: z for the first qudit, w for a CNOT target), or
+  // layer -1: an N1 that follows reads the gate's columns, so it rides on the
+  // gate's tasks (the slot holds its ordinal + 1) instead of taking a layer
+  struct GateSlot { int layer, pos, slot; };
+  std::vector<GateSlot> lgate(n, GateSlot{-1, 0, 0});
   int window = 0, last_p = -1;
   bool in_block = false;
   uint32_t mord = 0, nord = 0;
@@ -1223,18 +1229,29 @@ void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int 
       continue;
     }
     in_block = false;
+    if (noise && gen[q] == window && lgate[q].layer >= 0) {
+      uint4& g = layers[lgate[q].layer][lgate[q].pos];
+      uint32_t& slot = lgate[q].slot == 2 ? g.z : g.w;
+      if (slot == 0u) {
+        slot = nord++ + 1u;
+        continue;
+      }
+    }
     const bool two = op == OP_CNOT || op == OP_CNOT_INV;
     const bool is_p = op == OP_P || op == OP_P_INV;
     int lv = level(q) + 1;
     if (two) lv = std::max(lv, level((int)w.y) + 1);
     if (is_p) lv = std::max(lv, last_p + 1);
     if (lv == (int)layers.size()) layers.emplace_back();
+    const int pos = (int)layers[lv].size();
     layers[lv].push_back(make_uint4(w.x, w.y, noise ? nord++ : 0u, 0u));
     last[q] = lv;
     gen[q] = window;
+    lgate[q] = noise ? GateSlot{-1, 0, 0} : GateSlot{lv, pos, 2};
     if (two) {
       last[w.y] = lv;
       gen[w.y] = window;
+      lgate[w.y] = GateSlot{lv, pos, 3};
     }
     if (is_p) last_p = lv;
   }

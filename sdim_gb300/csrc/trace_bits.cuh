@@ -45,12 +45,26 @@ using TraceTab = TGroupBits<CtaTeam>;
 
 // ---------------------------------------------------------------- x / z pass
 
+// Word w of N1 ordinal j's rows (x_q, z_q).
+__device__ __forceinline__ void n1_rows(const TraceDesc& td, uint32_t j, int w, uint32_t x, uint32_t z, int* status) {
+  if ((int)j >= td.nn1) {
+    atomicCAS(status, DEV_OK, DEV_SLOT_TOO_SMALL);
+    return;
+  }
+  uint32_t* dst = td.nrow + (size_t)j * 2 * td.tw;
+  dst[w] = x;
+  dst[td.tw + w] = z;
+}
+
 // Word w of one op of a gate layer (w in [0, tw); words past 2 Wn only pad
-// the N1 rows with zeros).
+// the N1 rows with zeros).  A gate entry's z (w) holds 1 + the ordinal of an
+// N1 on its qudit (target) that follows it with no op on that qudit between
+// (the host scheduler folds it in): the same thread writes that N1's rows
+// from the words it just produced.
 __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, const uint4 lo, int w, int* status) {
   const uint32_t op = lo.x & kOpMask;
   const int q = (int)(lo.x >> 8);
-  const int n = e.n, W2 = e.W2, RS = e.RS, tw = td.tw;
+  const int n = e.n, W2 = e.W2, RS = e.RS;
   if (q >= n) {
     atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
     return;
@@ -58,6 +72,7 @@ __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, con
   const bool in = w < W2;
   uint32_t* xr = e.X + (size_t)q * RS;
   uint32_t* zr = e.Z + (size_t)q * RS;
+  uint32_t xa = 0u, za = 0u;  // word w of x_q, z_q after the op (0 past 2 Wn)
   switch (op) {
     case OP_H:
     case OP_H_INV:
@@ -66,6 +81,8 @@ __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, con
         if (x & z) atomicXor(&e.C1[w], x & z);
         xr[w] = z;
         zr[w] = x;
+        xa = z;
+        za = x;
       }
       break;
     case OP_P:
@@ -75,7 +92,9 @@ __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, con
         const uint32_t c = (op == OP_P_INV) ? (~lo0 & x) : (lo0 & x);
         e.C0[w] = lo0 ^ x;  // the layer's only P
         if (c) atomicXor(&e.C1[w], c);
-        zr[w] ^= x;
+        za = zr[w] ^ x;
+        zr[w] = za;
+        xa = x;
       }
       break;
     case OP_CNOT:
@@ -85,47 +104,49 @@ __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, con
         atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
         return;
       }
+      uint32_t xb = 0u, zb = 0u;
       if (in) {
-        e.X[(size_t)tq * RS + w] ^= xr[w];
-        zr[w] ^= e.Z[(size_t)tq * RS + w];
+        uint32_t* xt = e.X + (size_t)tq * RS + w;
+        const uint32_t zt = e.Z[(size_t)tq * RS + w];
+        xa = xr[w];
+        xb = *xt ^ xa;
+        *xt = xb;
+        za = zr[w] ^ zt;
+        zr[w] = za;
+        zb = zt;
       }
+      if (lo.w) n1_rows(td, lo.w - 1u, w, xb, zb, status);
       break;
     }
     case OP_X:
     case OP_X_INV:  // d = 2: phase += 2 z_q
       if (in) {
-        const uint32_t v = zr[w];
-        if (v) atomicXor(&e.C1[w], v);
+        xa = xr[w];
+        za = zr[w];
+        if (za) atomicXor(&e.C1[w], za);
       }
       break;
     case OP_Z:
     case OP_Z_INV:  // d = 2: phase += 2 x_q
       if (in) {
-        const uint32_t v = xr[w];
-        if (v) atomicXor(&e.C1[w], v);
+        xa = xr[w];
+        za = zr[w];
+        if (xa) atomicXor(&e.C1[w], xa);
       }
       break;
     case OP_N1D:
     case OP_N1F:
     case OP_N1P:
-    case OP_N1OFF: {
-      const uint32_t j = lo.z;
-      if ((int)j >= td.nn1) {
-        atomicCAS(status, DEV_OK, DEV_SLOT_TOO_SMALL);
-        return;
-      }
-      if (op != OP_N1OFF) {
-        uint32_t* dst = td.nrow + (size_t)j * 2 * tw;
-        dst[w] = in ? xr[w] : 0u;
-        dst[tw + w] = in ? zr[w] : 0u;
-      }
-      break;
-    }
+    case OP_N1OFF:  // an N1 of its own: its ordinal in z
+      n1_rows(td, lo.z, w, in ? xr[w] : 0u, in ? zr[w] : 0u, status);
+      return;
     case OP_NOP:
-      break;
+      return;
     default:
       atomicCAS(status, DEV_OK, DEV_BAD_OPCODE);
+      return;
   }
+  if (lo.z) n1_rows(td, lo.z - 1u, w, xa, za, status);  // a gate's folded N1
 }
 
 // Work of entries M[s..r) of a block -- deterministic measurements and N1 --
@@ -297,6 +318,176 @@ __device__ void trace_block(TraceTab& e, const TraceDesc& td, const uint4* L, in
   }
 }
 
+// Row groups of the fused random-measurement phase: W2p threads (the
+// factor words rounded up to a power of two) per group, all in one warp, and
+// at most 32 tableau rows per thread, so a thread's pivot bits fit one word.
+__device__ __forceinline__ bool trace_fused_rows(const TraceTab& e) {
+  int W2p = 1;
+  while (W2p < e.W2) W2p <<= 1;
+  const int R = e.tm.size() / W2p;
+  return W2p <= 32 && R > 0 && (e.n + R - 1) / R <= 32;
+}
+
+// First entry at or after s of a block whose x_q has a set bit in the
+// stabilizer half (the next random measurement) into *first.
+__device__ __forceinline__ void trace_pivot_search(const TraceTab& e, const uint4* M, int s, int B, int* first) {
+  const int t = e.tm.t, size = e.tm.size(), Wn = e.Wn, RS = e.RS;
+  for (int task = t; task < (B - s) * Wn; task += size) {
+    const int kk = task / Wn, w = task - kk * Wn;
+    const uint4 m = M[s + kk];
+    const uint32_t op = m.x & kOpMask;
+    if (op != OP_M && op != OP_RESET) continue;
+    if (e.X[(size_t)(m.x >> 8) * RS + w]) atomicMin(first, s + kk);
+  }
+}
+
+// trace_block with three CTA barriers per random measurement instead of six
+// or seven (when trace_fused_rows holds).  A round of the loop:
+//   phase 1 (after the pivot search's barrier): r = the first random entry;
+//     its pivot p (atomicMin), its factor words FW = x_q (bit p cleared when
+//     read), CW = 0, and the deterministic entries before r evaluated;
+//   phase 2 (barrier C): their headers; the rowsum of the rows with x_p = 1
+//     by rows, the pivot columns folded in: each row group of W2p threads is
+//     one warp, reads the pivot bits of all its rows before any of its
+//     threads writes (__syncwarp), and writes only its own words, so the
+//     pivot-column fix-ups need no barrier; commute parities into CW;
+//   phase 3 (barrier E): the common phase words and their pivot bits, the
+//     factor row, the header and the RESET row; and the next round's pivot
+//     search, whose barrier starts the next round.
+// Rounds with no random entry left end the block after phase 2's headers.
+__device__ void trace_block_fused(TraceTab& e, const TraceDesc& td, const uint4* L, int count, int* sc, int* tacc,
+                                  int* pacc, int* status) {
+  const int t = e.tm.t, size = e.tm.size();
+  const int n = e.n, Wn = e.Wn, W2 = e.W2, RS = e.RS, tw = td.tw;
+  int W2p = 1;
+  while (W2p < W2) W2p <<= 1;
+  const int R = size / W2p;
+  const int gw = t & (W2p - 1), gr = t / W2p;  // word and row group of this thread
+  const bool gact = gw < W2 && gr < R;
+  const unsigned gbase = (unsigned)(t & 31) & ~(unsigned)(W2p - 1);
+  const unsigned gmask = (W2 >= 32 ? 0xffffffffu : ((1u << W2) - 1u)) << gbase;
+  for (int c0 = 0; c0 < count; c0 += kTraceBlockMeas) {
+    const int B = min(kTraceBlockMeas, count - c0);
+    const uint4* M = L + c0;
+    for (int k = t; k < B; k += size) {
+      const uint4 m = M[k];
+      const uint32_t op = m.x & kOpMask;
+      const bool meas = op == OP_M || op == OP_RESET;
+      if ((int)(m.x >> 8) >= n || (meas ? (int)m.z >= td.nm : (int)m.z >= td.nn1))
+        atomicCAS(status, DEV_OK, DEV_BAD_QUDIT);
+      tacc[k] = 0;
+      pacc[k] = 0;
+    }
+    if (t == 0) {
+      sc[0] = INT_MAX;
+      sc[1] = INT_MAX;
+    }
+    if (e.tm.any(*(volatile int*)status != DEV_OK)) return;
+    trace_pivot_search(e, M, 0, B, &sc[0]);  // the first round's
+    e.tm.sync();
+    int s = 0;
+    while (s < B) {
+      // phase 1
+      const int first = sc[0];
+      const int r = first == INT_MAX ? B : first;
+      const int qr = r < B ? (int)(M[r].x >> 8) : 0;
+      if (r < B) {
+        if (t < Wn) {
+          const uint32_t v = e.X[(size_t)qr * RS + t];
+          if (v) atomicMin(&sc[1], (t << 5) + __ffs(v) - 1);
+        }
+        for (int w = t; w < W2; w += size) {
+          e.FW[w] = e.X[(size_t)qr * RS + w];
+          e.CW[w] = 0u;
+        }
+      }
+      if (r > s) trace_det_tasks(e, td, M, s, r, tacc, pacc, status);
+      e.tm.sync();  // C
+      // phase 2
+      if (r > s) trace_det_headers(e, td, M, s, r, tacc, pacc);
+      if (r >= B) break;
+      const uint4 mr = M[r];
+      const int p = sc[1];
+      const int wp = p >> 5, bp = p & 31, wd = Wn + wp;
+      const uint32_t pbit = 1u << bp;
+      const int phc = (int)((e.C0[wp] >> bp) & 1u) | (int)(((e.C1[wp] >> bp) & 1u) << 1);
+      if (t == 0) sc[0] = INT_MAX;  // r was read by every thread before barrier C
+      uint32_t F = 0u, Cp = 0u;
+      if (gact) {
+        F = e.FW[gw];
+        if (gw == wp) F &= ~pbit;
+        uint32_t xpm = 0u, zpm = 0u;
+        int i = 0;
+        for (int k = gr; k < n; k += R, ++i) {
+          xpm |= ((e.X[(size_t)k * RS + wp] >> bp) & 1u) << i;
+          zpm |= ((e.Z[(size_t)k * RS + wp] >> bp) & 1u) << i;
+        }
+        __syncwarp(gmask);  // the group's pivot bits are read before any of its threads writes
+        i = 0;
+        for (int k = gr; k < n; k += R, ++i) {
+          uint32_t* xr = e.X + (size_t)k * RS;
+          uint32_t* zr = e.Z + (size_t)k * RS;
+          const uint32_t xpk = (xpm >> i) & 1u, zpk = (zpm >> i) & 1u;
+          const uint32_t zk = zr[gw];
+          Cp ^= zk & (0u - xpk);
+          uint32_t xn = xr[gw] ^ (F & (0u - xpk));
+          uint32_t zn = zk ^ (F & (0u - zpk));
+          if (gw == wd) {  // x_{n+p}, z_{n+p} := the pivot bits before the rowsum
+            xn = (xn & ~pbit) | (xpk << bp);
+            zn = (zn & ~pbit) | (zpk << bp);
+          } else if (gw == wp) {  // x_p := 0, z_p := [k == q]
+            xn &= ~pbit;
+            zn = (zn & ~pbit) | (k == qr ? pbit : 0u);
+          }
+          xr[gw] = xn;
+          zr[gw] = zn;
+        }
+      }
+      // commute parities: the row groups of a warp by shuffles, then one
+      // atomic per warp and word
+      if (W2p < 32)
+        for (int off = W2p; off < 32; off <<= 1) Cp ^= __shfl_xor_sync(0xffffffffu, Cp, off);
+      if (gact && (t & 31) < W2p && Cp) atomicXor(&e.CW[gw], Cp);
+      e.tm.sync();  // E
+      // phase 3
+      const bool reset = (mr.x & kOpMask) == OP_RESET;
+      uint32_t* row = td.mrow + (size_t)mr.z * 2 * tw;
+      if (gact && gr == 0) {
+        const uint32_t lo_m = (phc & 1) ? 0xffffffffu : 0u;
+        const uint32_t hi_m = (phc & 2) ? 0xffffffffu : 0u;
+        const uint32_t lo = e.C0[gw];
+        const uint32_t a_lo = F & lo_m;
+        uint32_t c0 = lo ^ a_lo;
+        uint32_t c1 = e.C1[gw] ^ (F & (hi_m ^ e.CW[gw])) ^ (lo & a_lo);
+        if (gw == wd) {
+          c0 = (c0 & ~pbit) | ((uint32_t)(phc & 1) << bp);
+          c1 = (c1 & ~pbit) | ((uint32_t)(phc >> 1) << bp);
+        } else if (gw == wp) {
+          c0 &= ~pbit;
+          c1 &= ~pbit;
+        }
+        e.C0[gw] = c0;
+        e.C1[gw] = c1;
+      }
+      for (int w = t; w < tw; w += size) {
+        uint32_t f = w < W2 ? e.FW[w] : 0u;
+        if (w == wp) f &= ~pbit;
+        row[w] = f;
+        if (reset) row[tw + w] = w < W2 ? e.Z[(size_t)qr * RS + w] : 0u;
+      }
+      if (t == 0) {
+        td.mhdr[mr.z] = make_uint4(reset ? 2u : 0u, (uint32_t)p, mr.w, 0u);
+        sc[1] = INT_MAX;
+      }
+      // the next round's pivot search (x / z are final since barrier E)
+      s = r + 1;
+      trace_pivot_search(e, M, s, B, &sc[0]);
+      e.tm.sync();  // the next round's pivot-search barrier
+    }
+    e.tm.sync();
+  }
+}
+
 // Runs the shared part of td's program over its layered schedule and writes
 // the trace.  Each schedule window is staged in shared memory (win: room for
 // kTraceWinSteps steps, then kTraceWinOps ops) with one cooperative load.
@@ -305,6 +496,7 @@ __device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int*
   e.init(0);
   const int t = e.tm.t, size = e.tm.size(), tw = td.tw;
   const int lg = __ffs(tw) - 1;
+  const bool fused = trace_fused_rows(e);
   uint4* wsteps = win;
   uint4* wops = win + kTraceWinSteps;
   for (int wi = 0; wi < td.nwins; ++wi) {
@@ -326,6 +518,8 @@ __device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int*
         const int total = (int)st.z << lg;
         for (int task = t; task < total; task += size) layer_word(e, td, L[task >> lg], task & (tw - 1), status);
         e.tm.sync();
+      } else if (fused) {
+        trace_block_fused(e, td, L, (int)st.z, sc, tacc, pacc, status);
       } else {
         trace_block(e, td, L, (int)st.z, sc, tacc, pacc, status);
       }
