@@ -269,7 +269,8 @@ int sdim_last_stage_ms(const sdim_ctx* ctx, double out[3]);
 int sdim_last_pass_ms(const sdim_ctx* ctx, double out[2]);
 /* The passes of that span timed by themselves, first n of: [0] from the
  * start of the kernels to the end of the last x / z pass, [1] the d = 2 coin
- * pass, [2] the d = 2 column pass, [3] the shot-group engines when they ran
+ * pass, [2] the d = 2 header and column passes (from the end of the x / z
+ * pass; 0 without record columns), [3] the shot-group engines when they ran
  * on their own stream beside the trace engines (0 for a pass that did not
  * run).  No counterpart in the reference. */
 int sdim_last_passes_ms(const sdim_ctx* ctx, double* out, int n);

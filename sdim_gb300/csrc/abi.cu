@@ -59,6 +59,7 @@ struct sdim_ctx {
   DevBuf descs, counters, status, gslots, out, snap, arena, tdescs, trace, masks, tdescs_u8, trace_u8, xz_u8;
   DevBuf gslots_xz;  // d = 2 x / z pass tableaux in global memory (gslots: the shot-group engines')
   DevBuf cols;       // record columns of a d = 2 trace program (trace_cols.cuh)
+  DevBuf dsnap;      // its x / z pass's deterministic snapshots (TraceDesc::snap)
   cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
   cudaStream_t grp = nullptr;                      // shot-group engines of a batch with trace programs
   cudaEvent_t ev_gf = nullptr, ev_gj = nullptr;    // fork to and join from grp
@@ -646,6 +647,18 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.wn = (j.c->n + 31) >> 5;
       td.nused = j.c->nn1_used;
     }
+    if (k == 1 && !skip_xz && jobs[0].c->nmeas > 0) {
+      // one program: the x / z pass leaves the deterministic cross terms to
+      // the header pass, a snapshot per run of deterministic measurements
+      const sdim_circuit* c0 = jobs[0].c;
+      const size_t per = (size_t)8 * c0->n * ((c0->n + 31) >> 5);
+      const long long ns = std::min<long long>(c0->nmeas, (long long)(kSnapBudget / per));
+      if (ns > 0) {
+        if ((rc = ensure(ctx, ctx->dsnap, (size_t)ns * per)) != SDIM_OK) return rc;
+        hd[0].snap = static_cast<uint32_t*>(ctx->dsnap.p);
+        hd[0].nsnap = (int)ns;
+      }
+    }
     if (colform) {
       // the fire masks must be there unless the program has no N1 before its
       // last measurement (a mask budget overflow falls back to the replay)
@@ -860,7 +873,15 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       CK(cudaStreamWaitEvent(s, ctx->ev_xzj[i], 0));
     }
   if (timed) CK(cudaEventRecord(ctx->ev_xzo, s));
-  // ---- column pass: after the x / z pass, beside the rest of the coin pass
+  // ---- header and column passes: after the x / z pass, beside the rest of
+  // the coin pass.  (On a stream of the highest priority their blocks shared
+  // SMs with the coin pass's and the latency-bound column pass took twice as
+  // long: 0.389 against 0.370 ms on the L = 7 step.)
+  if (k == 1 && d2_xz && hd[0].snap) {
+    launch_header_pass((jobs[0].c->nmeas + 3) / 4, s, dd, status);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return cuda_fail(ctx, le, "header pass launch");
+  }
   if (colform && !skip_cols) {
     if (!launch_column_pass(hd[0].tw, (int)((ncols + 32 * kColumnWarps - 1) / (32 * kColumnWarps)), s, dd, status))
       return fail(ctx, SDIM_EINVAL, "no column pass for trace rows of " + std::to_string(hd[0].tw) + " words");
@@ -1224,7 +1245,7 @@ void append_schedule(std::vector<uint2>& dev, size_t op_begin, size_t nops, int 
       continue;
     }
     if (noise && in_block) {
-      lops.push_back(make_uint4(w.x, w.y, nord++, 0u));
+      lops.push_back(make_uint4(w.x, w.y, nord++, mord));  // w: the next measurement's ordinal
       ++steps.back().z;
       continue;
     }
@@ -1468,7 +1489,7 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) cudaStreamSynchronize(ctx->xzs[i]);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
                     &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8,
-                    &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols};
+                    &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols, &ctx->dsnap};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);
@@ -1518,7 +1539,7 @@ int sdim_memory_info(sdim_ctx* ctx, int64_t info[3]) {
   info[1] = (int64_t)total_b;
   const DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap,
                           &ctx->arena, &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8,
-                          &ctx->xz_u8, &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols};
+                          &ctx->xz_u8, &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols, &ctx->dsnap};
   int64_t held = 0;
   for (const DevBuf* b : bufs) held += (int64_t)b->cap;
   info[2] = held;

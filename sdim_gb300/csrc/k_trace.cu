@@ -15,7 +15,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
                                                                   int xz_in_smem, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int red[40];
-  __shared__ int sc[2], tacc[kTraceBlockMeas], pacc[kTraceBlockMeas];
+  __shared__ int sc[3], tacc[kTraceBlockMeas], pacc[kTraceBlockMeas];
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
   uint4* win = reinterpret_cast<uint4*>(smem + hot_bytes + (xz_in_smem ? xz_bytes : 0));
@@ -25,6 +25,44 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
     trace_program(td, e, win, sc, tacc, pacc, status);
     __syncthreads();
   }
+}
+
+// One warp per measurement of descs[0]: a deterministic measurement whose
+// header carries flag 4 gets the cross term T = sum over qudit rows of the
+// pairs i < j of the factor f with f_i z_i f_j x_j (mod 2), from the
+// snapshot of the stabilizer halves its x / z pass took, added to its
+// common phase: w += 2 T (mod 4).  Lane = qudit rows, one ballot per warp.
+__global__ void __launch_bounds__(128) k_header_pass(const TraceDesc* __restrict__ descs, const int* status) {
+  if (*(volatile const int*)status != DEV_OK) return;
+  const TraceDesc* tdp = descs;
+  const int k = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (k >= tdp->nm) return;
+  uint4 h = tdp->mhdr[k];
+  if (!(h.x & 4u)) return;  // uniform over the warp
+  const int n = tdp->c.n, wn = tdp->wn;
+  const uint32_t* f = tdp->mrow + (size_t)k * 2 * tdp->tw;
+  const uint32_t* sx = tdp->snap + (size_t)h.y * 2 * n * wn;
+  const uint32_t* sz = sx + (size_t)n * wn;
+  uint32_t tpar = 0u;
+  for (int kr = lane; kr < n; kr += 32) {
+    uint32_t carry = 0u;
+    for (int w = 0; w < wn; ++w) {
+      const uint32_t fw = f[w];
+      if (!fw) continue;
+      const uint32_t a = sx[(size_t)kr * wn + w] & fw, b = sz[(size_t)kr * wn + w] & fw;
+      uint32_t v = b;
+      v ^= v << 1;
+      v ^= v << 2;
+      v ^= v << 4;
+      v ^= v << 8;
+      v ^= v << 16;
+      const uint32_t excl = (v ^ b) ^ (0u - carry);
+      tpar ^= (uint32_t)__popc(a & excl) & 1u;
+      carry ^= (uint32_t)__popc(b) & 1u;
+    }
+  }
+  const uint32_t par = (uint32_t)__popc(__ballot_sync(0xffffffffu, tpar != 0u)) & 1u;
+  if (lane == 0) tdp->mhdr[k] = make_uint4(h.x & ~4u, 0u, h.z, (h.w + 2u * par) & 3u);
 }
 
 // One single-warp block per group of 32 SPL shots (groups of all programs
@@ -118,6 +156,10 @@ __global__ void __launch_bounds__(256) k_philox_probe(const unsigned long long* 
 
 void launch_philox_probe(int grid, cudaStream_t s, const unsigned long long* seeds, int iters, uint4* sink) {
   k_philox_probe<<<grid, 256, 0, s>>>(seeds, iters, sink);
+}
+
+void launch_header_pass(int grid, cudaStream_t s, const TraceDesc* descs, const int* status) {
+  k_header_pass<<<grid, 128, 0, s>>>(descs, status);
 }
 
 void launch_coin_pass(int grid, int block, size_t smem, cudaStream_t s, const TraceDesc* descs, int ndesc,

@@ -44,6 +44,11 @@ struct TraceDesc {
   uint32_t* masks;
   uint32_t* cmap;
   uint32_t* cols;        // record columns (trace_cols.cuh), null when the phase pass replays
+  // nsnap slots of 2 n wn words: the stabilizer halves of x (n rows of wn
+  // words), then of z, at a run of deterministic measurements; their headers
+  // carry flag 4 and the slot until the header pass adds the cross term
+  uint32_t* snap;
+  int nsnap;
   long long coin_begin;  // first coin-pass item of this program
   int nsteps;
   int nwins;
@@ -182,6 +187,12 @@ inline int column_words(int nm) {
   while (32 * w < nm) w <<= 1;
   return w;
 }
+// Header pass: one warp per measurement of descs[0]; completes the headers
+// of deterministic measurements whose cross terms were left to it.
+void launch_header_pass(int grid, cudaStream_t s, const TraceDesc* descs, const int* status);
+// Device memory the deterministic snapshots of one program may take.
+constexpr size_t kSnapBudget = (size_t)64 << 20;
+
 // Fewest shots for which a run takes the record columns by default (one
 // 32-shot group per SM and scheduler); SDIM_FLAG_COLUMNS takes them at any
 // shot count.

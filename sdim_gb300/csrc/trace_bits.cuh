@@ -149,11 +149,38 @@ __device__ __forceinline__ void layer_word(TraceTab& e, const TraceDesc& td, con
   if (lo.z) n1_rows(td, lo.z - 1u, w, xa, za, status);  // a gate's folded N1
 }
 
+// Ordinal of entry k of a block in the program's measurement order: its own
+// for an M / RESET (z), the next measurement's for an N1 (w, set by the host
+// scheduler), so ordinal(r) - ordinal(s) counts the measurements in [s, r).
+__device__ __forceinline__ uint32_t block_ordinal(const uint4* M, int k, int B) {
+  if (k >= B) {
+    const uint4 m = M[B - 1];
+    const uint32_t op = m.x & kOpMask;
+    return (op == OP_M || op == OP_RESET) ? m.z + 1u : m.w;
+  }
+  const uint4 m = M[k];
+  const uint32_t op = m.x & kOpMask;
+  return (op == OP_M || op == OP_RESET) ? m.z : m.w;
+}
+
+// The snapshot a run of deterministic entries M[s..r) takes (trace.cuh:
+// TraceDesc::snap), or -1 for none: no measurement among them, no snapshot
+// buffer, or all its slots used (then the cross terms are summed here).
+// Read by every thread before the barrier after trace_det_tasks; sc[2]
+// counts the slots used and advances in trace_det_headers.
+__device__ __forceinline__ int det_snapshot(const TraceDesc& td, const uint4* M, int s, int r, int B, const int* sc) {
+  if (!td.snap || block_ordinal(M, r, B) == block_ordinal(M, s, B)) return -1;
+  return sc[2] < td.nsnap ? sc[2] : -1;
+}
+
 // Work of entries M[s..r) of a block -- deterministic measurements and N1 --
 // all on the current tableau, without barriers (M may point into shared
-// memory: plain loads).  tacc / pacc of the entries must be zero.
+// memory: plain loads).  tacc / pacc of the entries must be zero.  With a
+// snapshot slot (snap >= 0) the stabilizer halves of x and z go there and
+// the cross terms are left to the header pass (k_header_pass), which sums
+// them on all SMs; they are this pass's largest share of work on its one SM.
 __device__ __forceinline__ void trace_det_tasks(TraceTab& e, const TraceDesc& td, const uint4* M, int s, int r,
-                                                int* tacc, int* pacc, int* status) {
+                                                int* tacc, int* pacc, int* status, int snap) {
   const int t = e.tm.t, size = e.tm.size();
   const int n = e.n, Wn = e.Wn, W2 = e.W2, RS = e.RS, tw = td.tw;
   const int cnt = r - s;
@@ -177,6 +204,16 @@ __device__ __forceinline__ void trace_det_tasks(TraceTab& e, const TraceDesc& td
     }
     row[w] = f;
     if (op == OP_RESET) row[tw + w] = w < W2 ? e.Z[(size_t)q * RS + w] : 0u;
+  }
+  if (snap >= 0) {
+    uint32_t* sx = td.snap + (size_t)snap * 2 * n * Wn;
+    uint32_t* sz = sx + (size_t)n * Wn;
+    for (int i = t; i < n * Wn; i += size) {
+      const int k = i / Wn, w = i - k * Wn;
+      sx[i] = e.X[(size_t)k * RS + w];
+      sz[i] = e.Z[(size_t)k * RS + w];
+    }
+    return;
   }
   // cross term T: one task per (entry, qudit row), walked without divisions
   int kk = t / n, kr = t - (t / n) * n;
@@ -213,15 +250,18 @@ __device__ __forceinline__ void trace_det_tasks(TraceTab& e, const TraceDesc& td
 }
 
 // Trace headers of the deterministic measurements among M[s..r) (after the
-// barrier that ends trace_det_tasks).
+// barrier that ends trace_det_tasks).  With a snapshot the header carries
+// flag 4 and the slot in y, and w holds the phase without the cross term.
 __device__ __forceinline__ void trace_det_headers(TraceTab& e, const TraceDesc& td, const uint4* M, int s, int r,
-                                                  const int* tacc, const int* pacc) {
+                                                  const int* tacc, const int* pacc, int snap, int* sc) {
   for (int k = s + e.tm.t; k < r; k += e.tm.size()) {
     const uint4 m = M[k];
     const uint32_t op = m.x & kOpMask;
     if (op != OP_M && op != OP_RESET) continue;
-    td.mhdr[m.z] = make_uint4(op == OP_RESET ? 3u : 1u, 0u, m.w, (uint32_t)((pacc[k] + 2 * tacc[k]) & 3));
+    const uint32_t flags = (op == OP_RESET ? 3u : 1u) | (snap >= 0 ? 4u : 0u);
+    td.mhdr[m.z] = make_uint4(flags, snap >= 0 ? (uint32_t)snap : 0u, m.w, (uint32_t)((pacc[k] + 2 * tacc[k]) & 3));
   }
+  if (e.tm.t == 0 && snap >= 0) sc[2] = snap + 1;
 }
 
 // A random measurement with pivot p, on the whole CTA: the rowsum (two
@@ -267,7 +307,8 @@ __device__ void trace_random(TraceTab& e, const TraceDesc& td, const uint4 m, in
 // L[0..count), in shared or global memory).  Per round of the loop: find the
 // first random measurement r at or after s (one atomicMin), evaluate the
 // deterministic entries before it and r's pivot in the same phase, write
-// their headers and run r.  sc: two ints of scratch.
+// their headers and run r.  sc: three ints of scratch (the third counts
+// snapshot slots).
 __device__ void trace_block(TraceTab& e, const TraceDesc& td, const uint4* L, int count, int* sc, int* tacc,
                             int* pacc, int* status) {
   const int t = e.tm.t, size = e.tm.size();
@@ -308,9 +349,10 @@ __device__ void trace_block(TraceTab& e, const TraceDesc& td, const uint4* L, in
         const uint32_t v = e.X[(size_t)(M[r].x >> 8) * RS + t];
         if (v) atomicMin(&sc[1], (t << 5) + __ffs(v) - 1);
       }
-      if (r > s) trace_det_tasks(e, td, M, s, r, tacc, pacc, status);
+      const int snap = r > s ? det_snapshot(td, M, s, r, B, sc) : -1;
+      if (r > s) trace_det_tasks(e, td, M, s, r, tacc, pacc, status, snap);
       e.tm.sync();
-      if (r > s) trace_det_headers(e, td, M, s, r, tacc, pacc);
+      if (r > s) trace_det_headers(e, td, M, s, r, tacc, pacc, snap, sc);
       if (r < B) trace_random(e, td, M[r], sc[1]);
       s = r + 1;
     }
@@ -401,10 +443,11 @@ __device__ void trace_block_fused(TraceTab& e, const TraceDesc& td, const uint4*
           e.CW[w] = 0u;
         }
       }
-      if (r > s) trace_det_tasks(e, td, M, s, r, tacc, pacc, status);
+      const int snap = r > s ? det_snapshot(td, M, s, r, B, sc) : -1;
+      if (r > s) trace_det_tasks(e, td, M, s, r, tacc, pacc, status, snap);
       e.tm.sync();  // C
       // phase 2
-      if (r > s) trace_det_headers(e, td, M, s, r, tacc, pacc);
+      if (r > s) trace_det_headers(e, td, M, s, r, tacc, pacc, snap, sc);
       if (r >= B) break;
       const uint4 mr = M[r];
       const int p = sc[1];
@@ -495,6 +538,7 @@ __device__ void trace_program(const TraceDesc& td, TraceTab& e, uint4* win, int*
                               int* status) {
   e.init(0);
   const int t = e.tm.t, size = e.tm.size(), tw = td.tw;
+  if (t == 0) sc[2] = 0;  // snapshot slots used (the window load's barrier publishes it)
   const int lg = __ffs(tw) - 1;
   const bool fused = trace_fused_rows(e);
   uint4* wsteps = win;
