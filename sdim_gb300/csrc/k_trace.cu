@@ -27,20 +27,44 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
   }
 }
 
-// One warp per measurement of descs[0]: a deterministic measurement whose
-// header carries flag 4 gets the cross term T = sum over qudit rows of the
-// pairs i < j of the factor f with f_i z_i f_j x_j (mod 2), from the
-// snapshot of the stabilizer halves its x / z pass took, added to its
-// common phase: w += 2 T (mod 4).  Lane = qudit rows, one ballot per warp.
+// One warp per measurement k of descs[0], for its deterministic ones:
+//  * with flag 4 in the header, the cross term T = sum over qudit rows of the
+//    pairs i < j of the factor f with f_i z_i f_j x_j (mod 2), from the
+//    snapshot of the stabilizer halves its x / z pass took, is added to its
+//    common phase: w += 2 T (mod 4) (lane = qudit rows, one ballot);
+//  * the coupling mask goes into y: bit t = f_k . z_j (mod 2) for the RESET
+//    j = k - 1 - t when no random measurement lies in [j, k) (the column
+//    pass evaluates such runs of deterministic measurements at once and
+//    corrects each outcome by the earlier RESETs it sees; lane = t).
 __global__ void __launch_bounds__(128) k_header_pass(const TraceDesc* __restrict__ descs, const int* status) {
   if (*(volatile const int*)status != DEV_OK) return;
   const TraceDesc* tdp = descs;
   const int k = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (k >= tdp->nm) return;
-  uint4 h = tdp->mhdr[k];
-  if (!(h.x & 4u)) return;  // uniform over the warp
-  const int n = tdp->c.n, wn = tdp->wn;
-  const uint32_t* f = tdp->mrow + (size_t)k * 2 * tdp->tw;
+  const uint4 h = tdp->mhdr[k];
+  if (!(h.x & 1u)) return;  // random (uniform over the warp)
+  const int n = tdp->c.n, wn = tdp->wn, tw = tdp->tw;
+  const uint32_t* f = tdp->mrow + (size_t)k * 2 * tw;
+  uint32_t cm;
+  {
+    const int j = k - 1 - lane;
+    // read x alone: another warp may be rewriting that header's other words
+    const uint32_t xj = j >= 0 ? *(volatile const uint32_t*)&tdp->mhdr[j].x : 0u;
+    const uint32_t stop = __ballot_sync(0xffffffffu, j < 0 || !(xj & 1u));  // random or before the start
+    const uint32_t in_run = stop ? (1u << (__ffs(stop) - 1)) - 1u : 0xffffffffu;
+    uint32_t c = 0u;
+    if (((in_run >> lane) & 1u) && (xj & 2u)) {
+      const uint32_t* zj = tdp->mrow + (size_t)j * 2 * tw + tw;
+      uint32_t v = 0u;
+      for (int w = 0; w < wn; ++w) v ^= f[w] & zj[w];
+      c = (uint32_t)__popc(v) & 1u;
+    }
+    cm = __ballot_sync(0xffffffffu, c != 0u);
+  }
+  if (!(h.x & 4u)) {
+    if (lane == 0) tdp->mhdr[k] = make_uint4(h.x, cm, h.z, h.w);
+    return;
+  }
   const uint32_t* sx = tdp->snap + (size_t)h.y * 2 * n * wn;
   const uint32_t* sz = sx + (size_t)n * wn;
   uint32_t tpar = 0u;
@@ -62,7 +86,7 @@ __global__ void __launch_bounds__(128) k_header_pass(const TraceDesc* __restrict
     }
   }
   const uint32_t par = (uint32_t)__popc(__ballot_sync(0xffffffffu, tpar != 0u)) & 1u;
-  if (lane == 0) tdp->mhdr[k] = make_uint4(h.x & ~4u, 0u, h.z, (h.w + 2u * par) & 3u);
+  if (lane == 0) tdp->mhdr[k] = make_uint4(h.x & ~4u, cm, h.z, (h.w + 2u * par) & 3u);
 }
 
 // One single-warp block per group of 32 SPL shots (groups of all programs

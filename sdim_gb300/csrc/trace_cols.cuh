@@ -41,6 +41,25 @@ __device__ __forceinline__ int fire_measurement(const uint4* __restrict__ mhdr, 
 // aph_c and the factor sum s (the replay's ((aph_c + 2 s) mod 4 + 1) / 2 mod 2).
 __device__ __forceinline__ uint32_t det_constant(uint32_t aph) { return (((aph & 3u) + 1u) >> 1) & 1u; }
 
+// N words of a row staged in shared memory (16-byte aligned when N % 4 == 0).
+template <int N>
+__device__ __forceinline__ void srow_load(const uint32_t* p, uint32_t (&r)[N]) {
+  if constexpr (N % 4 == 0) {
+    const uint4* p4 = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) {
+      const uint4 v = p4[i];
+      r[4 * i] = v.x;
+      r[4 * i + 1] = v.y;
+      r[4 * i + 2] = v.z;
+      r[4 * i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) r[i] = p[i];
+  }
+}
+
 // Measurements of the trace a column-pass block stages in shared memory at
 // a time: headers and both rows of each, within 48 KB.
 template <int TW>
@@ -109,48 +128,109 @@ __device__ __forceinline__ void column_block(const TraceDesc* __restrict__ tdp, 
       for (int t = threadIdx.x; t < n4; t += 32 * WARPS) dst[t] = __ldg(src + t);
     }
     __syncthreads();
-    // the header one measurement ahead and the factor row at the top of
-    // each step (neither depends on the delta), so the shared-memory loads
-    // overlap the dependent bit arithmetic
     int k = max(wb, k0);
-    uint4 hn = k < we ? shdr[k - wb] : make_uint4(0u, 0u, 0u, 0u);
-    for (; k < we; ++k) {
-      const uint4 h = hn;
-      if (k + 1 < we) hn = shdr[k + 1 - wb];
+    while (k < we) {
+      const uint4 h = shdr[k - wb];
       const uint32_t* row = srow + (size_t)(k - wb) * 2 * TW;
-      uint32_t r[TW];
-#pragma unroll
-      for (int w = 0; w < TW; ++w) r[w] = row[w];
       if (kind == 3 && start == k) {
 #pragma unroll
         for (int w = 0; w < TW; ++w) d1[w] ^= __ldg(inj + w);
       }
-      uint32_t bit;
       if (!(h.x & 1u)) {
+        // a random measurement: the rowsum and the pivot bits
+        uint32_t r[TW];
+#pragma unroll
+        for (int w = 0; w < TW; ++w) r[w] = row[w];
         const int p = (int)h.y, wp = p >> 5, bp = p & 31;
         const uint32_t dp = (word_at<0, TW>(d1, wp) >> bp) & 1u;
         const uint32_t mk = 0u - dp;
 #pragma unroll
         for (int w = 0; w < TW; ++w) d1[w] ^= r[w] & mk;
-        bit = (kind == 2 && start == k) ? 1u : 0u;  // the outcome itself
+        const uint32_t bit = (kind == 2 && start == k) ? 1u : 0u;  // the outcome itself
         put_bit<0, TW>(d1, wn + wp, bp, dp);
         put_bit<0, TW>(d1, wp, bp, bit);
+        if (h.x & 2u) {
+#pragma unroll
+          for (int w = 0; w < TW; ++w) d1[w] ^= row[TW + w] & (0u - bit);
+        }
+        acc |= bit << (k & 31);
+        if ((k & 31) == 31 || k == nm - 1) {
+          if (kind) out[k >> 5] = acc;
+          acc = 0u;
+        }
+        ++k;
+        continue;
+      }
+      // a run of up to 32 deterministic measurements [k, ke): every factor
+      // parity from the delta at the run's start (independent, so they
+      // overlap), each outcome corrected by the earlier RESETs of the run
+      // that its factor sees (the header pass's coupling mask in y against
+      // the run's outcomes so far), then the run's RESET rows XORed in.  A
+      // fire input entering inside the run adds its own parities from its
+      // start on (its outcomes before that are zero).
+      int ke = k + 1;
+      while (ke < we && ke - k < 32 && (shdr[ke - wb].x & 1u)) ++ke;
+      const int len = ke - k;
+      const bool late = kind == 3 && start > k && start < ke;
+      const uint32_t cst = kind == 1 ? 0xffffffffu : 0u;
+      uint32_t hist = 0u, bits = 0u;
+      if (__any_sync(0xffffffffu, late)) {
+        uint32_t v[TW];
+#pragma unroll
+        for (int w = 0; w < TW; ++w) v[w] = late ? __ldg(inj + w) : 0u;
+        for (int i = 0; i < len; ++i) {
+          const uint4 hi = shdr[k + i - wb];
+          uint32_t f[FH];
+          srow_load<FH>(srow + (size_t)(k + i - wb) * 2 * TW, f);
+          uint32_t x = 0u, y = 0u;
+#pragma unroll
+          for (int w = 0; w < FH; ++w) {
+            x ^= f[w] & d1[w];
+            y ^= f[w] & v[w];
+          }
+          uint32_t b = ((uint32_t)__popc(x) ^ (k + i >= start ? (uint32_t)__popc(y) : 0u)) & 1u;
+          b ^= (det_constant(hi.w) & cst) ^ ((uint32_t)__popc(hi.y & hist) & 1u);
+          hist = (hist << 1) | b;
+        }
+#pragma unroll
+        for (int w = 0; w < TW; ++w) d1[w] ^= v[w];
       } else {
-        int s = 0;
+#pragma unroll 4
+        for (int i = 0; i < len; ++i) {
+          const uint4 hi = shdr[k + i - wb];
+          uint32_t f[FH];
+          srow_load<FH>(srow + (size_t)(k + i - wb) * 2 * TW, f);
+          uint32_t x = 0u;
 #pragma unroll
-        for (int w = 0; w < FH; ++w) s += __popc(r[w] & d1[w]);
-        bit = ((uint32_t)s & 1u) ^ (kind == 1 ? det_constant(h.w) : 0u);
+          for (int w = 0; w < FH; ++w) x ^= f[w] & d1[w];
+          const uint32_t b = ((uint32_t)__popc(x) ^ (det_constant(hi.w) & cst) ^ (uint32_t)__popc(hi.y & hist)) & 1u;
+          hist = (hist << 1) | b;
+        }
       }
-      if (h.x & 2u) {
-        const uint32_t mk = 0u - bit;
+      // hist holds the run's outcomes, the last in bit 0: bit i of bits =
+      // measurement k + i
+      bits = __brev(hist) >> (32 - len);
+      for (int i = 0; i < len; ++i) {
+        if (!(shdr[k + i - wb].x & 2u)) continue;
+        uint32_t z[TW];
+        srow_load<TW>(srow + (size_t)(k + i - wb) * 2 * TW + TW, z);
+        const uint32_t mk = 0u - ((bits >> i) & 1u);
 #pragma unroll
-        for (int w = 0; w < TW; ++w) d1[w] ^= row[TW + w] & mk;
+        for (int w = 0; w < TW; ++w) d1[w] ^= z[w] & mk;
       }
-      acc |= bit << (k & 31);
-      if ((k & 31) == 31 || k == nm - 1) {
+      // the run's outcomes into the record words: word k / 32 completes when
+      // the run reaches its end
+      const int sh = k & 31;
+      acc |= bits << sh;
+      if (sh + len >= 32) {
         if (kind) out[k >> 5] = acc;
+        acc = sh + len > 32 ? bits >> (32 - sh) : 0u;
+      }
+      if (ke == nm && (nm & 31)) {
+        if (kind) out[(nm - 1) >> 5] = acc;
         acc = 0u;
       }
+      k = ke;
     }
   }
   if (kind)
