@@ -62,6 +62,15 @@ struct sdim_ctx {
   DevBuf dsnap;      // its x / z pass's deterministic snapshots (TraceDesc::snap)
   cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
   cudaStream_t grp = nullptr;                      // shot-group engines of a batch with trace programs
+  // sdim_run's device-to-host copy of the records, when the record pass can
+  // feed it in chunks (launch_trace_jobs copies each chunk as it is written)
+  static constexpr int kD2HChunks = 4;
+  cudaStream_t cps = nullptr;
+  cudaEvent_t ev_rec[kD2HChunks] = {};
+  cudaEvent_t ev_cps = nullptr;
+  uint8_t* d2h_dst = nullptr;        // host records of the pending sdim_run
+  const uint8_t* d2h_src = nullptr;  // their device buffer
+  bool d2h_done = false;             // the copies are enqueued on cps
   cudaEvent_t ev_gf = nullptr, ev_gj = nullptr;    // fork to and join from grp
   cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr;    // shot-group engines' span on grp (SDIM_FLAG_TIME)
   static constexpr int kXzStreams = 3;
@@ -914,8 +923,25 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   if (colform) {
     const long long groups = (jobs[0].nshots + 31) / 32;
     if (groups > 0x7fffffffLL) return fail(ctx, SDIM_EINVAL, "too many shots in one record pass");
-    if (groups > 0 && !launch_record_pass(cnw, (int)groups, s, dd, groups, status))
-      return fail(ctx, SDIM_EINVAL, "no record pass for columns of " + std::to_string(cnw) + " words");
+    // sdim_run with host records: the record pass in chunks of shots, each
+    // chunk's rows copied down on a copy stream while the next is written
+    const int K = sdim_ctx::kD2HChunks;
+    const bool pipe = ctx->d2h_dst && !ctx->capture && jobs[0].out_dev == ctx->d2h_src && groups >= 8LL * K;
+    const long long per = pipe ? (groups + K - 1) / K : groups;
+    const size_t rowb = (size_t)jobs[0].c->nmeas;
+    for (long long g0 = 0, c = 0; g0 < groups; g0 += per, ++c) {
+      const long long gn = std::min(per, groups - g0);
+      if (!launch_record_pass(cnw, g0, (int)gn, s, dd, gn, status))
+        return fail(ctx, SDIM_EINVAL, "no record pass for columns of " + std::to_string(cnw) + " words");
+      if (pipe) {
+        const long long r0 = 32 * g0, rn = std::min(32 * gn, jobs[0].nshots - r0);
+        CK(cudaEventRecord(ctx->ev_rec[c], s));
+        CK(cudaStreamWaitEvent(ctx->cps, ctx->ev_rec[c], 0));
+        CK(cudaMemcpyAsync(ctx->d2h_dst + (size_t)r0 * rowb, ctx->d2h_src + (size_t)r0 * rowb, (size_t)rn * rowb,
+                           cudaMemcpyDeviceToHost, ctx->cps));
+      }
+    }
+    if (pipe) ctx->d2h_done = true;
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) return cuda_fail(ctx, le, "record pass launch");
   }
@@ -1456,11 +1482,19 @@ int sdim_ctx_create(int device, sdim_ctx** out) {
       cudaEventCreateWithFlags(&ctx->ev_gf, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_gj, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&ctx->ev_g0) != cudaSuccess || cudaEventCreate(&ctx->ev_g1) != cudaSuccess ||
-      cudaEventCreate(&ctx->ev_cols) != cudaSuccess) {
+      cudaEventCreate(&ctx->ev_cols) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->cps, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_cps, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
     return SDIM_ECUDA;
   }
+  for (int i = 0; i < sdim_ctx::kD2HChunks; ++i)
+    if (cudaEventCreateWithFlags(&ctx->ev_rec[i], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      delete ctx;
+      return SDIM_ECUDA;
+    }
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i)
     if (cudaStreamCreateWithFlags(&ctx->xzs[i], cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_xzj[i], cudaEventDisableTiming) != cudaSuccess) {
@@ -1486,6 +1520,7 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   cudaStreamSynchronize(ctx->aux);
   cudaStreamSynchronize(ctx->grp);
+  cudaStreamSynchronize(ctx->cps);
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) cudaStreamSynchronize(ctx->xzs[i]);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
                     &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8,
@@ -1508,6 +1543,9 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   cudaEventDestroy(ctx->ev_g0);
   cudaEventDestroy(ctx->ev_g1);
   cudaEventDestroy(ctx->ev_cols);
+  for (int i = 0; i < sdim_ctx::kD2HChunks; ++i) cudaEventDestroy(ctx->ev_rec[i]);
+  cudaEventDestroy(ctx->ev_cps);
+  cudaStreamDestroy(ctx->cps);
   cudaStreamDestroy(ctx->grp);
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) {
     cudaEventDestroy(ctx->ev_xzj[i]);
@@ -1677,13 +1715,28 @@ int sdim_run(sdim_ctx* ctx, const sdim_circuit* c, uint64_t seed, int64_t shot0,
   CK(cudaMemcpyAsync(c->d_ops, c->h_ops, (size_t)c->blob_words * sizeof(uint2), cudaMemcpyHostToDevice,
                      ctx->stream));
   std::vector<Job> jobs{Job{c, seed, shot0, nshots, direct ? direct : static_cast<uint8_t*>(ctx->out.p)}};
+  ctx->d2h_done = false;
+  if (bytes && !direct) {
+    ctx->d2h_dst = out;
+    ctx->d2h_src = static_cast<uint8_t*>(ctx->out.p);
+  }
   rc = launch_jobs(ctx, jobs, ctx->stream, flags & ~SDIM_FLAG_ASYNC);
-  if (rc != SDIM_OK) return rc;
+  ctx->d2h_dst = nullptr;
+  ctx->d2h_src = nullptr;
+  if (rc != SDIM_OK) {
+    cudaStreamSynchronize(ctx->cps);  // no copy outlives the call
+    return rc;
+  }
   if (flags & SDIM_FLAG_TIME) {
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->timing_pending = true;
   }
-  if (bytes && !direct) CK(cudaMemcpyAsync(out, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (ctx->d2h_done) {  // the record pass's chunks are being copied on cps
+    CK(cudaEventRecord(ctx->ev_cps, ctx->cps));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_cps, 0));
+  } else if (bytes && !direct) {
+    CK(cudaMemcpyAsync(out, ctx->out.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->timing_pending) {
     const int trc = collect_times(ctx);

@@ -136,11 +136,11 @@ __global__ void __launch_bounds__(32 * kColumnWarps) k_column_pass(const TraceDe
 // columns: up to 16 column words, 32 blocks per SM at 64 registers.
 template <int NW>
 __global__ void __launch_bounds__(32, NW >= 32 ? 16 : 32)
-    k_record_pass(const TraceDesc* __restrict__ descs, long long groups, const int* status) {
+    k_record_pass(const TraceDesc* __restrict__ descs, long long g0, long long groups, const int* status) {
   __shared__ __align__(16) uint8_t rec[32 * kRecStride];
   if (*(volatile const int*)status != DEV_OK) return;
   if ((long long)blockIdx.x >= groups) return;
-  record_group<NW>(descs, blockIdx.x, threadIdx.x, rec);
+  record_group<NW>(descs, g0 + blockIdx.x, threadIdx.x, rec);
 }
 
 // One thread per (chunk group, shot) item of the coin pass; descs with
@@ -239,14 +239,14 @@ bool launch_column_pass(int tw, int grid, cudaStream_t s, const TraceDesc* descs
   }
 }
 
-bool launch_record_pass(int nw, int grid, cudaStream_t s, const TraceDesc* descs, long long groups,
+bool launch_record_pass(int nw, long long g0, int grid, cudaStream_t s, const TraceDesc* descs, long long groups,
                         const int* status) {
   switch (nw) {
-    case 2: k_record_pass<2><<<grid, 32, 0, s>>>(descs, groups, status); return true;
-    case 4: k_record_pass<4><<<grid, 32, 0, s>>>(descs, groups, status); return true;
-    case 8: k_record_pass<8><<<grid, 32, 0, s>>>(descs, groups, status); return true;
-    case 16: k_record_pass<16><<<grid, 32, 0, s>>>(descs, groups, status); return true;
-    case 32: k_record_pass<32><<<grid, 32, 0, s>>>(descs, groups, status); return true;
+    case 2: k_record_pass<2><<<grid, 32, 0, s>>>(descs, g0, groups, status); return true;
+    case 4: k_record_pass<4><<<grid, 32, 0, s>>>(descs, g0, groups, status); return true;
+    case 8: k_record_pass<8><<<grid, 32, 0, s>>>(descs, g0, groups, status); return true;
+    case 16: k_record_pass<16><<<grid, 32, 0, s>>>(descs, g0, groups, status); return true;
+    case 32: k_record_pass<32><<<grid, 32, 0, s>>>(descs, g0, groups, status); return true;
     default: return false;
   }
 }

@@ -201,8 +201,9 @@ constexpr long long kColumnMinShots = 152LL * 32 * 4;
 constexpr int kColumnWarps = 4;
 // Column pass: one block per 32 kColumnWarps columns of descs[0].
 bool launch_column_pass(int tw, int grid, cudaStream_t s, const TraceDesc* descs, const int* status);
-// Record pass: one single-warp block per 32-shot group of descs[0].
-bool launch_record_pass(int nw, int grid, cudaStream_t s, const TraceDesc* descs, long long groups,
+// Record pass: one single-warp block per 32-shot group of descs[0], groups
+// g0 .. g0 + groups.
+bool launch_record_pass(int nw, long long g0, int grid, cudaStream_t s, const TraceDesc* descs, long long groups,
                         const int* status);
 
 

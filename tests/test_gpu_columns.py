@@ -131,3 +131,20 @@ def test_kept_trace_and_columns():
     assert np.array_equal(dev.cpu().numpy(), cold)
     _lib.check(ctx.lib.sdim_run_device(ctx.ptr, dp3.ptr, 3, 0, 700, dev.data_ptr(), None, keep), ctx.ptr, "run")
     assert kept(prog3) == (1, 1)
+
+
+@pytest.mark.parametrize("shots", [1024, 4113, 20000])
+def test_records_copied_down_in_chunks(shots):
+    """sdim_run into page-locked host memory: the record pass runs in chunks
+    and each chunk is copied down while the next one is written (partial last
+    chunk and group included); the records equal the device-side run's."""
+    torch = pytest.importorskip("torch")
+    spec = workloads.surface_memory(5, 3, prob=0.02)
+    prog = Program(spec.build())
+    dp, ctx = prog.compile(), prog.context
+    host = torch.zeros((shots, dp.num_records), dtype=torch.uint8, pin_memory=True)
+    _lib.check(ctx.lib.sdim_run(ctx.ptr, dp.ptr, 6, 3, shots, host.data_ptr(), COLS), ctx.ptr, "run")
+    dev = torch.zeros((shots, dp.num_records), dtype=torch.uint8, device="cuda")
+    _lib.check(ctx.lib.sdim_run_device(ctx.ptr, dp.ptr, 6, 3, shots, dev.data_ptr(), None, COLS), ctx.ptr, "run")
+    assert np.array_equal(host.numpy(), dev.cpu().numpy())
+    assert np.array_equal(host.numpy(), run(prog, shots, 6, 3, REPLAY)[0])
