@@ -442,9 +442,10 @@ struct TGroupU8 {
         if (f) sacc += f * ds[i];
       }
     }
-    const int P = M.mo(tm.add(pl));
-    const int T = M.md(tm.add(tl));
-    const int Dd = M.md(tm.add(dl));
+    tm.add3(pl, tl, dl);
+    const int P = M.mo(pl);
+    const int T = M.md(tl);
+    const int Dd = M.md(dl);
     const int aphc = M.mo(P + M.phi * T + M.phi * M.phi * Dd);
     if (nch > 1) {
       if (live && sacc) atomicAdd(&shot_acc[s], sacc);

@@ -14,7 +14,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pass(const TraceDesc* __restr
                                                                   uint8_t* gxz, size_t xz_bytes, size_t hot_bytes,
                                                                   int xz_in_smem, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ int red[40];
+  __shared__ int red[kTeamRedInts];
   __shared__ int sc[3], tacc[kTraceBlockMeas], pacc[kTraceBlockMeas];
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;

@@ -14,7 +14,7 @@ __global__ void __launch_bounds__(TH, TH > kN4Threads ? 1 : 2)
     k_trace_pass_n4(const TraceDescU8* __restrict__ descs, int ndesc, uint8_t* gxz, size_t xz_bytes,
                     size_t hot_bytes, int xz_in_smem, unsigned* queue, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ int red[40];
+  __shared__ int red[kTeamRedInts];
   __shared__ int next;
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;

@@ -17,7 +17,7 @@ __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const Trace
                                                                      uint8_t* gxz, size_t xz_bytes, size_t hot_bytes,
                                                                      int xz_in_smem, unsigned* queue, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ int red[40];
+  __shared__ int red[kTeamRedInts];
   __shared__ int next;
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
@@ -48,7 +48,7 @@ template <int DD>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTracePassThreads)
     k_trace_pass_split(const TraceDescU8* __restrict__ descs, int ndesc, size_t win_off, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ int red[40];
+  __shared__ int red[kTeamRedInts];
   uint2* win = reinterpret_cast<uint2*>(smem + win_off);
   cluster_sync_all();  // both CTAs run before either writes into the other's shared memory
   for (int i = (int)(blockIdx.x >> 1); i < ndesc; i += (int)(gridDim.x >> 1)) {
@@ -66,7 +66,7 @@ __global__ void __cluster_dims__(kTraceClusterCtas, 1, 1) __launch_bounds__(kTra
     k_trace_pass_cluster(const TraceDescU8* __restrict__ descs, int ndesc, uint8_t* gxz, size_t xz_bytes,
                          size_t hot_bytes, int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ int red[40];
+  __shared__ int red[kTeamRedInts];
   uint8_t* xz = kStream ? gxz + (size_t)blockIdx.x * xz_bytes : smem + hot_bytes;
   uint2* win = reinterpret_cast<uint2*>(smem + hot_bytes + (kStream ? 0 : xz_bytes));
   cluster_sync_all();  // every CTA of the cluster runs before any writes into its shared memory

@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(512) k_group_cta(const CircuitDesc* __restrict
                                                    uint8_t* gxz, size_t xz_bytes, size_t hot_bytes, int xz_in_smem,
                                                    int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ int red[40];
+  __shared__ int red[kTeamRedInts];
   __shared__ long long item;
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz + (size_t)blockIdx.x * xz_bytes;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(512) k_group_snapshot(const CircuitDesc* __res
                                                         int xz_in_smem, int8_t* snap, int snap_mode, int snap_lane,
                                                         int* status) {
   extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ int red[40];
+  __shared__ int red[kTeamRedInts];
   const CircuitDesc c = *desc;
   uint8_t* hot = smem;
   uint8_t* xz = xz_in_smem ? smem + hot_bytes : gxz;

@@ -8,6 +8,10 @@
 
 namespace sdim {
 
+// Shared-memory ints a CtaTeam's reductions use (add3: three partial sums per
+// warp of a CTA of up to 1024 threads, and the three results).
+constexpr int kTeamRedInts = 3 * 32 + 8;
+
 struct WarpTeam {
   int t;
   __device__ WarpTeam() : t(threadIdx.x & 31) {}
@@ -15,12 +19,18 @@ struct WarpTeam {
   __device__ __forceinline__ void sync() const { __syncwarp(); }
   __device__ __forceinline__ int min(int v) const { return __reduce_min_sync(0xffffffffu, v); }
   __device__ __forceinline__ int add(int v) const { return __reduce_add_sync(0xffffffffu, v); }
+  // Three sums at once.
+  __device__ __forceinline__ void add3(int& a, int& b, int& c) const {
+    a = __reduce_add_sync(0xffffffffu, a);
+    b = __reduce_add_sync(0xffffffffu, b);
+    c = __reduce_add_sync(0xffffffffu, c);
+  }
   __device__ __forceinline__ unsigned bxor(unsigned v) const { return __reduce_xor_sync(0xffffffffu, v); }
   __device__ __forceinline__ bool any(bool b) const { return __any_sync(0xffffffffu, b); }
   __device__ __forceinline__ bool leader() const { return t == 0; }
 };
 
-// red: at least 33 ints of shared memory owned by the team.
+// red: kTeamRedInts ints of shared memory owned by the team.
 struct CtaTeam {
   int t, nt;
   int* red;
@@ -50,6 +60,42 @@ struct CtaTeam {
   }
   __device__ __forceinline__ int add(int v) const {
     return reduce(v, 0, [](int a, int b) { return a + b; });
+  }
+  // Three sums over the CTA in the barriers of one (three sums one after the
+  // other take three times as many): per-warp partials in red[3 w + i], the
+  // totals in red[96 + i].
+  __device__ __forceinline__ void add3(int& a, int& b, int& c) const {
+    const int lane = t & 31, w = t >> 5, nw = (nt + 31) >> 5;
+    for (int off = 16; off > 0; off >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, off);
+      b += __shfl_xor_sync(0xffffffffu, b, off);
+      c += __shfl_xor_sync(0xffffffffu, c, off);
+    }
+    if (lane == 0) {
+      red[3 * w] = a;
+      red[3 * w + 1] = b;
+      red[3 * w + 2] = c;
+    }
+    __syncthreads();
+    if (w == 0) {
+      int x = lane < nw ? red[3 * lane] : 0, y = lane < nw ? red[3 * lane + 1] : 0,
+          z = lane < nw ? red[3 * lane + 2] : 0;
+      for (int off = 16; off > 0; off >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, off);
+        y += __shfl_xor_sync(0xffffffffu, y, off);
+        z += __shfl_xor_sync(0xffffffffu, z, off);
+      }
+      if (lane == 0) {
+        red[96] = x;
+        red[97] = y;
+        red[98] = z;
+      }
+    }
+    __syncthreads();
+    a = red[96];
+    b = red[97];
+    c = red[98];
+    __syncthreads();
   }
   __device__ __forceinline__ unsigned bxor(unsigned v) const {
     return (unsigned)reduce((int)v, 0, [](int a, int b) { return a ^ b; });

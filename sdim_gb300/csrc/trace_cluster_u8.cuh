@@ -412,9 +412,10 @@ __device__ void cluster_measure(ClusterU8<DD, K, kStream>& e, const TraceDescU8&
       al += acc;
       dl += M.md(dd);
     }
-    const int P = M.mo(e.tm.add(pl_sum));
-    const int A = M.md(e.tm.add(al));
-    const int Dd = M.md(e.tm.add(dl));
+    e.tm.add3(pl_sum, al, dl);
+    const int P = M.mo(pl_sum);
+    const int A = M.md(al);
+    const int Dd = M.md(dl);
     if (e.tm.leader()) {
       int* hs = reinterpret_cast<int*>(e.HS);
       hs[0] = P;

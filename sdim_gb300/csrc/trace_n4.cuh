@@ -354,9 +354,10 @@ __device__ void trace_measure_n4(TabN4<DD>& e, const TraceDescU8& td, int q, uin
       dl += dd % DD;
     }
     e.row_bytes(xq, L.Wh, n, row, sw);
-    const int P = e.tm.add(pl) % DD;
-    const int T = e.tm.add(tl) % DD;
-    const int Dd = e.tm.add(dl) % DD;
+    e.tm.add3(pl, tl, dl);
+    const int P = pl % DD;
+    const int T = tl % DD;
+    const int Dd = dl % DD;
     const int aphc = (P + T + Dd) % DD;
     if (e.tm.leader()) td.mhdr[mord] = make_uint4(reset ? 3u : 1u, 0u, nord, (uint32_t)aphc);
     e.tm.sync();

@@ -313,9 +313,10 @@ __device__ void trace_measure_p3(TabP3& e, const TraceDescU8& td, int q, uint32_
       dl += dk % 3;
     }
     e.row_bytes(xq, L.Wh, n, row, sw);
-    const int P = e.tm.add(pl) % 3;
-    const int T = e.tm.add(tl) % 3;
-    const int Dd = e.tm.add(dl) % 3;
+    e.tm.add3(pl, tl, dl);
+    const int P = pl % 3;
+    const int T = tl % 3;
+    const int Dd = dl % 3;
     const int aphc = (P + T + Dd) % 3;
     if (e.tm.leader()) td.mhdr[mord] = make_uint4(reset ? 3u : 1u, 0u, nord, (uint32_t)aphc);
     e.tm.sync();

@@ -134,9 +134,10 @@ __device__ void trace_measure_u8(TGroupU8<DD, Team>& e, const TraceDescU8& td, i
       dl += M.md(dd);
     }
     for (int g = t; g < sw; g += size) row[g] = g < n ? e.CX[g] : (uint8_t)0;
-    const int P = M.mo(e.tm.add(pl));
-    const int T = M.md(e.tm.add(tl));
-    const int Dd = M.md(e.tm.add(dl));
+    e.tm.add3(pl, tl, dl);
+    const int P = M.mo(pl);
+    const int T = M.md(tl);
+    const int Dd = M.md(dl);
     const int aphc = M.mo(P + M.phi * T + M.phi * M.phi * Dd);
     if (e.tm.leader()) td.mhdr[mord] = make_uint4(reset ? 3u : 1u, 0u, nord, (uint32_t)aphc);
     e.tm.sync();
