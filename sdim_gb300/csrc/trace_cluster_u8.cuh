@@ -412,20 +412,13 @@ __device__ void cluster_measure(ClusterU8<DD, K, kStream>& e, const TraceDescU8&
       al += acc;
       dl += M.md(dd);
     }
-    e.tm.add3(pl_sum, al, dl);
+    e.tm.add3(pl_sum, al, dl);  // its barriers also publish CX / CZ
     const int P = M.mo(pl_sum);
     const int A = M.md(al);
     const int Dd = M.md(dl);
-    if (e.tm.leader()) {
-      int* hs = reinterpret_cast<int*>(e.HS);
-      hs[0] = P;
-      hs[1] = A;
-      hs[2] = Dd;
-      hs[3] = 0;
-    }
-    e.tm.sync();
     uint8_t* slot = b + e.L.det + cs * e.L.slot;
-    put_peer_bytes(slot, e.HS, 16, 0u, t, size);
+    // the slice's sums straight to CTA 0 (every thread holds them)
+    if (t < 4) st_peer_u32(peer_addr(slot + 4 * t, 0u), (uint32_t)(t == 0 ? P : t == 1 ? A : t == 2 ? Dd : 0));
     put_peer_bytes(slot + 16, e.CX, np, 0u, t, size);
     put_peer_bytes(slot + 16 + np, e.CZ, np, 0u, t, size);
     for (int j = t; j < nc; j += size) row[cs * C0 + j] = fb[j];  // this slice of the factor row
