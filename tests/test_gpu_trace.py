@@ -269,3 +269,23 @@ def test_kept_xz_trace_with_coins_in_the_phase_pass():
         state = (ctypes.c_int32 * 2)()
         _lib.check(ctx.lib.sdim_circuit_kept(dp.ptr, state), ctx.ptr, "kept")
         assert state[0] == 1, "the x / z trace was not kept"
+
+
+def test_snapshot_slots_run_out_on_a_wide_program():
+    """n = 2048: a deterministic snapshot is 1 MB, so the 64 MB budget holds
+    64; 80 runs of deterministic measurements (each measured qudit measured
+    again right after its random outcome) use them up and the x / z pass
+    sums the rest's cross terms itself.  Records equal the shot-group
+    engine's."""
+    n = 2048
+    ops = [("H", q, None, {}) for q in range(0, 160)]
+    ops += [("CNOT", q, q + 1, {}) for q in range(0, 159, 2)]
+    ops += [("P", q, None, {}) for q in range(1, 160, 3)]
+    for q in range(80):
+        ops += [("M", 2 * q, None, {}), ("M", 2 * q, None, {})]
+    spec = workloads.CircuitSpec(n, 2, ops)
+    prog = Program(spec.build())
+    rec = prog.sample(64, seed=3, engine="trace")
+    det = rec[0] >> 7
+    assert det[1::2].all() and not det[0::2].any(), "the pairs should alternate random / deterministic"
+    assert np.array_equal(rec, prog.sample(64, seed=3, engine="group"))
