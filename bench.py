@@ -978,7 +978,8 @@ def run_single(args, torch, dist, ws, rank, local):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(dp.num_device_ops * 8),
                 "d2h_bytes_per_step": int(shots * nrec), "ms_per_step": e2e_total / args.steps,
                 "form": "sdim_run into a page-locked host record buffer: instruction stream copied up, records "
-                        "into device memory, then one device-to-host copy; wall clock per call",
+                        "into device memory and copied down (in four chunks behind the record pass when the run "
+                        "takes record columns); wall clock per call",
                 "direct_host": {"value": units_per_step * len(staged_ms) / (sum(staged_ms) / 1e3), "unit": UNIT,
                                 "ms_per_step": statistics.mean(staged_ms),
                                 "form": "the same call with SDIM_FLAG_DIRECT_HOST: the kernels store the records "

@@ -366,7 +366,7 @@ int finish(sdim_ctx* ctx, cudaStream_t s, unsigned flags) {
 // written this way reach the host with the kernels' own stores, so no
 // device-to-host copy follows.  Without the flag (null) they are staged in
 // device memory and copied down, which measured faster for the d = 2 trace
-// engine's record runs (0.67 against 0.95 ms for 38.5 MB of records).
+// engine's record runs (0.56 against 1.16 ms for 38.5 MB of records).
 uint8_t* mapped_host(void* p, unsigned flags) {
   if (!p || !(flags & SDIM_FLAG_DIRECT_HOST)) return nullptr;
   cudaPointerAttributes a;
