@@ -425,7 +425,7 @@ def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=11):
     CTA when the byte tableau fits in shared memory; else, in a batch of at
     least num_sms / 2, a CTA pair when that fits and one CTA streaming from
     HBM above; in a smaller batch a cluster of 8 CTAs, columns in shared
-    memory up to n = 636 and streamed from global memory, held in L2, above."""
+    memory up to n = 642 and streamed from global memory, held in L2, above."""
     few = 2 * odd_trace_programs < num_sms
     if d in (3, 5, 7) and (not few or (n >= 128 and u8_single_cta(n, smem_optin))):
         th = packed_threads(n, few)
@@ -441,8 +441,8 @@ def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=11):
         return (2, "smem") if pair + win + 4096 <= smem_optin else (1, "hbm")
     cols = (n + 3) // 4
     sl = _split_stride(cols)
-    xchg = 16 + 16 + 2 * npad + ((cols + 15) & ~15) + 4 * (16 + 2 * npad)
-    hot = r16(2 * sl + 2 * npad) + 4 * sl + 16 + 2 * r16(xchg)
+    xchg = 4 * (16 + 2 * npad) + 5 * ((cols + 15) & ~15)
+    hot = r16(2 * sl) + 4 * sl + 16 + 2 * r16(xchg)
     return 8, ("smem" if hot + r16(2 * n * sl) + win + 4096 <= smem_optin else "l2")
 
 

@@ -38,6 +38,7 @@ FLAG_LANE_SHOTS_1 = 65536
 FLAG_REUSE_XZ = 262144
 FLAG_COLUMNS = 524288
 FLAG_PHASE_REPLAY = 1048576
+FLAG_UNLAYERED = 2097152
 
 
 def engine_flags(engine) -> int:

@@ -60,6 +60,7 @@ struct sdim_ctx {
   DevBuf gslots_xz;  // d = 2 x / z pass tableaux in global memory (gslots: the shot-group engines')
   DevBuf cols;       // record columns of a d = 2 trace program (trace_cols.cuh)
   DevBuf dsnap;      // its x / z pass's deterministic snapshots (TraceDesc::snap)
+  DevBuf cdet;       // deterministic slice sums of the odd-d cluster x / z passes (TraceDescU8::dsum)
   cudaStream_t aux = nullptr;                      // coin pass, concurrent with the x / z pass
   cudaStream_t grp = nullptr;                      // shot-group engines of a batch with trace programs
   // sdim_run's device-to-host copy of the records, when the record pass can
@@ -144,6 +145,8 @@ struct sdim_circuit {
   int nsteps = 0, nwins = 0, nn1_used = 0;
   int64_t fops_off = 0;  // frame instruction stream (frame.cuh), inside the blob
   int nfops = 0;
+  const uint2* d_lay = nullptr;  // odd d: the layered x / z stream (append_layers_u8), inside the blob
+  int nlay = 0;
   // d = 2 x / z trace kept on the device for SDIM_FLAG_REUSE_XZ: written by a
   // run with the flag, valid once that synchronous run has ended without a
   // device error, then read by the later runs with the flag instead of
@@ -701,15 +704,26 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
   std::vector<TraceDescU8> hu(ku);
   TraceDescU8* du = nullptr;
   if (ku) {
-    std::vector<size_t> off(ku);
-    size_t total = 0;
+    // per program its trace, and for a cluster x / z pass (odd_xz_mode 3, 4)
+    // its deterministic slice sums
+    std::vector<size_t> off(ku), doff(ku, SIZE_MAX);
+    std::vector<int> xmode(ku);
+    size_t total = 0, dtotal = 0;
     for (size_t i = 0; i < ku; ++i) {
+      const Job& j = ujobs[i];
       size_t o[5];
-      trace_offsets_u8(ujobs[i].c->nmeas, ujobs[i].c->nn1, trace_row_bytes_u8(ujobs[i].c->n), o);
+      trace_offsets_u8(j.c->nmeas, j.c->nn1, trace_row_bytes_u8(j.c->n), o);
       off[i] = total;
       total += o[4];
+      const int mode = odd_xz_mode(j.c->n, j.c->d, (long long)ku, flags, (size_t)ctx->smem_optin, ctx->num_sms);
+      xmode[i] = mode;
+      if (mode == 3 || mode == 4) {
+        doff[i] = dtotal;
+        dtotal += round_up((size_t)j.c->nmeas * trace_u8_cluster_det(j.c->n), 256);
+      }
     }
     if ((rc = ensure(ctx, ctx->trace_u8, std::max<size_t>(total, 256))) != SDIM_OK) return rc;
+    if (dtotal && (rc = ensure(ctx, ctx->cdet, dtotal)) != SDIM_OK) return rc;
     if ((rc = ensure(ctx, ctx->tdescs_u8, sizeof(TraceDescU8) * ku)) != SDIM_OK) return rc;
     long long groups = 0;
     for (size_t i = 0; i < ku; ++i) {
@@ -738,6 +752,14 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.nhdr = reinterpret_cast<uint2*>(b + o[3]);
       td.nm = j.c->nmeas;
       td.nn1 = j.c->nn1;
+      td.dsum = doff[i] == SIZE_MAX ? nullptr : static_cast<uint8_t*>(ctx->cdet.p) + doff[i];
+      // the byte forms walk the layered stream (gate groups); the CTA pair
+      // and the packed forms the instructions as written
+      const int xm = xmode[i];
+      if ((xm == 0 || xm == 2 || xm == 3 || xm == 4) && j.c->d_lay && !(flags & SDIM_FLAG_UNLAYERED)) {
+        td.lay = j.c->d_lay;
+        td.nlay = j.c->nlay;
+      }
     }
     du = static_cast<TraceDescU8*>(ctx->tdescs_u8.p);
     if ((rc = upload_descs(ctx, du, hu.data(), sizeof(TraceDescU8), ku, offsetof(TraceDescU8, c),
@@ -862,6 +884,9 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       const size_t clusters = in_smem ? std::min<size_t>(e - b, 65535 / kTraceClusterCtas) : stream_clusters(e - b);
       launch_trace_u8_cluster(v, (int)clusters, smem, rs, du + b, (int)(e - b),
                               static_cast<uint8_t*>(ctx->xz_u8.p) + run.slot_off, xz, hot, in_smem ? 1 : 0, status);
+      int maxnm = 0;
+      for (size_t i = b; i < e; ++i) maxnm = std::max(maxnm, hu[i].nm);
+      launch_cluster_det_headers(maxnm, rs, du + b, (int)(e - b), status);
     } else {
       const size_t hot = trace_u8_hot_bytes(nmax), xz = trace_u8_xz_bytes(nmax);
       const bool in_smem = mode == 0;
@@ -1212,6 +1237,71 @@ int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* n
   return SDIM_OK;
 }
 
+// Layered instruction stream of an odd-d program for the byte x / z passes
+// (trace_u8.cuh, trace_cluster_u8.cuh), appended to dev: the program's
+// instructions, with each run of gates between two measurements, RESETs or
+// N1 reordered into layers -- every gate goes one layer after the last gate
+// that shares a qudit with it, so a layer's gates act on pairwise disjoint
+// qudits -- and each layer cut into groups of up to kGateGroup gates, a
+// group being the header {OP_GROUP, count} and its gates.  Gates on disjoint
+// qudits commute and their phase terms add, so a thread applies a group to
+// its column with all operands loaded first.  No group straddles a window of
+// kOpWindow words (NOPs pad the window's end).  Gates on out-of-range qudits
+// stay single, for the walker's own check.
+void append_layers_u8(std::vector<uint2>& dev, size_t op_begin, size_t nops, int n, int64_t& off, int& count) {
+  std::vector<uint2> out;
+  std::vector<std::vector<uint2>> layers;
+  std::vector<int> level(std::max(n, 1), -1);
+  std::vector<int> touched;
+  auto put_group = [&](const uint2* g, int cnt) {
+    const size_t pos = out.size() % (size_t)kOpWindow;
+    if (pos + (size_t)cnt + 1 > (size_t)kOpWindow)
+      out.insert(out.end(), (size_t)kOpWindow - pos, make_uint2(OP_NOP, 0u));
+    out.push_back(make_uint2(OP_GROUP, (uint32_t)cnt));
+    out.insert(out.end(), g, g + cnt);
+  };
+  auto flush = [&]() {
+    for (const auto& l : layers)
+      for (size_t a = 0; a < l.size(); a += kGateGroup) {
+        const int cnt = (int)std::min<size_t>(kGateGroup, l.size() - a);
+        if (cnt == 1)
+          out.push_back(l[a]);
+        else
+          put_group(l.data() + a, cnt);
+      }
+    layers.clear();
+    for (int q : touched) level[q] = -1;
+    touched.clear();
+  };
+  for (size_t i = op_begin; i < op_begin + nops; ++i) {
+    const uint2 w = dev[i];
+    const uint32_t op = w.x & kOpMask;
+    if (op == OP_NOP) continue;
+    const bool gate = op >= OP_X && op <= OP_CNOT_INV;
+    const bool two = op == OP_CNOT || op == OP_CNOT_INV;
+    const int q = (int)(w.x >> 8), t = (int)w.y;
+    if (!gate || q >= n || (two && t >= n)) {
+      flush();
+      out.push_back(w);
+      continue;
+    }
+    int lv = level[q] + 1;
+    if (two) lv = std::max(lv, level[t] + 1);
+    if (lv == (int)layers.size()) layers.emplace_back();
+    layers[lv].push_back(make_uint2(w.x & ~kOpEnd, w.y));
+    if (level[q] < 0) touched.push_back(q);
+    level[q] = lv;
+    if (two) {
+      if (level[t] < 0) touched.push_back(t);
+      level[t] = lv;
+    }
+  }
+  flush();
+  off = (int64_t)dev.size();
+  count = (int)out.size();
+  dev.insert(dev.end(), out.begin(), out.end());
+}
+
 // Layered schedule of a d = 2 program for the trace engine's x / z pass,
 // appended to dev after the instruction words (16-byte aligned):
 //   steps[s] = {kind, first, count, 0}: kind 0 is a gate layer -- ops on
@@ -1524,7 +1614,7 @@ int sdim_ctx_destroy(sdim_ctx* ctx) {
   for (int i = 0; i < sdim_ctx::kXzStreams; ++i) cudaStreamSynchronize(ctx->xzs[i]);
   DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap, &ctx->arena,
                     &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8, &ctx->xz_u8,
-                    &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols, &ctx->dsnap};
+                    &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols, &ctx->dsnap, &ctx->cdet};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (ctx->staging) cudaFreeHost(ctx->staging);
@@ -1577,7 +1667,7 @@ int sdim_memory_info(sdim_ctx* ctx, int64_t info[3]) {
   info[1] = (int64_t)total_b;
   const DevBuf* bufs[] = {&ctx->descs, &ctx->counters, &ctx->status, &ctx->gslots, &ctx->out, &ctx->snap,
                           &ctx->arena, &ctx->tdescs, &ctx->trace, &ctx->masks, &ctx->tdescs_u8, &ctx->trace_u8,
-                          &ctx->xz_u8, &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols, &ctx->dsnap};
+                          &ctx->xz_u8, &ctx->xz_queue, &ctx->gslots_xz, &ctx->cols, &ctx->dsnap, &ctx->cdet};
   int64_t held = 0;
   for (const DevBuf* b : bufs) held += (int64_t)b->cap;
   info[2] = held;
@@ -1605,6 +1695,9 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
   const size_t ndev = dev.size();
   TraceSchedule sch;
   if (d == 2 && trace_words(n)) append_schedule(dev, 0, ndev, n, kTraceWinSteps, kTraceWinOps, sch);
+  int64_t lay_off = -1;
+  int nlay = 0;
+  if (d != 2) append_layers_u8(dev, 0, ndev, n, lay_off, nlay);
   int64_t fops_off = 0;
   int nfops = 0;
   append_frame_ops(ops, nops, noise_prob, dev, fops_off, nfops);
@@ -1647,6 +1740,10 @@ int sdim_encode_circuit(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const d
     c->nsteps = sch.nsteps;
     c->nwins = sch.nwins;
     c->nn1_used = sch.nn1_used;
+  }
+  if (lay_off >= 0) {
+    c->d_lay = c->d_ops + lay_off;
+    c->nlay = nlay;
   }
   c->fops_off = fops_off;
   c->nfops = nfops;
@@ -2021,6 +2118,8 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
   std::vector<uint2> dev;
   std::vector<size_t> op_off(ncirc);
   std::vector<TraceSchedule> sch(ncirc);
+  std::vector<int64_t> lay_off(ncirc, -1);
+  std::vector<int> nlay(ncirc, 0);
   std::vector<sdim_circuit> circs(ncirc);
   int rc;
   for (int i = 0; i < ncirc; ++i) {
@@ -2040,6 +2139,7 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
     c.nops = (int)(dev.size() - op_off[i]);
     if (d[i] == 2 && trace_words(n[i]))
       append_schedule(dev, op_off[i], (size_t)c.nops, n[i], kTraceWinSteps, kTraceWinOps, sch[i]);
+    if (d[i] != 2) append_layers_u8(dev, op_off[i], (size_t)c.nops, n[i], lay_off[i], nlay[i]);
     c.variant = variant_for(d[i]);
     c.gvariant = group_variant_for(d[i], n[i], 0);
     c.gblock = variant_ops(c.gvariant).cta ? cta_block_for(n[i]) : 32;
@@ -2072,6 +2172,10 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
       circs[i].nsteps = sch[i].nsteps;
       circs[i].nwins = sch[i].nwins;
       circs[i].nn1_used = sch[i].nn1_used;
+    }
+    if (lay_off[i] >= 0) {
+      circs[i].d_lay = base + lay_off[i];
+      circs[i].nlay = nlay[i];
     }
   }
   const bool on_dev = flags & SDIM_FLAG_OUT_DEVICE;

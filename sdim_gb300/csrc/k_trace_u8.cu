@@ -77,6 +77,17 @@ __global__ void __cluster_dims__(kTraceClusterCtas, 1, 1) __launch_bounds__(kTra
   }
 }
 
+// Deterministic headers of the cluster x / z pass: program blockIdx.y of
+// descs, one warp per measurement.
+__global__ void __launch_bounds__(128) k_cluster_det_headers(const TraceDescU8* __restrict__ descs, int ndesc,
+                                                             const int* status) {
+  if (*(volatile const int*)status != DEV_OK) return;  // the trace is incomplete
+  const int i = (int)blockIdx.y;
+  const int m = (int)blockIdx.x * 4 + (int)(threadIdx.x >> 5);
+  if (i >= ndesc || m >= descs[i].nm) return;
+  cluster_det_header<kTraceClusterCtas>(descs[i], m, (int)(threadIdx.x & 31));
+}
+
 template <int DD>
 __global__ void __launch_bounds__(512) k_phase_pass_u8(const TraceDescU8* __restrict__ descs, int ndesc,
                                                        long long total_groups, const int* status) {
@@ -138,6 +149,15 @@ size_t trace_u8_split_smem(int n) { return round16(split_smem_bytes(n)); }
 size_t trace_u8_window_bytes() { return sizeof(uint2) * kOpWindow; }
 size_t trace_u8_cluster_hot(int n) { return round16(cluster_hot_bytes(n, kTraceClusterCtas)); }
 size_t trace_u8_cluster_xz(int n) { return round16(cluster_xz_bytes(n, kTraceClusterCtas)); }
+size_t trace_u8_cluster_det(int n) { return cluster_det_bytes(n, kTraceClusterCtas); }
+
+void launch_cluster_det_headers(int maxnm, cudaStream_t s, const TraceDescU8* d, int nd, int* status) {
+  if (maxnm <= 0) return;
+  for (int b = 0; b < nd; b += 65535) {
+    const dim3 grid((unsigned)((maxnm + 3) / 4), (unsigned)std::min(65535, nd - b));
+    k_cluster_det_headers<<<grid, 128, 0, s>>>(d + b, nd - b, status);
+  }
+}
 
 void launch_trace_u8_cluster(int variant, int clusters, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
                              uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status) {

@@ -95,6 +95,12 @@ __host__ __device__ inline size_t coin_map_bytes(long long nchunk, long long nsh
 
 // Trace of one odd-d program (layout in trace_u8.cuh); N1 coins are drawn in
 // its phase pass.
+// Instructions the odd-d x / z passes stage in shared memory at a time.
+constexpr int kOpWindow = 512;
+
+// Gates in one OP_GROUP of a layered odd-d stream (abi.cu: append_layers_u8).
+constexpr int kGateGroup = 8;
+
 struct TraceDescU8 {
   CircuitDesc c;  // item_begin counts 32-shot groups of the phase pass
   uint4* mhdr;
@@ -102,7 +108,10 @@ struct TraceDescU8 {
   uint8_t* nrow;
   uint2* nhdr;  // N1 ordinal j: (coin threshold, opcode), 0xffffffff for probability 0
   int nm, nn1;
-  int sw;  // bytes per trace row
+  int sw;         // bytes per trace row
+  uint8_t* dsum;  // cluster x / z pass: per measurement its deterministic slice sums (cluster_det_bytes)
+  const uint2* lay;  // the byte x / z passes' layered instruction stream (OP_GROUP), or null: c.ops
+  int nlay;
 };
 
 __host__ __device__ inline int trace_row_bytes_u8(int n) { return (int)round_up((size_t)2 * n, 16); }
@@ -237,6 +246,12 @@ size_t trace_u8_cluster_hot(int n);
 size_t trace_u8_cluster_xz(int n);
 void launch_trace_u8_cluster(int variant, int clusters, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd,
                              uint8_t* gxz, size_t xzb, size_t hot, int in_smem, int* status);
+// Each program's deterministic slice sums: trace_u8_cluster_det(n) bytes per
+// measurement at TraceDescU8::dsum.  After the cluster x / z pass of programs
+// d[0, nd), with at most maxnm measurements each, the deterministic-header
+// pass writes their deterministic outcomes' common phases.
+size_t trace_u8_cluster_det(int n);
+void launch_cluster_det_headers(int maxnm, cudaStream_t s, const TraceDescU8* d, int nd, int* status);
 void launch_trace_u8_phase(int variant, int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d,
                            int nd, long long total, int* status);
 

@@ -165,7 +165,7 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     """sdim_trace_xz_mode (host-only) on GB300's limits.  Residue bytes
     (d >= 11, or SDIM_FLAG_U8_XZ): one CTA to n = 226; for batches of 76+
     programs a CTA pair to n = 330, then one streaming CTA; for smaller
-    batches an eight-CTA cluster, in shared memory to n = 636.  d = 3: one
+    batches an eight-CTA cluster, in shared memory to n = 642.  d = 3: one
     CTA on the bit-plane tableau, in shared memory to n = 448, then
     streamed.  d = 5, 7: one CTA on 4-bit lanes, in shared memory to n = 320,
     then streamed in batches of 76+ and the byte cluster in smaller ones.
@@ -177,7 +177,7 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     optin, sms = 232448, 152
     mode = lambda n, progs, flags=0, d=11: lib.sdim_trace_xz_mode(n, d, progs, flags, optin, sms)  # noqa: E731
     assert [mode(n, 1000) for n in (1, 226, 227, 330, 331, 2048)] == [0, 0, 1, 1, 2, 2]
-    assert [mode(n, 75) for n in (226, 227, 636, 637, 2048)] == [0, 3, 3, 4, 4]
+    assert [mode(n, 75) for n in (226, 227, 642, 643, 2048)] == [0, 3, 3, 4, 4]
     assert mode(100, 1000, _lib.FLAG_CLUSTER_XZ) == 3
     assert mode(100, 1, _lib.FLAG_CLUSTER_XZ | _lib.FLAG_FORCE_GMEM) == 4
     assert mode(100, 1, _lib.FLAG_FORCE_GMEM) == 2
@@ -195,7 +195,7 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     # (more room for its row-group sums), so the shared-memory limits differ
     for d, batch_max, lone_max in ((5, 324, 315), (7, 320, 310)):
         assert [mode(n, 1000, 0, d) for n in (1, 256, batch_max, batch_max + 1, 2048)] == [7, 7, 7, 8, 8]
-        assert [mode(n, 75, 0, d) for n in (127, 128, 226, 227, 636, 637)] == [0, 7, 7, 3, 3, 4]
+        assert [mode(n, 75, 0, d) for n in (127, 128, 226, 227, 642, 643)] == [0, 7, 7, 3, 3, 4]
         assert [mode(n, 1, packed, d) for n in (256, lone_max, lone_max + 1)] == [7, 7, 8]
         assert mode(100, 1, packed | _lib.FLAG_FORCE_GMEM, d) == 8
     forms = {0: (1, "smem"), 1: (2, "smem"), 2: (1, "hbm"), 3: (8, "smem"), 4: (8, "l2"), 5: (1, "smem"),

@@ -57,9 +57,9 @@ def test_deterministic_sweep_across_slices(n, d, flags):
     assert np.array_equal(rec, _run(prog, 11, 0, 40, _lib.FLAG_TRACE | _lib.FLAG_SPLIT_XZ)), (n, d)
 
 
-@pytest.mark.parametrize("n,d", [(400, 7), (636, 5), (637, 3), (1000, 5)])
+@pytest.mark.parametrize("n,d", [(400, 7), (642, 5), (643, 3), (1000, 5)])
 def test_large_programs_every_odd_d_pass(n, d):
-    """Around the shared-memory limit of the cluster's columns (n = 636):
+    """Around the shared-memory limit of the cluster's columns (n = 642):
     cluster in shared memory, cluster streamed, one CTA streamed and the
     shot-group engine agree; the oracle checks two shots."""
     spec = workloads.random_hpc(n, d, 2 * n, seed=n, mr_every=n // 2, mr_fraction=0.1)
@@ -90,3 +90,24 @@ def test_mixed_batch_routes_every_mode(large):
     for e, s, out in zip(runner.entries, specs, outs):
         prog = Program(s.build())
         assert np.array_equal(out, prog.sample(e.shots, seed=e.seed, shot0=e.shot0, engine="group")), s.name
+
+
+@pytest.mark.parametrize("flags", [_lib.FLAG_TRACE | _lib.FLAG_U8_XZ,
+                                   _lib.FLAG_TRACE | _lib.FLAG_U8_XZ | _lib.FLAG_FORCE_GMEM, CLUSTER, STREAMED],
+                         ids=["cta", "cta-gmem", "cluster", "streamed"])
+@pytest.mark.parametrize("d", [3, 7, 11])
+@pytest.mark.parametrize("kind", ["hpc", "all-gates"])
+def test_layered_gate_groups(kind, d, flags):
+    """The byte x / z passes walk the layered stream: gates between
+    measurements in groups on disjoint qudits.  Runs of up to 2,000 gates,
+    so that groups meet the ends of the 512-word instruction windows; every
+    gate kind and N1 between them.  Records equal the gates applied one at a
+    time (SDIM_FLAG_UNLAYERED) and the oracle."""
+    if kind == "hpc":
+        spec = workloads.random_hpc(40, d, 2000, seed=d, mr_every=700, mr_fraction=0.2)
+    else:
+        spec = workloads.all_gates_random(12, d, 1500, seed=d, noise_probs=(0.0, 0.3, 1.0))
+    prog = Program(spec.build())
+    rec = _run(prog, 5, 0, 64, flags)
+    assert np.array_equal(rec, _run(prog, 5, 0, 64, flags | _lib.FLAG_UNLAYERED)), (kind, d)
+    assert np.array_equal(rec[:8], oracle_run([spec], 5, 0, 8)["records"]), (kind, d)
