@@ -82,8 +82,8 @@ extern "C" {
                                      measurements */
 #define SDIM_FLAG_PHASE_REPLAY 1048576u /* d = 2 trace engine: never the record columns (every shot
                                            replays its phase deltas) */
-#define SDIM_FLAG_UNLAYERED 2097152u /* odd-d trace engine: the byte x / z passes apply the gates one at a
-                                        time as written (by default they walk the program's layered
+#define SDIM_FLAG_UNLAYERED 2097152u /* odd-d trace engine: the cluster x / z pass applies the gates one at
+                                        a time as written (by default it walks the program's layered
                                         stream: gates between measurements in groups on disjoint qudits) */
 #define SDIM_FLAG_DIRECT_HOST 8192u /* host outputs in page-locked memory: the kernels store the records
                                        into the host buffer directly, with no device buffer and no copy

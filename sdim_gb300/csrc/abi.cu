@@ -753,10 +753,11 @@ int launch_trace_jobs(sdim_ctx* ctx, std::vector<Job> jobs, std::vector<Job> ujo
       td.nm = j.c->nmeas;
       td.nn1 = j.c->nn1;
       td.dsum = doff[i] == SIZE_MAX ? nullptr : static_cast<uint8_t*>(ctx->cdet.p) + doff[i];
-      // the byte forms walk the layered stream (gate groups); the CTA pair
-      // and the packed forms the instructions as written
+      // the cluster walks the layered stream (gate groups); the other forms
+      // the instructions as written.  On GB300: oddd5's cluster x / z pass
+      // 2.17 ms layered against 2.21, PR1's single CTA 0.257 against 0.241
       const int xm = xmode[i];
-      if ((xm == 0 || xm == 2 || xm == 3 || xm == 4) && j.c->d_lay && !(flags & SDIM_FLAG_UNLAYERED)) {
+      if ((xm == 3 || xm == 4) && j.c->d_lay && !(flags & SDIM_FLAG_UNLAYERED)) {
         td.lay = j.c->d_lay;
         td.nlay = j.c->nlay;
       }
@@ -1237,17 +1238,18 @@ int encode_rows(sdim_ctx* ctx, const int32_t* ops, int64_t nops, const double* n
   return SDIM_OK;
 }
 
-// Layered instruction stream of an odd-d program for the byte x / z passes
-// (trace_u8.cuh, trace_cluster_u8.cuh), appended to dev: the program's
+// Layered instruction stream of an odd-d program for the cluster x / z pass
+// (trace_cluster_u8.cuh), appended to dev: the program's
 // instructions, with each run of gates between two measurements, RESETs or
 // N1 reordered into layers -- every gate goes one layer after the last gate
 // that shares a qudit with it, so a layer's gates act on pairwise disjoint
 // qudits -- and each layer cut into groups of up to kGateGroup gates, a
 // group being the header {OP_GROUP, count} and its gates.  Gates on disjoint
 // qudits commute and their phase terms add, so a thread applies a group to
-// its column with all operands loaded first.  No group straddles a window of
-// kOpWindow words (NOPs pad the window's end).  Gates on out-of-range qudits
-// stay single, for the walker's own check.
+// its column with all operands loaded first.  Each run starts with
+// {OP_RUN, words}, so that warps holding no column pass it in one step.  No
+// group straddles a window of kOpWindow words (NOPs pad the window's end).
+// Gates on out-of-range qudits stay single, for the walker's own check.
 void append_layers_u8(std::vector<uint2>& dev, size_t op_begin, size_t nops, int n, int64_t& off, int& count) {
   std::vector<uint2> out;
   std::vector<std::vector<uint2>> layers;
@@ -1261,6 +1263,9 @@ void append_layers_u8(std::vector<uint2>& dev, size_t op_begin, size_t nops, int
     out.insert(out.end(), g, g + cnt);
   };
   auto flush = [&]() {
+    if (layers.empty()) return;
+    const size_t head = out.size();  // {OP_RUN, words of the run}
+    out.push_back(make_uint2(OP_RUN, 0u));
     for (const auto& l : layers)
       for (size_t a = 0; a < l.size(); a += kGateGroup) {
         const int cnt = (int)std::min<size_t>(kGateGroup, l.size() - a);
@@ -1269,6 +1274,7 @@ void append_layers_u8(std::vector<uint2>& dev, size_t op_begin, size_t nops, int
         else
           put_group(l.data() + a, cnt);
       }
+    out[head].y = (uint32_t)(out.size() - head - 1);
     layers.clear();
     for (int q : touched) level[q] = -1;
     touched.clear();

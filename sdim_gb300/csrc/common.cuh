@@ -29,7 +29,8 @@ enum DevOp : uint32_t {
   OP_N1F = 18,   // flip: X^a, a != 0
   OP_N1P = 19,   // phase: Z^b, b != 0
   OP_N1OFF = 20,  // N1 whose coin never fires (prob 0): only advances the noise ordinal
-  OP_GROUP = 21   // layered odd-d x / z streams only: y gates on pairwise disjoint qudits follow
+  OP_GROUP = 21,  // layered odd-d x / z streams only: y gates on pairwise disjoint qudits follow
+  OP_RUN = 22     // layered odd-d x / z streams only: a run of gates (y words) follows
 };
 
 // Instruction word: x = opcode | qudit << 8; y = target qudit (two-qudit

@@ -12,7 +12,10 @@ namespace {
 // CTAs than programs) every CTA takes the next program from the atomic
 // counter, so the programs (largest first) are dealt out as CTAs free up;
 // without, CTA b takes programs b, b + grid, ...
-template <int DD>
+// Team: StreamCtaTeam (16 rows in flight) when the tableau streams from
+// global memory, CtaTeam (8) when it sits in shared memory, which leaves the
+// in-smem kernel registers to spare.
+template <int DD, class Team>
 __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const TraceDescU8* __restrict__ descs, int ndesc,
                                                                      uint8_t* gxz, size_t xz_bytes, size_t hot_bytes,
                                                                      int xz_in_smem, unsigned* queue, int* status) {
@@ -30,7 +33,7 @@ __global__ void __launch_bounds__(kTracePassThreads) k_trace_pass_u8(const Trace
   }
   while (i < ndesc) {
     const TraceDescU8 td = descs[i];
-    TGroupU8<DD, StreamCtaTeam> e(xz, hot, td.c.n, td.c.d, StreamCtaTeam(red));
+    TGroupU8<DD, Team> e(xz, hot, td.c.n, td.c.d, Team(red));
     trace_program_u8(td, e, win, status);
     __syncthreads();
     if (queue) {
@@ -102,7 +105,8 @@ __global__ void __launch_bounds__(512) k_phase_pass_u8(const TraceDescU8* __rest
 template <int DD>
 struct TraceU8 {
   static cudaError_t set_smem(int optin) {
-    cudaError_t e = set_dynamic_smem(k_trace_pass_u8<DD>, optin);
+    cudaError_t e = set_dynamic_smem(k_trace_pass_u8<DD, CtaTeam>, optin);
+    if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_u8<DD, StreamCtaTeam>, optin);
     if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_split<DD>, optin);
     if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_cluster<DD, false>, optin);
     if (e == cudaSuccess) e = set_dynamic_smem(k_trace_pass_cluster<DD, true>, optin);
@@ -122,7 +126,10 @@ struct TraceU8 {
   }
   static void xz(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, uint8_t* gxz,
                  size_t xzb, size_t hot, int in_smem, unsigned* queue, int* status) {
-    k_trace_pass_u8<DD><<<grid, block, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, queue, status);
+    if (in_smem)
+      k_trace_pass_u8<DD, CtaTeam><<<grid, block, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, queue, status);
+    else
+      k_trace_pass_u8<DD, StreamCtaTeam><<<grid, block, smem, s>>>(d, nd, gxz, xzb, hot, in_smem, queue, status);
   }
   static void phase(int grid, int block, size_t smem, cudaStream_t s, const TraceDescU8* d, int nd, long long total,
                     int* status) {

@@ -110,7 +110,7 @@ struct TraceDescU8 {
   int nm, nn1;
   int sw;         // bytes per trace row
   uint8_t* dsum;  // cluster x / z pass: per measurement its deterministic slice sums (cluster_det_bytes)
-  const uint2* lay;  // the byte x / z passes' layered instruction stream (OP_GROUP), or null: c.ops
+  const uint2* lay;  // the cluster x / z pass's layered instruction stream (OP_GROUP), or null: c.ops
   int nlay;
 };
 

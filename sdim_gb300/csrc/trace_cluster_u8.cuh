@@ -595,12 +595,18 @@ __device__ void cluster_program(const TraceDescU8& td, ClusterU8<DD, K, kStream>
   const uint2* ops = td.lay ? td.lay : c.ops;
   const int nops = td.lay ? td.nlay : c.nops;
   uint32_t mord = 0, nord = 0;
+  const bool colless = (t & ~31) >= nc;  // this thread's warp holds no column
+  int skip_to = 0;
   for (int i = 0; i < nops; ++i) {
     if ((i & (kOpWindow - 1)) == 0) {  // stage the next window of instructions
       e.tm.sync();
       const int cnt = min(kOpWindow, nops - i);
       for (int j = t; j < cnt; j += size) win[j] = __ldg(ops + i + j);
       e.tm.sync();
+    }
+    if (i < skip_to) {  // a warp with no column passes a run of gates, stopping at window starts
+      i = min(skip_to, (i | (kOpWindow - 1)) + 1) - 1;
+      continue;
     }
     const uint2 cur = win[i & (kOpWindow - 1)];
     const uint32_t op = cur.x & kOpMask;
@@ -613,6 +619,9 @@ __device__ void cluster_program(const TraceDescU8& td, ClusterU8<DD, K, kStream>
     bool bad = false;
     switch (op) {
       case OP_NOP: break;
+      case OP_RUN:
+        if (colless) skip_to = i + 1 + (int)cur.y;
+        break;
       case OP_GROUP: {  // never straddles a window; the column owners apply it
         const int cnt = (int)cur.y;
         const uint2* gops = win + ((i + 1) & (kOpWindow - 1));

@@ -150,28 +150,29 @@ __device__ void trace_measure_u8(TGroupU8<DD, Team>& e, const TraceDescU8& td, i
 }
 
 // Column j of a group of cnt <= kGateGroup gates on pairwise disjoint qudits
-// (ops: their instruction words): X, Z rows of `stride` bytes, phases C.
-// Every operand is loaded before any result is stored, so the group costs
-// about one gate's latency; the gates commute and their phase terms add, so
-// the order within the group does not matter.  Per gate the arithmetic of
+// (ops: their instruction words, in shared memory): X, Z rows of `stride`
+// bytes, phases C.  Every operand is loaded before any result is stored, so
+// the loads of the group overlap; the gates commute and their phase terms
+// add, so the order within the group does not matter.  Per gate the arithmetic of
 // TGroupU8's h, h_inv, p, cnot and pauli (group_u8.cuh).
 template <class Mod>
 __device__ __forceinline__ void gate_group_column(const uint2* ops, int cnt, uint8_t* X, uint8_t* Z, size_t stride,
                                                   uint8_t* C, int j, const Mod& M) {
-  int xa[kGateGroup], za[kGateGroup], xb[kGateGroup], zb[kGateGroup];
-  uint2 w[kGateGroup];
+  // operands of gate g packed in v[g]: x_a | z_a << 8 | x_b << 16 | z_b << 24
+  // (b: a CNOT's target), one register a gate
+  uint32_t v[kGateGroup];
 #pragma unroll
   for (int g = 0; g < kGateGroup; ++g) {
     if (g < cnt) {
-      w[g] = ops[g];
-      const size_t qa = (size_t)(w[g].x >> 8) * stride + j, qb = (size_t)w[g].y * stride + j;
-      xa[g] = X[qa];
-      za[g] = Z[qa];
-      const uint32_t op = w[g].x & kOpMask;
+      const uint2 w = ops[g];
+      const size_t qa = (size_t)(w.x >> 8) * stride + j;
+      uint32_t a = (uint32_t)X[qa] | ((uint32_t)Z[qa] << 8);
+      const uint32_t op = w.x & kOpMask;
       if (op == OP_CNOT || op == OP_CNOT_INV) {
-        xb[g] = X[qb];
-        zb[g] = Z[qb];
+        const size_t qb = (size_t)w.y * stride + j;
+        a |= ((uint32_t)X[qb] << 16) | ((uint32_t)Z[qb] << 24);
       }
+      v[g] = a;
     }
   }
   int ph = C[j];
@@ -179,8 +180,10 @@ __device__ __forceinline__ void gate_group_column(const uint2* ops, int cnt, uin
 #pragma unroll
   for (int g = 0; g < kGateGroup; ++g) {
     if (g < cnt) {
-      const int x = xa[g], z = za[g];
-      switch (w[g].x & kOpMask) {
+      const uint2 w = ops[g];
+      const size_t qa = (size_t)(w.x >> 8) * stride + j;
+      const int x = (int)(v[g] & 0xffu), z = (int)((v[g] >> 8) & 0xffu);
+      switch (w.x & kOpMask) {
         case OP_X: ph += M.phi * (d - 1) * z; break;
         case OP_X_INV: ph += M.phi * z; break;
         case OP_Z: ph += M.phi * x; break;
@@ -188,34 +191,29 @@ __device__ __forceinline__ void gate_group_column(const uint2* ops, int cnt, uin
         case OP_H: {
           const int nx = M.neg(z);
           ph += M.phi * nx * x;
-          xa[g] = nx;
-          za[g] = x;
+          X[qa] = (uint8_t)nx;
+          Z[qa] = (uint8_t)x;
           break;
         }
         case OP_H_INV: {
           const int nz = M.neg(x);
           ph += M.phi * z * nz;
-          xa[g] = z;
-          za[g] = nz;
+          X[qa] = (uint8_t)z;
+          Z[qa] = (uint8_t)nz;
           break;
         }
-        case OP_P: ph += M.mo((x * (x - 1)) >> 1); za[g] = M.md(z + x); break;
-        case OP_P_INV: ph += M.ord - M.mo((x * (x - 1)) >> 1); za[g] = M.md(z + d - x); break;
-        case OP_CNOT: xb[g] = M.md(xb[g] + x); za[g] = M.md(z + d - zb[g]); break;
-        case OP_CNOT_INV: xb[g] = M.md(xb[g] + d - x); za[g] = M.md(z + zb[g]); break;
+        case OP_P: ph += M.mo((x * (x - 1)) >> 1); Z[qa] = (uint8_t)M.md(z + x); break;
+        case OP_P_INV: ph += M.ord - M.mo((x * (x - 1)) >> 1); Z[qa] = (uint8_t)M.md(z + d - x); break;
+        case OP_CNOT:
+        case OP_CNOT_INV: {
+          const int xb = (int)((v[g] >> 16) & 0xffu), zb = (int)(v[g] >> 24);
+          const bool inv = (w.x & kOpMask) == OP_CNOT_INV;
+          X[(size_t)w.y * stride + j] = (uint8_t)M.md(inv ? xb + d - x : xb + x);
+          Z[qa] = (uint8_t)M.md(inv ? z + zb : z + d - zb);
+          break;
+        }
         default: break;
       }
-    }
-  }
-#pragma unroll
-  for (int g = 0; g < kGateGroup; ++g) {
-    if (g < cnt) {
-      const uint32_t op = w[g].x & kOpMask;
-      const size_t qa = (size_t)(w[g].x >> 8) * stride + j;
-      if (op == OP_H || op == OP_H_INV) X[qa] = (uint8_t)xa[g];
-      if (op == OP_H || op == OP_H_INV || op == OP_P || op == OP_P_INV || op == OP_CNOT || op == OP_CNOT_INV)
-        Z[qa] = (uint8_t)za[g];
-      if (op == OP_CNOT || op == OP_CNOT_INV) X[(size_t)w[g].y * stride + j] = (uint8_t)xb[g];
     }
   }
   C[j] = (uint8_t)M.mo(ph);
@@ -229,14 +227,12 @@ __device__ void trace_program_u8(const TraceDescU8& td, TGroupU8<DD, Team>& e, u
   e.init(0);
   const int t = e.tm.t, size = e.tm.size();
   const int n = c.n, d = c.d, S = e.S, sw = td.sw;
-  const uint2* ops = td.lay ? td.lay : c.ops;
-  const int nops = td.lay ? td.nlay : c.nops;
   uint32_t mord = 0, nord = 0;
-  for (int i = 0; i < nops; ++i) {
+  for (int i = 0; i < c.nops; ++i) {
     if ((i & (kOpWindow - 1)) == 0) {  // stage the next window of instructions
       e.tm.sync();
-      const int cnt = min(kOpWindow, nops - i);
-      for (int j = t; j < cnt; j += size) win[j] = __ldg(ops + i + j);
+      const int cnt = min(kOpWindow, c.nops - i);
+      for (int j = t; j < cnt; j += size) win[j] = __ldg(c.ops + i + j);
       e.tm.sync();
     }
     const uint2 cur = win[i & (kOpWindow - 1)];
@@ -248,15 +244,6 @@ __device__ void trace_program_u8(const TraceDescU8& td, TGroupU8<DD, Team>& e, u
     }
     switch (op) {
       case OP_NOP: break;
-      case OP_GROUP: {
-        // the group never straddles a window; column g of each row was last
-        // written by thread g mod size: no barrier needed
-        const int cnt = (int)cur.y;
-        const uint2* gops = win + ((i + 1) & (kOpWindow - 1));
-        for (int g = t; g < 2 * n; g += size) gate_group_column(gops, cnt, e.X, e.Z, (size_t)S, e.C, g, e.M);
-        i += cnt;
-        break;
-      }
       case OP_X: e.pauli(q, d - 1, 0); break;
       case OP_X_INV: e.pauli(q, 1, 0); break;
       case OP_Z: e.pauli(q, 0, 1); break;

@@ -92,13 +92,11 @@ def test_mixed_batch_routes_every_mode(large):
         assert np.array_equal(out, prog.sample(e.shots, seed=e.seed, shot0=e.shot0, engine="group")), s.name
 
 
-@pytest.mark.parametrize("flags", [_lib.FLAG_TRACE | _lib.FLAG_U8_XZ,
-                                   _lib.FLAG_TRACE | _lib.FLAG_U8_XZ | _lib.FLAG_FORCE_GMEM, CLUSTER, STREAMED],
-                         ids=["cta", "cta-gmem", "cluster", "streamed"])
+@pytest.mark.parametrize("flags", [CLUSTER, STREAMED], ids=["smem", "streamed"])
 @pytest.mark.parametrize("d", [3, 7, 11])
 @pytest.mark.parametrize("kind", ["hpc", "all-gates"])
 def test_layered_gate_groups(kind, d, flags):
-    """The byte x / z passes walk the layered stream: gates between
+    """The cluster x / z pass walks the layered stream: gates between
     measurements in groups on disjoint qudits.  Runs of up to 2,000 gates,
     so that groups meet the ends of the 512-word instruction windows; every
     gate kind and N1 between them.  Records equal the gates applied one at a
