@@ -2126,6 +2126,13 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
   std::vector<TraceSchedule> sch(ncirc);
   std::vector<int64_t> lay_off(ncirc, -1);
   std::vector<int> nlay(ncirc, 0);
+  // layered streams only serve the cluster x / z pass, which a batch takes
+  // only with fewer than num_sms / 2 odd-d programs (odd_xz_mode); larger
+  // batches skip building them (SDIM_FLAG_CLUSTER_XZ then walks the
+  // instructions as written)
+  int odd = 0;
+  for (int i = 0; i < ncirc; ++i) odd += d[i] != 2 ? 1 : 0;
+  const bool layered = 2 * odd < ctx->num_sms;
   std::vector<sdim_circuit> circs(ncirc);
   int rc;
   for (int i = 0; i < ncirc; ++i) {
@@ -2145,7 +2152,7 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
     c.nops = (int)(dev.size() - op_off[i]);
     if (d[i] == 2 && trace_words(n[i]))
       append_schedule(dev, op_off[i], (size_t)c.nops, n[i], kTraceWinSteps, kTraceWinOps, sch[i]);
-    if (d[i] != 2) append_layers_u8(dev, op_off[i], (size_t)c.nops, n[i], lay_off[i], nlay[i]);
+    if (d[i] != 2 && layered) append_layers_u8(dev, op_off[i], (size_t)c.nops, n[i], lay_off[i], nlay[i]);
     c.variant = variant_for(d[i]);
     c.gvariant = group_variant_for(d[i], n[i], 0);
     c.gblock = variant_ops(c.gvariant).cta ? cta_block_for(n[i]) : 32;
