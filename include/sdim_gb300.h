@@ -231,6 +231,19 @@ int sdim_run_tables(sdim_ctx* ctx, int ncirc, const int32_t* rows, const int64_t
  * counterpart in the reference. */
 int sdim_trace_xz_mode(int32_t n, int32_t d, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
                        int32_t num_sms);
+/* The device instruction words of a program (rows as in
+ * sdim_encode_circuit), or with layered != 0 (odd d) the layered stream the
+ * cluster x / z pass walks instead: gates between measurements, RESETs and
+ * N1 reordered into layers on disjoint qudits, in groups of up to 8 behind
+ * {OP_GROUP = 21, count} headers, each run of gates behind {OP_RUN = 22,
+ * words}, no group across a 512-word window.  Word k is out[2k] (opcode |
+ * qudit << 8) and out[2k + 1] (target or N1 threshold); *count receives the
+ * number of words.  Host-only (no device is touched), for inspection and
+ * tests.  The codes of sdim_encode_circuit; SDIM_ENOMEM when cap words are
+ * too few (*count still set); SDIM_EINVAL for layered with d = 2.  No
+ * counterpart in the reference. */
+int sdim_program_words(const int32_t* ops, int64_t nops, const double* noise_prob, int32_t n, int32_t d,
+                       int32_t layered, uint32_t* out, int64_t cap, int64_t* count);
 /* Measured shared-memory read bandwidth of the device in GB/s (all SMs):
  * the roofline denominator for tableaux resident in shared memory.  No
  * counterpart in the reference (which has no device code). */

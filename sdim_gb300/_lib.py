@@ -86,6 +86,7 @@ SIGNATURES = {
     "sdim_probe_smem_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_probe_l2_bandwidth": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_trace_xz_mode": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_uint, C.c_int32, C.c_int32]),
+    "sdim_program_words": (C.c_int, [_P, C.c_int64, _P, C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "sdim_probe_philox_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sdim_graph_create": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, C.c_uint, C.POINTER(_P)]),
     "sdim_graph_launch": (C.c_int, [_P, _P, _P, _P]),

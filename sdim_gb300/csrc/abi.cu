@@ -1478,6 +1478,31 @@ void append_frame_ops(const int32_t* ops, int64_t nops, const double* noise_prob
 
 extern "C" {
 
+int sdim_program_words(const int32_t* ops, int64_t nops, const double* noise_prob, int32_t n, int32_t d,
+                       int32_t layered, uint32_t* out, int64_t cap, int64_t* count) {
+  if ((nops > 0 && !ops) || nops < 0 || !count || (cap > 0 && !out) || cap < 0) return SDIM_EINVAL;
+  std::vector<uint2> dev;
+  int nmeas = 0, nn1 = 0;
+  const int rc = encode_rows(nullptr, ops, nops, noise_prob, n, d, dev, nmeas, nn1);
+  if (rc != SDIM_OK) return rc;
+  size_t first = 0, len = dev.size();
+  if (layered) {
+    if (d == 2) return SDIM_EINVAL;
+    int64_t off = 0;
+    int cnt = 0;
+    append_layers_u8(dev, 0, dev.size(), n, off, cnt);
+    first = (size_t)off;
+    len = (size_t)cnt;
+  }
+  *count = (int64_t)len;
+  if ((int64_t)len > cap) return SDIM_ENOMEM;
+  for (size_t k = 0; k < len; ++k) {
+    out[2 * k] = dev[first + k].x;
+    out[2 * k + 1] = dev[first + k].y;
+  }
+  return SDIM_OK;
+}
+
 int sdim_trace_xz_mode(int32_t n, int32_t d, int64_t odd_trace_programs, unsigned flags, int32_t smem_optin,
                        int32_t num_sms) {
   if (n < 1 || n > kTraceU8MaxQudits || d < 3 || !(d & 1) || odd_trace_programs < 0 || smem_optin <= 0 ||
