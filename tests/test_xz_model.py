@@ -1,14 +1,14 @@
 """CPU: the x / z pass model (tests/xz_model.py).  Its tableau equals the
-oracle's after every instruction, and the blocked form -- the rank-1
-updates of consecutive random measurements deferred and applied in one pass
--- gives the same trace records and final state as one measurement at a
-time, for every block size."""
+oracle's after every instruction; the blocked form -- the rank-1 updates of
+consecutive random measurements deferred and applied in one pass -- gives
+the same trace records and final state as one measurement at a time, for
+every block size; so does the cluster pass's decomposition."""
 import numpy as np
 import pytest
 
 from sdim_gb300 import workloads
 from tests.conftest import oracle_run
-from tests.xz_model import blocked_xz, sequential_xz
+from tests.xz_model import blocked_xz, cluster_xz, sequential_xz
 
 
 def _ops(spec):
@@ -69,3 +69,23 @@ def test_blocked_sweeps_are_mostly_random():
     recs, _ = sequential_xz(n, d, _ops(workloads.random_hpc(n, d, 8 * n, seed=3)))
     kinds = [h[0] for h, _, _ in recs]
     assert kinds.count("rand") >= 0.8 * n
+
+
+@pytest.mark.parametrize("d", [3, 5, 7])
+@pytest.mark.parametrize("n,kind", [(1, "twice"), (3, "hpc"), (6, "twice"), (13, "hpc"), (30, "twice"), (37, "hpc")])
+def test_cluster_decomposition_matches_sequential(n, d, kind):
+    """The cluster pass's arithmetic (slices, the unexponentiated pivot
+    column with scaled factors, the deterministic slice sums as byte dot
+    products and the cross-slice header term) gives the one-at-a-time
+    records and final state; slices are empty for n < 4 and ragged when 4
+    does not divide n."""
+    ops = _ops(_spec(n, d, seed=n * 7 + d, kind=kind))
+    seq, st = sequential_xz(n, d, ops)
+    cl, ct = cluster_xz(n, d, ops)
+    assert len(seq) == len(cl)
+    for i, ((h1, r1, z1), (h2, r2, z2)) in enumerate(zip(seq, cl)):
+        assert h1 == h2, (i, h1, h2)
+        assert np.array_equal(r1, r2), i
+        assert (z1 is None) == (z2 is None) and (z1 is None or np.array_equal(z1, z2)), i
+    assert np.array_equal(st.X, ct.X) and np.array_equal(st.Z, ct.Z) and np.array_equal(st.C, ct.C)
+    assert any(h[0] == "det" for h, _, _ in seq) or n == 1 or kind == "hpc"

@@ -10,6 +10,11 @@ generators, plus the z_q row after a RESET.  Its X and Z equal the
 reference's tableau (sdim/tableau/tableau_prime.py:88-380) at every
 instruction, checked against the oracle in tests/test_xz_model.py.
 
+``cluster_xz`` restates the cluster pass's decomposition (candidates per
+slice, the unexponentiated pivot column with scaled factors, deterministic
+slice sums as byte dot products, the cross-slice header term) and gives the
+same records and final state.
+
 ``blocked_xz`` computes the same records and the same final state with the
 rank-1 updates of up to ``block`` consecutive random measurements deferred
 and applied in one pass over the tableau: the form that reads and writes a
@@ -266,4 +271,104 @@ def blocked_xz(n: int, d: int, ops, block: int) -> Tuple[List, _Tab]:
             dfr.flush()
             tab.gate(gid, q, t)
     dfr.flush()
+    return recs, tab
+
+
+def _byte_dot(a, b):
+    """dp4a over one word: the sum of four byte products."""
+    return int((np.asarray(a, dtype=np.int64) * np.asarray(b, dtype=np.int64)).sum())
+
+
+def cluster_xz(n: int, d: int, ops, K: int = 8) -> Tuple[List, _Tab]:
+    """The arithmetic of the cluster x / z pass (sdim_gb300/csrc/
+    trace_cluster_u8.cuh) over whole arrays: H = K / 2 stabilizer slices of
+    C0 = ceil(n / H) columns.
+    - Pivot: each slice's lowest column with x_q != 0 is its candidate, the
+      lowest candidate the pivot.
+    - Random outcome: the rank-1 update runs with the pivot column as it
+      stands and the factors scaled by the exponent e (x += (e f) cx is the
+      update with the exponentiated column e cx); the dots and the column's
+      self-dot are taken on the unexponentiated column and scaled by e, e^2.
+    - Deterministic outcome: per slice the partial sums P_c = sum f c and, per
+      row, words of four columns with Z_w = f . z, X_w = f . x and the in-word
+      terms sum_j x_j (z . G_j), G_j holding f_i f_j in byte i < j and
+      f_j (f_j - 1) / 2 in byte j (so the in-slice cross terms and the
+      f (f - 1) / 2 x.z terms share one sum, phi = 1 for odd d); the header
+      pass adds the cross-slice term sum_k sum_{c' < c} Z_c'[k] X_c[k].
+    Returns (records, tableau) as sequential_xz does."""
+    assert d % 2 == 1
+    tab = _Tab(n, d)
+    X, Z, C = tab.X, tab.Z, tab.C
+    H = K // 2
+    C0 = -(-n // H)
+    slices = [(c * C0, max(c * C0, min(n, (c + 1) * C0))) for c in range(H)]  # empty past n
+    recs: List = []
+    for gid, q, t in ops:
+        if gid not in (M, RESET):
+            tab.gate(gid, q, t)
+            continue
+        cands = [a + int(np.nonzero(X[q, a:b])[0][0]) for a, b in slices if b > a and X[q, a:b].any()]
+        if cands:
+            p = min(cands)
+            cx, cz = X[:, p].copy(), Z[:, p].copy()  # unexponentiated
+            xv = int(X[q, p])
+            e = 1 if xv == 1 else _inv(xv, d)
+            f = (-X[q]) % d
+            f[p] = 0
+            g = (e * f) % d
+            dot_raw = (Z.T @ cx) % d  # old z
+            X[:] = (X + np.outer(cx, g)) % d
+            Z[:] = (Z + np.outer(cz, g)) % d
+            s0 = int((cx * cz).sum()) % d
+            s1 = (e * e % d) * s0 % d
+            phc = int(C[p]) if e == 1 else (int(C[p]) * e + (s0 * ((e * (e - 1) // 2) % d)) % d) % d
+            dot = (e * dot_raw) % d
+            half = (s1 * ((f * (f - 1)) // 2)) % d
+            C[:] = np.where(f != 0, (C + phc * f + (f * dot) % d + half) % d, C)
+            X[:, n + p], Z[:, n + p], C[n + p] = (e * cx) % d, (e * cz) % d, phc
+            X[:, p], Z[:, p], C[p] = 0, 0, 0
+            Z[q, p] = 1
+            hdr, row = ("rand", p, e, 0), f
+        else:
+            fall = X[q, n:].copy()
+            P_, A = 0, 0
+            zc, xc = [], []
+            for a, b in slices:
+                f = np.zeros(4 * -(-(b - a) // 4), dtype=np.int64)
+                f[:b - a] = fall[a:b]
+                P_ += int((fall[a:b] * C[a:b]).sum())
+                G = []
+                for w in range(len(f) // 4):
+                    fw = f[4 * w:4 * w + 4]
+                    G.append([[fw[i] * fw[j] if i < j else (fw[j] * (fw[j] - 1)) // 2 if i == j else 0
+                               for i in range(4)] for j in range(4)])
+                zk, xk = np.zeros(n, dtype=np.int64), np.zeros(n, dtype=np.int64)
+                for k in range(n):
+                    xr = np.zeros(len(f), dtype=np.int64)
+                    zr = np.zeros(len(f), dtype=np.int64)
+                    xr[:b - a], zr[:b - a] = X[k, a:b], Z[k, a:b]
+                    pre = acc = xs = 0
+                    for w in range(len(f) // 4):
+                        fw, xw, zw = f[4 * w:4 * w + 4], xr[4 * w:4 * w + 4], zr[4 * w:4 * w + 4]
+                        if not fw.any():
+                            continue
+                        zs, xsw = _byte_dot(zw, fw), _byte_dot(xw, fw)
+                        inw = sum(int(xw[j]) * _byte_dot(zw, G[w][j]) for j in range(4))
+                        acc = (acc + pre * xsw + inw) % d
+                        pre = (pre + zs) % d
+                        xs += xsw
+                    zk[k], xk[k] = pre, xs % d
+                    A += acc
+                zc.append(zk)
+                xc.append(xk)
+            cross = 0
+            zb = np.zeros(n, dtype=np.int64)
+            for c in range(H):
+                cross += int((zb * xc[c]).sum())
+                zb += zc[c]
+            aphc = (P_ + A + cross) % d
+            row = np.zeros(2 * n, dtype=np.int64)
+            row[:n] = fall
+            hdr = ("det", 0, 1, aphc)
+        _records_append(recs, hdr, row, Z[q].copy() if gid == RESET else None)
     return recs, tab
