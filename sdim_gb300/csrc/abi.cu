@@ -465,8 +465,9 @@ constexpr int kTraceU8MaxQudits = 2048;
 // shared memory (5) up to n = 448 on GB300, else in a global-memory slot (6).
 // For d = 5 and 7 likewise on the 4-bit-lane tableau (trace_n4.cuh): shared
 // memory (7) up to n = 320, else a global-memory slot (8).  A cluster shares each
-// measurement's fixed cost (two cluster barriers, pivot search, broadcast)
-// among 8 SMs, so it finishes one program sooner but a full batch later.
+// measurement's fixed cost (a cluster barrier, pivot search, candidate
+// broadcast) among 8 SMs, so it finishes one program sooner but a full batch
+// later.
 // Threads of a packed odd-d x / z pass CTA for programs of up to n qudits:
 // about one per qudit (64 to 512) in a batch, where more warps would only
 // spend issue slots walking the instruction stream; 1024 for a few programs
@@ -485,8 +486,9 @@ int odd_xz_mode(int n, int d, long long programs, unsigned flags, size_t optin, 
   // for a few programs (latency) only where the byte tableau would sit in one
   // CTA and n >= 128.  On GB300, lone programs: d = 5, n = 180 1.27 ms packed
   // against 1.46 on one byte CTA, d = 3, n = 200 1.32 against 1.66; but
-  // d = 5, n = 256 4.32 against 3.16 on the byte cluster, d = 7, n = 600
-  // 11.5 against 5.6 on the streamed cluster, PR1 (n = 32) 0.31 against 0.26
+  // d = 5, n = 256 4.32 against 3.16 on the byte cluster (2.17 once it took
+  // one cluster barrier a measurement), d = 7, n = 600 11.5 against 5.6 on
+  // the streamed cluster, PR1 (n = 32) 0.31 against 0.26 (0.24 since)
   const bool packed = (d == 3 || d == 5 || d == 7) &&
                       !(flags & (SDIM_FLAG_U8_XZ | SDIM_FLAG_SPLIT_XZ | SDIM_FLAG_CLUSTER_XZ)) &&
                       (!few || (flags & SDIM_FLAG_PACKED_XZ) || (single && n >= 128));
