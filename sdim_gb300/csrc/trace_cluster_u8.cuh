@@ -25,7 +25,8 @@
 //     unexponentiated column and the factors scaled by the exponent e
 //     (x_k += (e f) cx_k is the update with the exponentiated column e cx),
 //     the phases, and the pivot columns.  A deterministic one needs no
-//     second barrier: each stabilizer CTA writes its slice sums to global
+//     second cluster barrier (a stabilizer CTA takes a CTA barrier once its
+//     rows are read): each stabilizer CTA writes its slice sums to global
 //     memory -- P_c = sum f_i c_i, the in-slice cross term A_c and
 //     D_c = sum f_i (f_i - 1) / 2 x_i.z_i as per-warp partials, and per row
 //     k the slice sums Z_c[k] = sum f_i z_k[i], X_c[k] = sum f_i x_k[i] --
@@ -526,6 +527,9 @@ __device__ void cluster_measure(ClusterU8<DD, K, kStream>& e, const TraceDescU8&
         part[1] = al;
         part[2] = dl;
       }
+      // every row was read across the slice's columns: the column owners
+      // may write them again (the next gate) only after this barrier
+      e.tm.sync();
     } else {
       for (int j = t; j < nc; j += size) row[e.g0 + j] = 0;
     }
