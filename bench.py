@@ -446,6 +446,13 @@ def u8_xz_layout(n, odd_trace_programs, smem_optin, num_sms=152, d=11):
     return 8, ("smem" if hot + r16(2 * n * sl) + win + 4096 <= smem_optin else "l2")
 
 
+def xz_kernel_name(mode):
+    """The odd-d x / z pass kernel of a sdim_trace_xz_mode form."""
+    return {0: "k_trace_pass_u8", 1: "k_trace_pass_split", 2: "k_trace_pass_u8", 3: "k_trace_pass_cluster",
+            4: "k_trace_pass_cluster", 5: "k_trace_pass_p3", 6: "k_trace_pass_p3", 7: "k_trace_pass_n4",
+            8: "k_trace_pass_n4"}.get(mode, "unknown")
+
+
 def tableau_place(n, d, on_trace, smem_optin, odd_trace_programs=1, num_sms=152):
     """Where a program's x / z tableau lives ("smem", "l2" or "hbm"): bit
     planes for d = 2 and the odd-d shot-group engine on one CTA, the odd-d
@@ -951,15 +958,19 @@ def run_single(args, torch, dist, ws, rank, local):
             sms, _ = u8_xz_layout(n, 1, ctx.smem_optin, ctx.num_sms, d)
             share = peak * sms / ctx.num_sms
             xz_ach = per_shot_bytes / (xz_ms / 1e3) / 1e9
-            xz_kernel = {1: {3: "k_trace_pass_p3", 5: "k_trace_pass_n4", 7: "k_trace_pass_n4"}.get(d, "k_trace_pass_u8"),
-                         2: "k_trace_pass_split",
-                         8: "k_trace_pass_cluster"}[sms]
+            xz_kernel = xz_kernel_name(ctx.lib.sdim_trace_xz_mode(n, d, 1, 0, ctx.smem_optin, ctx.num_sms))
             roofline = {"bound": f"smem (x/z pass, latency-bound on {sms} CTA{'s' if sms > 1 else ''})",
                         "achieved": xz_ach, "peak": share, "unit": "GB/s", "frac": xz_ach / share,
                         "traffic": read_traffic(f"trace_engine_{args.workload}.md"),
                         "traffic_source": "DRAM bytes of one step under ncu, read from profiles/ (not measured "
                                           "in this run)",
-                        "kernel": f"{xz_kernel}<{d}> (x/z pass), then k_phase_pass_u8<{d}>",
+                        "kernel": f"{xz_kernel}<{d}> (x/z pass{', with k_cluster_det_headers after it' if sms == 8 else ''}), "
+                                  f"then k_phase_pass_u8<{d}>",
+                        "xz_latency": {"ms": xz_ms, "measurements": spec.num_measurements(),
+                                       "us_per_measurement": 1e3 * xz_ms / max(spec.num_measurements(), 1),
+                                       "bound": "latency: the measurements run one after another, each with its "
+                                                "pivot search, barriers and rank-1 update or slice sums; the "
+                                                "gates between them are walked in order"},
                         "peak_source": f"sdim_probe_smem_bandwidth x {sms}/{ctx.num_sms} SMs",
                         "algorithmic_bytes_per_launch": per_shot_bytes,
                         "bytes_model": "per-instruction bytes of one tableau update (x/z pass: one tableau per program)",

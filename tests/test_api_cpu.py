@@ -182,6 +182,11 @@ def test_odd_d_xz_routing_and_its_bench_mirror():
     assert mode(100, 1, _lib.FLAG_CLUSTER_XZ | _lib.FLAG_FORCE_GMEM) == 4
     assert mode(100, 1, _lib.FLAG_FORCE_GMEM) == 2
     assert mode(100, 1, _lib.FLAG_SPLIT_XZ) == 1
+    # the bench names the x / z kernel of its lone programs from the same routing
+    assert bench.xz_kernel_name(mode(32, 1, 0, 3)) == "k_trace_pass_u8"  # PR1
+    assert bench.xz_kernel_name(mode(256, 1, 0, 5)) == "k_trace_pass_cluster"  # oddd5
+    assert bench.xz_kernel_name(mode(200, 1, 0, 3)) == "k_trace_pass_p3"
+    assert bench.xz_kernel_name(mode(200, 1, 0, 7)) == "k_trace_pass_n4"
     assert mode(0, 1) == _lib.SDIM_EINVAL and mode(2049, 1) == _lib.SDIM_EINVAL
     assert mode(10, 1, 0, 4) == _lib.SDIM_EINVAL
     packed = _lib.FLAG_PACKED_XZ
