@@ -2,7 +2,8 @@
 memory, or streamed from global memory) against the oracle and the other
 x / z passes: slices left empty (n < 4), every gate and noise channel,
 random outcomes, deterministic outcomes whose factors span every slice, the
-largest programs, and the default routing of mixed batches."""
+largest programs, the default routing of mixed batches, and the layered
+stream's gate groups against the gates applied one at a time."""
 import numpy as np
 import pytest
 
