@@ -272,8 +272,9 @@ int sdim_host_alloc(size_t bytes, void** out);
 int sdim_host_free(void* p);
 /* Milliseconds of the kernels of the last call made with SDIM_FLAG_TIME. */
 double sdim_last_kernel_ms(const sdim_ctx* ctx);
-/* The same span split by stage: out[0] the trace engine's x / z passes,
- * out[1] its phase passes, out[2] every other engine's kernels.  In a batch
+/* The same span split by stage: out[0] the trace engine's x / z passes
+ * (with the odd-d cluster's deterministic-header pass after them), out[1]
+ * its phase passes, out[2] every other engine's kernels.  In a batch
  * that has both, the shot-group engines run on their own stream beside the
  * trace engines: out[2] is then their own span, which overlaps out[0] and
  * out[1].  No counterpart in the reference (its shot loop is not staged). */
